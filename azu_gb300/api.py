@@ -1,0 +1,303 @@
+"""Python mirror of the reference's GPU-twin interfaces over the C ABI.
+
+  TSDFVolume     tsdf::TSDFVolume        (include/tsdf/TSDFVolume.h:69-190)
+  ICPTracker     tracking::ICPTracker    (include/tracking/ICPTracker.h:80-126)
+  Preprocessor   sensor::Preprocessor    (include/sensor/Preprocessor.h:23-113)
+  MarchingCubes  meshing::MarchingCubes  (include/meshing/MarchingCubes.h:35-62)
+  Pipeline       PipelineController's per-frame GPU body, lockstep
+
+Device buffers are torch CUDA tensors (plumbing only); every handle runs on
+the torch stream current at construction, so torch copies and library
+kernels are ordered on one stream. Poses are (4, 4) row-major float32.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import check
+
+FP = C.POINTER(C.c_float)
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("azu_gb300 needs a CUDA device (sm_103a); there is no CPU fallback")
+    return torch
+
+
+def _pose(p) -> C.Array:
+    a = np.ascontiguousarray(np.asarray(p, np.float32).reshape(16))
+    return (C.c_float * 16)(*a.tolist())
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream_handle():
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def volume_params(resolution, voxel_size, truncation, max_weight=64.0, origin=(0, 0, 0), min_depth=0.3,
+                  max_depth=2.5, format=_abi.AZU_TSDF_FP32, color=False) -> _abi.VolumeParams:
+    return _abi.VolumeParams(int(resolution), float(voxel_size), float(truncation), float(max_weight),
+                             (C.c_float * 3)(*[float(v) for v in origin]), float(min_depth), float(max_depth),
+                             int(format), int(bool(color)))
+
+
+def tracker_params(iters=(10, 5, 4), dist=0.1, angle=30.0, min_depth=0.3, max_depth=2.5, fx=525.0, fy=525.0,
+                   cx=319.5, cy=239.5, precision=0) -> _abi.TrackerParams:
+    return _abi.TrackerParams((C.c_int * 3)(*iters), float(dist), float(angle), float(min_depth),
+                              float(max_depth), float(fx), float(fy), float(cx), float(cy), int(precision))
+
+
+def result_dict(r: _abi.IcpResult) -> dict:
+    return dict(pose=np.array(r.pose, np.float32).reshape(4, 4), error=r.error, inliers=r.inliers,
+                converged=bool(r.converged), tracking_ok=bool(r.tracking_ok), final_step=r.final_step,
+                information=np.array(r.information, np.float32).reshape(6, 6),
+                valid_live_points=r.valid_live_points, valid_model_points=r.valid_model_points,
+                projected_points=r.projected_points, dist_filtered=r.dist_filtered,
+                angle_filtered=r.angle_filtered, iterations=list(r.iterations), status=r.status)
+
+
+class TSDFVolume:
+    def __init__(self, params: _abi.VolumeParams, device: int = 0):
+        self.lib = _abi.load()
+        self.device = device
+        self.h = C.c_void_p()
+        check(self.lib.azu_volume_create(device, C.byref(params), _stream_handle(), C.byref(self.h)),
+              "azu_volume_create")
+        self.params = params
+
+    def close(self):
+        if self.h:
+            self.lib.azu_volume_destroy(self.h)
+            self.h = C.c_void_p()
+
+    __del__ = close
+
+    @property
+    def n(self):
+        return self.params.resolution ** 3
+
+    def reset(self):
+        check(self.lib.azu_volume_reset(self.h), "reset")
+
+    def set_params(self, p):
+        check(self.lib.azu_volume_set_params(self.h, C.byref(p)), "set_params")
+        self.params = p
+
+    def integrate_gpu(self, d_depth, pose, K, W, H, min_depth, max_depth, d_rgb=None):
+        check(self.lib.azu_volume_integrate(self.h, _ptr(d_depth), _ptr(d_rgb), _pose(pose), *map(float, K), W, H,
+                                            float(min_depth), float(max_depth)), "integrate")
+
+    def integrate(self, depth_m: np.ndarray, pose, K, W, H, min_depth, max_depth, rgb=None):
+        d = np.ascontiguousarray(depth_m, np.float32)
+        c = None if rgb is None else np.ascontiguousarray(rgb, np.uint8)
+        check(self.lib.azu_volume_integrate_host(self.h, d.ctypes.data_as(C.c_void_p),
+                                                 None if c is None else c.ctypes.data_as(C.c_void_p), _pose(pose),
+                                                 *map(float, K), W, H, float(min_depth), float(max_depth)),
+              "integrate_host")
+
+    def raycast_gpu(self, pose, K, W, H, colors=False):
+        torch = _torch()
+        v = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+        n = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+        c = torch.empty((H, W, 3), dtype=torch.uint8, device="cuda") if colors else None
+        check(self.lib.azu_volume_raycast(self.h, _pose(pose), *map(float, K), W, H, _ptr(v), _ptr(n), _ptr(c)),
+              "raycast")
+        return v, n, c
+
+    def raycast(self, pose, K, W, H, colors=False):
+        v, n, c = self.raycast_gpu(pose, K, W, H, colors)
+        out = dict(vertices=v.cpu().numpy(), normals=n.cpu().numpy())
+        if colors:
+            out["colors"] = c.cpu().numpy()
+        return out
+
+    def stats(self) -> dict:
+        s = _abi.VolumeStats()
+        check(self.lib.azu_volume_get_stats(self.h, C.byref(s)), "stats")
+        return dict(integrated_frames=s.integrated_frames, observed_voxels=s.observed_voxels,
+                    last_voxels_updated=s.last_voxels_updated, last_color_updates=s.last_color_updates)
+
+    def download(self, color=False):
+        t = np.empty(self.n, np.float32)
+        w = np.empty(self.n, np.float32)
+        c = np.empty(3 * self.n, np.float32) if color else None
+        check(self.lib.azu_volume_download(self.h, t.ctypes.data_as(C.c_void_p), w.ctypes.data_as(C.c_void_p),
+                                           None if c is None else c.ctypes.data_as(C.c_void_p)), "download")
+        return (t, w, c) if color else (t, w)
+
+    def upload(self, tsdf, weight, color=None):
+        t = np.ascontiguousarray(tsdf, np.float32)
+        w = np.ascontiguousarray(weight, np.float32)
+        c = None if color is None else np.ascontiguousarray(color, np.float32)
+        check(self.lib.azu_volume_upload(self.h, t.ctypes.data_as(C.c_void_p), w.ctypes.data_as(C.c_void_p),
+                                         None if c is None else c.ctypes.data_as(C.c_void_p)), "upload")
+
+
+class ICPTracker:
+    def __init__(self, params: _abi.TrackerParams, device: int = 0):
+        self.lib = _abi.load()
+        self.h = C.c_void_p()
+        check(self.lib.azu_tracker_create(device, C.byref(params), _stream_handle(), C.byref(self.h)),
+              "azu_tracker_create")
+        self.params = params
+
+    def close(self):
+        if self.h:
+            self.lib.azu_tracker_destroy(self.h)
+            self.h = C.c_void_p()
+
+    __del__ = close
+
+    def prepare_live(self, d_depth, W, H):
+        check(self.lib.azu_tracker_prepare_live(self.h, _ptr(d_depth), W, H), "prepare_live")
+
+    def load_live(self, level, d_v, d_n, W, H):
+        check(self.lib.azu_tracker_load_live(self.h, level, _ptr(d_v), _ptr(d_n), W, H), "load_live")
+
+    def track_prepared(self, W, H, d_mv, d_mn, MW, MH, estimate, ref_pose) -> dict:
+        r = _abi.IcpResult()
+        check(self.lib.azu_tracker_track_prepared(self.h, W, H, _ptr(d_mv), _ptr(d_mn), MW, MH, _pose(estimate),
+                                                  _pose(ref_pose), C.byref(r)), "track_prepared")
+        return result_dict(r)
+
+    def build_system(self, level, d_mv, d_mn, MW, MH, pose, ref_pose) -> dict:
+        A = (C.c_float * 36)()
+        b = (C.c_float * 6)()
+        res = C.c_float()
+        cnt = (C.c_int * 6)()
+        check(self.lib.azu_tracker_build_system(self.h, level, _ptr(d_mv), _ptr(d_mn), MW, MH, _pose(pose),
+                                                _pose(ref_pose), A, b, C.byref(res), cnt), "build_system")
+        c = list(cnt)
+        return dict(A=np.array(A, np.float32).reshape(6, 6), b=np.array(b, np.float32), residual=res.value,
+                    inliers=c[0], valid_live=c[1], valid_model=c[2], projected=c[3], dist_filtered=c[4],
+                    angle_filtered=c[5])
+
+    def live_maps(self, level, W, H):
+        """(depth, vertices, normals) of a pyramid level as host arrays."""
+        v, n, d = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(self.lib.azu_tracker_live_maps(self.h, level, C.byref(v), C.byref(n), C.byref(d)), "live_maps")
+        w, h = W >> level, H >> level
+        return (device_to_host(d.value, (h, w), np.float32), device_to_host(v.value, (h, w, 3), np.float32),
+                device_to_host(n.value, (h, w, 3), np.float32))
+
+
+class _DevArray:
+    """A raw device pointer exposed through __cuda_array_interface__."""
+
+    def __init__(self, ptr, shape, dtype):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": np.dtype(dtype).str,
+                                         "data": (int(ptr), False), "version": 3}
+
+
+def device_to_host(ptr: int, shape, dtype) -> np.ndarray:
+    torch = _torch()
+    torch.cuda.current_stream().synchronize()
+    return torch.as_tensor(_DevArray(ptr, shape, dtype), device="cuda").cpu().numpy().copy()
+
+
+class Preprocessor:
+    def __init__(self, mode=_abi.AZU_PRE_FULL, device: int = 0):
+        self.lib = _abi.load()
+        self.h = C.c_void_p()
+        check(self.lib.azu_preprocessor_create(device, int(mode), _stream_handle(), C.byref(self.h)),
+              "azu_preprocessor_create")
+
+    def close(self):
+        if self.h:
+            self.lib.azu_preprocessor_destroy(self.h)
+            self.h = C.c_void_p()
+
+    __del__ = close
+
+    def reset(self):
+        check(self.lib.azu_preprocessor_reset(self.h), "reset")
+
+    def reset_temporal(self):
+        check(self.lib.azu_preprocessor_reset_temporal(self.h), "reset_temporal")
+
+    def process(self, depth_raw: np.ndarray, rgb: np.ndarray, min_depth, max_depth):
+        """RawFrame in place semantics: returns processed (depth, rgb) copies."""
+        d = np.ascontiguousarray(depth_raw, np.uint16).copy()
+        c = np.ascontiguousarray(rgb, np.uint8).copy()
+        check(self.lib.azu_preprocessor_process(self.h, d.ctypes.data_as(C.c_void_p), c.ctypes.data_as(C.c_void_p),
+                                                float(min_depth), float(max_depth)), "process")
+        return d, c
+
+    def device_outputs(self, W=640, H=480):
+        """(depth_m, depth_raw, luma, rgb) of the last frame as host arrays."""
+        L = self.lib
+        return (device_to_host(L.azu_preprocessor_depth_meters(self.h), (H, W), np.float32),
+                device_to_host(L.azu_preprocessor_depth_raw(self.h), (H, W), np.uint16),
+                device_to_host(L.azu_preprocessor_luma(self.h), (H, W), np.float32),
+                device_to_host(L.azu_preprocessor_rgb(self.h), (H, W, 3), np.uint8))
+
+
+class MarchingCubes:
+    def __init__(self, device: int = 0, max_triangles: int = 2_000_000):
+        self.lib = _abi.load()
+        self.h = C.c_void_p()
+        check(self.lib.azu_mesher_create(device, _stream_handle(), C.byref(self.h)), "azu_mesher_create")
+        self.set_max_triangles(max_triangles)
+
+    def close(self):
+        if self.h:
+            self.lib.azu_mesher_destroy(self.h)
+            self.h = C.c_void_p()
+
+    __del__ = close
+
+    def set_max_triangles(self, n):
+        check(self.lib.azu_mesher_set_max_triangles(self.h, C.c_int64(int(n))), "set_max_triangles")
+
+    def extract(self, vol: TSDFVolume) -> dict:
+        info = _abi.MeshInfo()
+        check(self.lib.azu_mesher_extract(self.h, vol.h, C.byref(info)), "extract")
+        nv, ni = info.n_vertices, info.n_indices
+        pos = np.empty((max(nv, 1), 3), np.float32)
+        nrm = np.empty((max(nv, 1), 3), np.float32)
+        col = np.empty((max(nv, 1), 3), np.uint8)
+        idx = np.empty(max(ni, 1), np.uint32)
+        check(self.lib.azu_mesher_copy_out(self.h, pos.ctypes.data_as(C.c_void_p), nrm.ctypes.data_as(C.c_void_p),
+                                           col.ctypes.data_as(C.c_void_p), idx.ctypes.data_as(C.c_void_p)),
+              "copy_out")
+        return dict(positions=pos[:nv], normals=nrm[:nv], colors=col[:nv], indices=idx[:ni],
+                    truncated=bool(info.truncated))
+
+
+def pipeline_params(volume: _abi.VolumeParams, tracker: _abi.TrackerParams, preprocess_mode=_abi.AZU_PRE_FULL,
+                    min_depth=0.3, max_depth=2.5, input_is_mm=False, use_graph=True) -> _abi.PipelineParams:
+    return _abi.PipelineParams(volume, tracker, int(preprocess_mode), float(min_depth), float(max_depth),
+                               int(bool(input_is_mm)), int(bool(use_graph)))
+
+
+class Pipeline:
+    def __init__(self, params: _abi.PipelineParams, device: int = 0):
+        self.lib = _abi.load()
+        self.h = C.c_void_p()
+        check(self.lib.azu_pipeline_create(device, C.byref(params), C.byref(self.h)), "azu_pipeline_create")
+
+    def close(self):
+        if self.h:
+            self.lib.azu_pipeline_destroy(self.h)
+            self.h = C.c_void_p()
+
+    __del__ = close
+
+    def process_frame(self, depth: np.ndarray, rgb: np.ndarray | None = None) -> dict:
+        r = _abi.FrameResult()
+        d = np.ascontiguousarray(depth, np.uint16)
+        c = None if rgb is None else np.ascontiguousarray(rgb, np.uint8)
+        check(self.lib.azu_pipeline_process_frame(self.h, d.ctypes.data_as(C.c_void_p),
+                                                  None if c is None else c.ctypes.data_as(C.c_void_p),
+                                                  C.byref(r)), "process_frame")
+        return dict(pose=np.array(r.pose, np.float32).reshape(4, 4), icp=result_dict(r.icp), quality=r.quality,
+                    integrated=bool(r.integrated), frame_index=r.frame_index)

@@ -1,0 +1,100 @@
+// Internal declarations shared by the translation units of libazu_gb300.so.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/azu_gpu.h"
+
+namespace azu {
+
+// Thread-local last-error text behind azu_last_error().
+void set_error(const char* fmt, ...);
+
+#define AZU_TRY_CUDA(expr)                                                                       \
+    do {                                                                                         \
+        cudaError_t e_ = (expr);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            ::azu::set_error("%s failed at %s:%d: %s", #expr, __FILE__, __LINE__,                \
+                             cudaGetErrorString(e_));                                            \
+            return e_ == cudaErrorMemoryAllocation ? AZU_E_NOMEM : AZU_E_CUDA;                   \
+        }                                                                                        \
+    } while (0)
+
+#define AZU_CHECK_ARG(cond, msg)                                                                 \
+    do {                                                                                         \
+        if (!(cond)) {                                                                           \
+            ::azu::set_error("invalid argument: %s", msg);                                       \
+            return AZU_E_INVALID;                                                                \
+        }                                                                                        \
+    } while (0)
+
+#define AZU_LAUNCH_CHECK() AZU_TRY_CUDA(cudaGetLastError())
+
+// Makes `device` current and checks that it is an sm_103 part.
+int bind_device(int device);
+
+// Stream owned or borrowed by a handle.
+struct StreamRef {
+    cudaStream_t s = nullptr;
+    bool owned = false;
+    int init(void* user) {
+        if (user) { s = static_cast<cudaStream_t>(user); owned = false; return AZU_OK; }
+        AZU_TRY_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        owned = true;
+        return AZU_OK;
+    }
+    void release() {
+        if (owned && s) cudaStreamDestroy(s);
+        s = nullptr;
+        owned = false;
+    }
+};
+
+// Error word written by bounded device-side waits (ICP grid barrier).
+enum : uint32_t { kDevErrNone = 0, kDevErrBarrierTimeout = 1 };
+
+// ---- volume -------------------------------------------------------------
+struct IntegrateConsts {
+    float R_wc[9];
+    float t_wc[3];
+    float step_x[3];
+    int x0, x1, y0, y1, z0, z1;
+    int valid;
+};
+
+struct RaycastConsts {
+    float R_cw[9];
+    float o[3];
+};
+
+}  // namespace azu
+
+struct azu_volume {
+    int device = 0;
+    azu_volume_params p{};
+    azu::StreamRef stream;
+    void* vox = nullptr;        // float2 (FP32) or uint32 (FP16) per voxel
+    float* color = nullptr;     // 3 floats per voxel when p.color
+    float* d_pose = nullptr;    // 16 floats: pose slot for host-pose calls
+    azu::IntegrateConsts* d_iconsts = nullptr;
+    unsigned long long* d_counters = nullptr;  // [0] newly observed (cumulative), [1] updated (last), [2] colour (last)
+    float* d_depth_stage = nullptr;            // host-depth staging (integrate_host)
+    uint8_t* d_rgb_stage = nullptr;
+    size_t stage_pixels = 0;
+    int integrated_frames = 0;
+};
+
+namespace azu {
+size_t voxel_bytes(int format);
+// Enqueue helpers shared with the pipeline (pose read from device memory).
+int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d_rgb, const float* d_pose,
+                         float fx, float fy, float cx, float cy, int W, int H, float min_d, float max_d,
+                         const int* d_gate, cudaStream_t s);
+int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, float cx, float cy, int W, int H,
+                       float* d_vertices, float* d_normals, uint8_t* d_colors, const int* d_gate, cudaStream_t s);
+// Writes a host pose into a device slot with a by-value kernel argument.
+int set_pose_async(float* d_pose, const float* pose, cudaStream_t s);
+}  // namespace azu

@@ -1,0 +1,981 @@
+// Coarse-to-fine point-to-plane ICP in one persistent kernel, behind the
+// azu_tracker_* C ABI. Semantics: src/tracking/ICPTracker.cpp:40-354 and the
+// numeric policy of include/tracking/ICPShared.h:34-110.
+//
+// One cooperative launch runs every level and iteration:
+//   1. each block accumulates the 21 + 6 normal-equation terms, the Huber loss
+//      and 6 counters over a slice of the level's interior pixels (projective
+//      association into the model image, one thread per pixel);
+//   2. warp shuffles, then shared memory, reduce them to one block partial,
+//      written to global memory;
+//   3. one grid barrier (bounded spin; a timeout sets an error word);
+//   4. every block reduces all block partials itself, in the same fixed order,
+//      and solves the damped 6x6 system itself — identical inputs and code give
+//      identical results in every block, so no second barrier is needed.
+// Partials are double-buffered by iteration parity.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "azu_internal.h"
+#include "kf_math.cuh"
+
+namespace azu {
+
+int launch_prepare_live(const float* d_depth, int W, int H, float fx, float fy, float cx, float cy, float* const V[3],
+                        float* const N[3], float* const D[3], cudaStream_t s);
+
+constexpr int kNF = 28;   // 21 A + 6 b + residual
+constexpr int kNI = 6;    // inliers, valid_live, valid_model, projected, dist_filtered, angle_filtered
+constexpr int kIcpThreads = 256;
+constexpr unsigned kSpinLimit = 1u << 22;
+
+constexpr float kHuberK = 0.02f;
+constexpr float kDampingDefault = 0.1f, kDampingLevel0 = 0.01f, kDampingEscalated = 1.0f;
+constexpr float kCondEscalate = 1e7f, kMinEigEscalate = 1e-4f;
+constexpr float kTranslationCapStep = 0.2f, kRotationCapStep = 0.5f;
+constexpr float kConvergenceStep = 5e-5f, kAcceptableFinalStep = 1e-3f;
+constexpr int kMinInliersForIteration = 10, kMinInliersForOk = 100;
+
+struct IcpLevel {
+    const float* v;
+    const float* n;
+    int W, H;
+};
+
+struct IcpArgs {
+    IcpLevel lv[3];
+    const float* mv;
+    const float* mn;
+    int MW, MH;
+    float fx, fy, cx, cy;  // camera intrinsics scaled to the model size
+    float dist2, angle_cos;
+    int iters[3];
+    int precision;
+    int build_level;  // >= 0: one association pass at this level, no solve
+    const float* d_estimate;
+    const float* d_ref;
+    const float* d_prev;  // non-null: grade, retry from prev on Failed (pipeline)
+    float* d_pose_out;    // non-null: final pose (pipeline: current pose, updated unless Failed)
+    azu_icp_result* d_result;
+    int* d_quality;
+    int* d_gate;          // set to 1 when the frame grades Good
+    double* partials;     // [2][nblocks][kNF]
+    int* ipartials;       // [2][nblocks][kNI]
+    unsigned* bar;        // [0] arrivals, [1] generation
+    unsigned* err;
+    float* build_out;     // build mode: A[36], b[6], residual, counts[6] (as int bits)
+};
+
+// ---------------------------------------------------------------------------
+// Grid barrier with a bounded spin. Co-residency comes from the cooperative
+// launch. After a timeout the error word is set and every later barrier
+// returns at once, so the kernel always finishes.
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ void grid_sync(unsigned* bar, unsigned* err, unsigned nblocks, unsigned& gen) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (ld_acquire(err) == 0) {
+            __threadfence();
+            const unsigned arrived = atomicAdd(&bar[0], 1u);
+            if (arrived == nblocks - 1) {
+                atomicExch(&bar[0], 0u);
+                __threadfence();
+                atomicAdd(&bar[1], 1u);
+            } else {
+                unsigned spins = 0;
+                while (ld_acquire(&bar[1]) == gen) {
+                    if (++spins > kSpinLimit) {
+                        atomicExch(err, kDevErrBarrierTimeout);
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+        }
+        gen += 1;
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Per-pixel association (ICPTracker.cpp:236-328).
+struct Rel {
+    float Rcw[9], Rrel[9];
+    F3 tcw, trel;
+};
+
+struct Acc {
+    float f[kNF];
+    int i[kNI];
+};
+
+__device__ __forceinline__ bool normal_valid(F3 n) { return finite3(n) && sqnorm3(n) > 0.9f; }
+
+__device__ __forceinline__ void associate(const IcpArgs& a, const Rel& r, const IcpLevel& L, int x, int y, Acc& acc) {
+    const int idx = y * L.W + x;
+    const F3 lv = mk3(__ldg(L.v + 3 * idx), __ldg(L.v + 3 * idx + 1), __ldg(L.v + 3 * idx + 2));
+    if (lv.z <= 0.001f || !finite3(lv)) return;
+    const F3 vr = add3(mv3(r.Rrel, lv), r.trel);
+    if (vr.z <= 0.001f) return;
+    acc.i[1]++;
+    const float inv_z = fd(1.0f, vr.z);
+    const float mxf = fa(fm(fm(a.fx, vr.x), inv_z), a.cx);
+    const float myf = fa(fm(fm(a.fy, vr.y), inv_z), a.cy);
+    int mx, my;
+    if (!floor_to_int(fa(mxf, 0.5f), &mx) || !floor_to_int(fa(myf, 0.5f), &my)) return;
+    if (mx < 0 || mx >= a.MW || my < 0 || my >= a.MH) return;
+    acc.i[3]++;
+    const int m = my * a.MW + mx;
+    const F3 mv = mk3(__ldg(a.mv + 3 * m), __ldg(a.mv + 3 * m + 1), __ldg(a.mv + 3 * m + 2));
+    const F3 mn = mk3(__ldg(a.mn + 3 * m), __ldg(a.mn + 3 * m + 1), __ldg(a.mn + 3 * m + 2));
+    if (!(finite3(mv) && sqnorm3(mv) > 1e-12f) || !normal_valid(mn)) return;
+    acc.i[2]++;
+    const F3 vw = add3(mv3(r.Rcw, lv), r.tcw);
+    const F3 dvm = sub3(vw, mv);
+    if (sqnorm3(dvm) > a.dist2) { acc.i[4]++; return; }
+    const F3 ln = mk3(__ldg(L.n + 3 * idx), __ldg(L.n + 3 * idx + 1), __ldg(L.n + 3 * idx + 2));
+    if (!normal_valid(ln)) return;
+    const F3 nw = mv3(r.Rcw, ln);
+    if (fabsf(dot3(nw, mn)) < a.angle_cos) { acc.i[5]++; return; }
+    const float err = dot3(mn, dvm);
+    if (!isfinite(err)) return;
+    const F3 nc = mtv3(r.Rcw, mn);
+    const F3 cr = cross3(lv, nc);
+    const float J[6] = {nc.x, nc.y, nc.z, cr.x, cr.y, cr.z};
+    if (!(isfinite(J[0]) && isfinite(J[1]) && isfinite(J[2]) && isfinite(J[3]) && isfinite(J[4]) && isfinite(J[5])))
+        return;
+    const float ae = fabsf(err);
+    const float w = (ae <= kHuberK) ? 1.0f : fd(kHuberK, ae);
+    const float we = fm(err, w);
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+#pragma unroll
+        for (int j = i; j < 6; ++j) {
+            acc.f[k] = fa(acc.f[k], fm(fm(w, J[i]), J[j]));
+            ++k;
+        }
+        acc.f[21 + i] = fs(acc.f[21 + i], fm(J[i], we));
+    }
+    const float loss = (ae <= kHuberK) ? fm(ae, ae) : fs(fm(fm(2.0f, kHuberK), ae), fm(kHuberK, kHuberK));
+    acc.f[27] = fa(acc.f[27], loss);
+    acc.i[0]++;
+}
+
+// Block reduction of one pass into global partial slot `slot`.
+__device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, double* s_red, int* s_ired) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    if (a.precision) {
+#pragma unroll
+        for (int k = 0; k < kNF; ++k) {
+            double v = acc.f[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) s_red[warp * kNF + k] = v;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kNF; ++k) {
+            float v = acc.f[k];
+            for (int o = 16; o > 0; o >>= 1) v = fa(v, __shfl_down_sync(0xffffffffu, v, o));
+            if (lane == 0) s_red[warp * kNF + k] = v;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kNI; ++k) {
+        int v = acc.i[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) s_ired[warp * kNI + k] = v;
+    }
+    __syncthreads();
+    const size_t base = (static_cast<size_t>(slot) * gridDim.x + blockIdx.x);
+    if (threadIdx.x < kNF) {
+        if (a.precision) {
+            double s = 0.0;
+            for (int w = 0; w < nw; ++w) s += s_red[w * kNF + threadIdx.x];
+            a.partials[base * kNF + threadIdx.x] = s;
+        } else {
+            float s = 0.0f;
+            for (int w = 0; w < nw; ++w) s = fa(s, static_cast<float>(s_red[w * kNF + threadIdx.x]));
+            a.partials[base * kNF + threadIdx.x] = static_cast<double>(s);
+        }
+    } else if (threadIdx.x < kNF + kNI) {
+        const int k = threadIdx.x - kNF;
+        int s = 0;
+        for (int w = 0; w < nw; ++w) s += s_ired[w * kNI + k];
+        a.ipartials[base * kNI + k] = s;
+    }
+    __syncthreads();
+}
+
+// Every block: sum all block partials of `slot` in a fixed order.
+__device__ void reduce_grid(const IcpArgs& a, int slot, double* s_sum, int* s_isum) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    const int nb = gridDim.x;
+    const size_t base = static_cast<size_t>(slot) * nb;
+    for (int k = warp; k < kNF + kNI; k += nw) {
+        if (k < kNF) {
+            if (a.precision) {
+                double s = 0.0;
+                for (int b = lane; b < nb; b += 32) s += __ldcg(a.partials + (base + b) * kNF + k);
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+                if (lane == 0) s_sum[k] = s;
+            } else {
+                float s = 0.0f;
+                for (int b = lane; b < nb; b += 32) s = fa(s, static_cast<float>(__ldcg(a.partials + (base + b) * kNF + k)));
+                for (int o = 16; o > 0; o >>= 1) s = fa(s, __shfl_down_sync(0xffffffffu, s, o));
+                if (lane == 0) s_sum[k] = static_cast<double>(s);
+            }
+        } else {
+            const int kk = k - kNF;
+            int s = 0;
+            for (int b = lane; b < nb; b += 32) s += __ldcg(a.ipartials + (base + b) * kNI + kk);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0) s_isum[kk] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// 6x6 symmetric eigenvalues by a parallel cyclic Jacobi sweep on one warp
+// (round-robin pairing: 5 rounds of 3 disjoint rotations per sweep).
+__constant__ int kPairs[5][3][2] = {{{0, 1}, {2, 5}, {3, 4}}, {{0, 2}, {1, 3}, {4, 5}}, {{0, 3}, {2, 4}, {1, 5}},
+                                    {{0, 4}, {3, 5}, {1, 2}}, {{0, 5}, {1, 4}, {2, 3}}};
+
+__device__ void warp_eig6(float* m /* smem 36, destroyed */, float* cs /* smem 12 */, float& mn, float& mx) {
+    const int lane = threadIdx.x & 31;
+    for (int sweep = 0; sweep < 8; ++sweep) {
+        for (int r = 0; r < 5; ++r) {
+            if (lane < 3) {
+                const int p = kPairs[r][lane][0], q = kPairs[r][lane][1];
+                const float apq = m[p * 6 + q];
+                float c = 1.0f, s = 0.0f;
+                if (apq != 0.0f) {
+                    const float theta = (m[q * 6 + q] - m[p * 6 + p]) / (2.0f * apq);
+                    const float t = (theta >= 0.0f ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+                    c = rsqrtf(t * t + 1.0f);
+                    s = t * c;
+                }
+                cs[4 * lane] = c;
+                cs[4 * lane + 1] = s;
+            }
+            __syncwarp();
+            // rows
+            float nv[2];
+            for (int h = 0; h < 2; ++h) {
+                const int e = lane + 32 * h;
+                if (e < 36) {
+                    const int i = e / 6, k = e % 6;
+                    int pi = 0;
+                    for (int t = 0; t < 3; ++t)
+                        if (kPairs[r][t][0] == i || kPairs[r][t][1] == i) pi = t;
+                    const int p = kPairs[r][pi][0], q = kPairs[r][pi][1];
+                    const float c = cs[4 * pi], s = cs[4 * pi + 1];
+                    nv[h] = (i == p) ? c * m[p * 6 + k] - s * m[q * 6 + k] : s * m[p * 6 + k] + c * m[q * 6 + k];
+                }
+            }
+            __syncwarp();
+            for (int h = 0; h < 2; ++h) if (lane + 32 * h < 36) m[lane + 32 * h] = nv[h];
+            __syncwarp();
+            // columns
+            for (int h = 0; h < 2; ++h) {
+                const int e = lane + 32 * h;
+                if (e < 36) {
+                    const int k = e / 6, j = e % 6;
+                    int pj = 0;
+                    for (int t = 0; t < 3; ++t)
+                        if (kPairs[r][t][0] == j || kPairs[r][t][1] == j) pj = t;
+                    const int p = kPairs[r][pj][0], q = kPairs[r][pj][1];
+                    const float c = cs[4 * pj], s = cs[4 * pj + 1];
+                    nv[h] = (j == p) ? c * m[k * 6 + p] - s * m[k * 6 + q] : s * m[k * 6 + p] + c * m[k * 6 + q];
+                }
+            }
+            __syncwarp();
+            for (int h = 0; h < 2; ++h) if (lane + 32 * h < 36) m[lane + 32 * h] = nv[h];
+            __syncwarp();
+        }
+    }
+    float lo = m[0], hi = m[0];
+    for (int i = 1; i < 6; ++i) {
+        lo = fminf(lo, m[i * 7]);
+        hi = fmaxf(hi, m[i * 7]);
+    }
+    mn = lo;
+    mx = hi;
+}
+
+// A x = b by LDL^T with symmetric diagonal pivoting (float, one thread).
+__device__ void ldlt_solve_f(const float* Ain, const float* b, float* x) {
+    float A[36], L[36], D[6], y[6], z[6];
+    int perm[6] = {0, 1, 2, 3, 4, 5};
+    for (int i = 0; i < 36; ++i) { A[i] = Ain[i]; L[i] = 0.0f; }
+    for (int k = 0; k < 6; ++k) {
+        int p = k;
+        for (int i = k + 1; i < 6; ++i) if (fabsf(A[i * 6 + i]) > fabsf(A[p * 6 + p])) p = i;
+        if (p != k) {
+            for (int j = 0; j < 6; ++j) { const float t = A[k * 6 + j]; A[k * 6 + j] = A[p * 6 + j]; A[p * 6 + j] = t; }
+            for (int i = 0; i < 6; ++i) { const float t = A[i * 6 + k]; A[i * 6 + k] = A[i * 6 + p]; A[i * 6 + p] = t; }
+            for (int j = 0; j < k; ++j) { const float t = L[k * 6 + j]; L[k * 6 + j] = L[p * 6 + j]; L[p * 6 + j] = t; }
+            const int t = perm[k]; perm[k] = perm[p]; perm[p] = t;
+        }
+        D[k] = A[k * 6 + k];
+        L[k * 6 + k] = 1.0f;
+        for (int i = k + 1; i < 6; ++i) L[i * 6 + k] = fd(A[i * 6 + k], D[k]);
+        for (int i = k + 1; i < 6; ++i)
+            for (int j = k + 1; j <= i; ++j) {
+                A[i * 6 + j] = fs(A[i * 6 + j], fm(L[i * 6 + k], A[j * 6 + k]));
+                A[j * 6 + i] = A[i * 6 + j];
+            }
+        for (int i = k + 1; i < 6; ++i) A[i * 6 + k] = A[k * 6 + i] = 0.0f;
+    }
+    for (int i = 0; i < 6; ++i) {
+        float s = b[perm[i]];
+        for (int j = 0; j < i; ++j) s = fs(s, fm(L[i * 6 + j], y[j]));
+        y[i] = s;
+    }
+    for (int i = 0; i < 6; ++i) y[i] = fd(y[i], D[i]);
+    for (int i = 5; i >= 0; --i) {
+        float s = y[i];
+        for (int j = i + 1; j < 6; ++j) s = fs(s, fm(L[j * 6 + i], z[j]));
+        z[i] = s;
+    }
+    for (int i = 0; i < 6; ++i) x[perm[i]] = z[i];
+}
+
+// A x = b by Cholesky in double (precision form).
+__device__ bool chol_solve_d(const double* Ain, const double* b, double* x) {
+    double L[36];
+    for (int i = 0; i < 36; ++i) L[i] = 0.0;
+    for (int j = 0; j < 6; ++j) {
+        double s = Ain[j * 6 + j];
+        for (int k = 0; k < j; ++k) s -= L[j * 6 + k] * L[j * 6 + k];
+        if (!(s > 0.0)) return false;
+        const double d = sqrt(s);
+        L[j * 6 + j] = d;
+        for (int i = j + 1; i < 6; ++i) {
+            double t = Ain[i * 6 + j];
+            for (int k = 0; k < j; ++k) t -= L[i * 6 + k] * L[j * 6 + k];
+            L[i * 6 + j] = t / d;
+        }
+    }
+    double y[6];
+    for (int i = 0; i < 6; ++i) {
+        double s = b[i];
+        for (int k = 0; k < i; ++k) s -= L[i * 6 + k] * y[k];
+        y[i] = s / L[i * 6 + i];
+    }
+    for (int i = 5; i >= 0; --i) {
+        double s = y[i];
+        for (int k = i + 1; k < 6; ++k) s -= L[k * 6 + i] * x[k];
+        x[i] = s / L[i * 6 + i];
+    }
+    return true;
+}
+
+// Nearest rotation (orthogonal polar factor, = U V^T of the SVD for det > 0)
+// by Newton's iteration R <- (R + R^-T) / 2 in double.
+__device__ void project_so3(float* P /* row-major 4x4, rotation block replaced */) {
+    double R[9];
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) R[3 * i + j] = P[4 * i + j];
+    for (int it = 0; it < 6; ++it) {
+        const double c00 = R[4] * R[8] - R[5] * R[7], c01 = R[5] * R[6] - R[3] * R[8], c02 = R[3] * R[7] - R[4] * R[6];
+        const double c10 = R[2] * R[7] - R[1] * R[8], c11 = R[0] * R[8] - R[2] * R[6], c12 = R[1] * R[6] - R[0] * R[7];
+        const double c20 = R[1] * R[5] - R[2] * R[4], c21 = R[2] * R[3] - R[0] * R[5], c22 = R[0] * R[4] - R[1] * R[3];
+        const double det = R[0] * c00 + R[1] * c01 + R[2] * c02;
+        const double id = 1.0 / det;  // R^-T = cofactor / det
+        const double N[9] = {0.5 * (R[0] + c00 * id), 0.5 * (R[1] + c01 * id), 0.5 * (R[2] + c02 * id),
+                             0.5 * (R[3] + c10 * id), 0.5 * (R[4] + c11 * id), 0.5 * (R[5] + c12 * id),
+                             0.5 * (R[6] + c20 * id), 0.5 * (R[7] + c21 * id), 0.5 * (R[8] + c22 * id)};
+        for (int k = 0; k < 9; ++k) R[k] = N[k];
+    }
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) P[4 * i + j] = static_cast<float>(R[3 * i + j]);
+}
+
+// Rodrigues rotation (Eigen::AngleAxisf::toRotationMatrix) into a row-major 3x3.
+__device__ void angle_axis(float angle, F3 axis, float* r) {
+    const float s = sinf(angle), c = cosf(angle);
+    const F3 sa = mul3(axis, s);
+    const F3 ca = mul3(axis, fs(1.0f, c));
+    float t = fm(ca.x, axis.y);
+    r[1] = fs(t, sa.z); r[3] = fa(t, sa.z);
+    t = fm(ca.x, axis.z);
+    r[2] = fa(t, sa.y); r[6] = fs(t, sa.y);
+    t = fm(ca.y, axis.z);
+    r[5] = fs(t, sa.x); r[7] = fa(t, sa.x);
+    r[0] = fa(fm(ca.x, axis.x), c); r[4] = fa(fm(ca.y, axis.y), c); r[8] = fa(fm(ca.z, axis.z), c);
+}
+
+struct LevelState {
+    float pose[16];
+    float error, final_step;
+    int inliers, converged;
+    float information[36];
+    int counts[6];  // valid_live .. angle_filtered (index 1..5 used)
+    int iters;
+};
+
+// Shared-memory scratch of the solve.
+struct SolveSmem {
+    double sum[kNF];
+    int isum[kNI];
+    float m[36];
+    float cs[12];
+    int action;  // 0 continue, 1 stop level
+};
+
+// One solve from the reduced sums (ICPTracker.cpp:78-131), executed by warp 0.
+__device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelState& st) {
+    const int lane = threadIdx.x & 31;
+    const int inl = sm.isum[0];
+    if (lane == 0) {
+        for (int k = 1; k < 6; ++k) st.counts[k] = sm.isum[k];
+        sm.action = (inl <= 0 || inl < kMinInliersForIteration) ? 1 : 0;
+        if (sm.action == 0) {
+            int k = 0;
+            for (int i = 0; i < 6; ++i)
+                for (int j = i; j < 6; ++j) {
+                    const float v = static_cast<float>(sm.sum[k++]);
+                    st.information[i * 6 + j] = v;
+                    st.information[j * 6 + i] = v;
+                }
+            for (int i = 0; i < 36; ++i) sm.m[i] = st.information[i];
+        }
+    }
+    __syncwarp();
+    if (sm.action != 0) return;
+    float mn, mx;
+    warp_eig6(sm.m, sm.cs, mn, mx);
+    if (lane != 0) return;
+    float damp = (level == 0) ? kDampingLevel0 : kDampingDefault;
+    if (!isfinite(mn) || !isfinite(mx) || mn < kMinEigEscalate) damp = kDampingEscalated;
+    else if (mx > kCondEscalate * mn) damp = kDampingEscalated;
+    float x[6];
+    if (a.precision) {
+        double A[36], b[6], xd[6];
+        int k = 0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j) { A[i * 6 + j] = A[j * 6 + i] = sm.sum[k++]; }
+        for (int i = 0; i < 6; ++i) { A[i * 6 + i] += damp; b[i] = sm.sum[21 + i]; }
+        if (!chol_solve_d(A, b, xd)) { sm.action = 1; return; }
+        for (int i = 0; i < 6; ++i) x[i] = static_cast<float>(xd[i]);
+    } else {
+        float A[36], b[6];
+        for (int i = 0; i < 36; ++i) A[i] = st.information[i];
+        for (int i = 0; i < 6; ++i) { A[i * 6 + i] = fa(A[i * 6 + i], damp); b[i] = static_cast<float>(sm.sum[21 + i]); }
+        ldlt_solve_f(A, b, x);
+    }
+    bool fin = true;
+    for (int i = 0; i < 6; ++i) fin = fin && isfinite(x[i]);
+    const float tn = norm3(mk3(x[0], x[1], x[2])), rn = norm3(mk3(x[3], x[4], x[5]));
+    if (!fin || tn > kTranslationCapStep || rn > kRotationCapStep) { sm.action = 1; return; }
+    float ss = 0.0f;
+    for (int i = 0; i < 6; ++i) ss = fa(ss, fm(x[i], x[i]));
+    const float step_norm = fsq(ss);
+    const float rx = x[3], ry = x[4], rz = x[5];
+    float delta[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    const float angle = fsq(fa(fa(fm(rx, rx), fm(ry, ry)), fm(rz, rz)));
+    float R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (angle > 1e-4f) {
+        F3 axis = mk3(rx, ry, rz);
+        axis = div3(axis, norm3(axis));
+        angle_axis(angle, axis, R);
+    } else {
+        R[1] = -rz; R[2] = ry; R[3] = rz; R[5] = -rx; R[6] = -ry; R[7] = rx;
+    }
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) delta[4 * i + j] = R[3 * i + j];
+    delta[3] = x[0]; delta[7] = x[1]; delta[11] = x[2];
+    float P[16];
+    if (a.precision) {
+        // SE(3) composition in double.
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 4; ++k) s += static_cast<double>(st.pose[4 * i + k]) * delta[4 * k + j];
+                P[4 * i + j] = static_cast<float>(s);
+            }
+    } else {
+        mm4(st.pose, delta, P);
+    }
+    project_so3(P);
+    for (int i = 0; i < 16; ++i) st.pose[i] = P[i];
+    st.final_step = step_norm;
+    st.error = fd(static_cast<float>(sm.sum[27]), static_cast<float>(inl > 1 ? inl : 1));
+    st.inliers = inl;
+    st.iters++;
+    if (step_norm < kConvergenceStep) {
+        st.converged = 1;
+        sm.action = 1;
+    }
+}
+
+__device__ void compute_rel(const float* pose, const float* ref_inv, Rel& r) {
+    rot_of(pose, r.Rcw);
+    r.tcw = trans_of(pose);
+    float Rrc[9];
+    rot_of(ref_inv, Rrc);
+    const F3 trc = trans_of(ref_inv);
+    mm3(Rrc, r.Rcw, r.Rrel);
+    r.trel = add3(mv3(Rrc, r.tcw), trc);
+}
+
+// classifyTracking (TrackingPolicy.h:70-112): 0 Good, 1 Poor, 2 Failed.
+__device__ int classify(const azu_icp_result& r, const float* prev) {
+    bool fin = true;
+    for (int i = 0; i < 16; ++i) fin = fin && isfinite(r.pose[i]);
+    if (!fin || !isfinite(r.error) || r.inliers < kMinInliersForOk) return 2;
+    const float fit = r.valid_model_points > 0 ? fd(float(r.inliers), float(r.valid_model_points)) : 0.0f;
+    const float rms = fsq(fmaxf(0.0f, r.error));
+    const int q = (r.inliers >= 2000 && fit >= 0.40f && rms <= 0.015f) ? 0 : 1;
+    float pinv[16], d[16];
+    inverse4(prev, pinv);
+    mm4(pinv, r.pose, d);
+    const float trans = norm3(trans_of(d));
+    const float tr = fa(fa(d[0], d[5]), d[10]);
+    const float c = fmaxf(-1.0f, fminf(1.0f, fm(fs(tr, 1.0f), 0.5f)));
+    const float ang = acosf(c);
+    if (!(trans <= 0.15f && ang <= 0.52f)) return 2;
+    return q;
+}
+
+__global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
+    __shared__ double s_red[(kIcpThreads / 32) * kNF];
+    __shared__ int s_ired[(kIcpThreads / 32) * kNI];
+    __shared__ SolveSmem sm;
+    __shared__ LevelState st;
+    __shared__ Rel s_rel;
+    __shared__ float s_refinv[16];
+    __shared__ unsigned s_gen;
+    __shared__ float s_start[16];
+    __shared__ azu_icp_result s_res;
+    __shared__ int s_retry;
+
+    if (threadIdx.x == 0) {
+        s_gen = ld_acquire(&a.bar[1]);
+        float ref[16];
+        for (int i = 0; i < 16; ++i) ref[i] = a.d_ref[i];
+        inverse4(ref, s_refinv);
+        for (int i = 0; i < 16; ++i) s_start[i] = a.d_estimate[i];
+    }
+    __syncthreads();
+    unsigned gen = s_gen;
+    int slot = 0;
+
+    if (a.build_level >= 0) {  // single association pass (parity probe)
+        const IcpLevel L = a.lv[a.build_level];
+        if (threadIdx.x == 0) compute_rel(s_start, s_refinv, s_rel);
+        __syncthreads();
+        const Rel rel = s_rel;
+        Acc acc;
+        for (int k = 0; k < kNF; ++k) acc.f[k] = 0.0f;
+        for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
+        const int iw = L.W - 2, ih = L.H - 2;
+        const int n = iw > 0 && ih > 0 ? iw * ih : 0;
+        for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+            associate(a, rel, L, 1 + p % iw, 1 + p / iw, acc);
+        reduce_block(a, acc, 0, s_red, s_ired);
+        grid_sync(a.bar, a.err, gridDim.x, gen);
+        reduce_grid(a, 0, sm.sum, sm.isum);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            int k = 0;
+            for (int i = 0; i < 6; ++i)
+                for (int j = i; j < 6; ++j) {
+                    const float v = static_cast<float>(sm.sum[k++]);
+                    a.build_out[i * 6 + j] = v;
+                    a.build_out[j * 6 + i] = v;
+                }
+            for (int i = 0; i < 6; ++i) a.build_out[36 + i] = static_cast<float>(sm.sum[21 + i]);
+            a.build_out[42] = static_cast<float>(sm.sum[27]);
+            for (int i = 0; i < 6; ++i) reinterpret_cast<int*>(a.build_out)[43 + i] = sm.isum[i];
+        }
+        return;
+    }
+
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        // ICPTracker::track (ICPTracker.cpp:40-66); thread 0 keeps the result.
+        if (threadIdx.x == 0) {
+            for (int i = 0; i < 16; ++i) s_res.pose[i] = (attempt == 0) ? s_start[i] : a.d_prev[i];
+            s_res.error = 0.0f; s_res.inliers = 0; s_res.converged = 0;
+            s_res.final_step = __int_as_float(0x7f800000);
+            for (int i = 0; i < 36; ++i) s_res.information[i] = 0.0f;
+            s_res.valid_live_points = s_res.valid_model_points = s_res.projected_points = 0;
+            s_res.dist_filtered = s_res.angle_filtered = 0;
+            for (int l = 0; l < 3; ++l) s_res.iterations[l] = 0;
+        }
+        __syncthreads();
+        for (int level = 2; level >= 0; --level) {
+            const int max_iter = a.iters[level];
+            if (max_iter <= 0) continue;
+            const IcpLevel L = a.lv[level];
+            if (threadIdx.x == 0) {
+                for (int i = 0; i < 16; ++i) st.pose[i] = s_res.pose[i];
+                st.error = 0.0f;
+                st.final_step = __int_as_float(0x7f800000);
+                st.inliers = 0;
+                st.converged = 0;
+                for (int i = 0; i < 36; ++i) st.information[i] = 0.0f;
+                for (int i = 0; i < 6; ++i) st.counts[i] = 0;
+                st.iters = 0;
+            }
+            __syncthreads();
+            const int iw = L.W - 2, ih = L.H - 2;
+            const int n = iw > 0 && ih > 0 ? iw * ih : 0;
+            for (int iter = 0; iter < max_iter; ++iter) {
+                if (threadIdx.x == 0) compute_rel(st.pose, s_refinv, s_rel);
+                __syncthreads();
+                const Rel rel = s_rel;
+                Acc acc;
+#pragma unroll
+                for (int k = 0; k < kNF; ++k) acc.f[k] = 0.0f;
+#pragma unroll
+                for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
+                for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+                    associate(a, rel, L, 1 + p % iw, 1 + p / iw, acc);
+                reduce_block(a, acc, slot, s_red, s_ired);
+                grid_sync(a.bar, a.err, gridDim.x, gen);
+                reduce_grid(a, slot, sm.sum, sm.isum);
+                slot ^= 1;
+                if (threadIdx.x < 32) solve_step(a, level, sm, st);
+                __syncthreads();
+                if (sm.action != 0) break;
+            }
+            // track(): the level result replaces the running one; final_step
+            // carries the last finite value.
+            if (threadIdx.x == 0) {
+                const float carried = s_res.final_step;
+                for (int i = 0; i < 16; ++i) s_res.pose[i] = st.pose[i];
+                s_res.error = st.error;
+                s_res.inliers = st.inliers;
+                s_res.converged = st.converged;
+                s_res.final_step = isfinite(st.final_step) ? st.final_step : carried;
+                for (int i = 0; i < 36; ++i) s_res.information[i] = st.information[i];
+                s_res.valid_live_points = st.counts[1];
+                s_res.valid_model_points = st.counts[2];
+                s_res.projected_points = st.counts[3];
+                s_res.dist_filtered = st.counts[4];
+                s_res.angle_filtered = st.counts[5];
+                s_res.iterations[level] = st.iters;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            bool pf = true;
+            for (int i = 0; i < 16; ++i) pf = pf && isfinite(s_res.pose[i]);
+            s_res.tracking_ok = pf && s_res.inliers > kMinInliersForOk &&
+                                (s_res.converged || s_res.final_step <= kAcceptableFinalStep);
+            s_res.status = 0;
+            s_retry = (a.d_prev != nullptr && attempt == 0 && classify(s_res, a.d_prev) == 2) ? 1 : 0;
+        }
+        __syncthreads();
+        if (!s_retry) break;
+    }
+
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        azu_icp_result res = s_res;
+        res.status = ld_acquire(a.err) ? AZU_E_TIMEOUT : AZU_OK;
+        *a.d_result = res;
+        if (a.d_prev) {
+            const int q = classify(res, a.d_prev);
+            if (a.d_quality) *a.d_quality = q;
+            if (a.d_gate) *a.d_gate = (q == 0) ? 1 : 0;
+            if (a.d_pose_out) {
+                if (q != 2) for (int i = 0; i < 16; ++i) a.d_pose_out[i] = res.pose[i];
+                else for (int i = 0; i < 16; ++i) a.d_pose_out[i] = a.d_prev[i];
+            }
+        } else if (a.d_pose_out) {
+            for (int i = 0; i < 16; ++i) a.d_pose_out[i] = res.pose[i];
+        }
+    }
+}
+
+}  // namespace azu
+
+// ---------------------------------------------------------------------------
+struct azu_tracker {
+    int device = 0;
+    azu_tracker_params p{};
+    azu::StreamRef stream;
+    float* V[3] = {nullptr, nullptr, nullptr};
+    float* N[3] = {nullptr, nullptr, nullptr};
+    float* D[3] = {nullptr, nullptr, nullptr};
+    int W = 0, H = 0;
+    bool prepared = false;
+    int nblocks = 0;
+    double* partials = nullptr;
+    int* ipartials = nullptr;
+    unsigned* bar = nullptr;  // [0] arrivals [1] generation [2] error
+    float* d_est = nullptr;   // 16 estimate, 16 ref, 16 prev
+    azu_icp_result* d_result = nullptr;
+    float* d_build = nullptr;
+};
+
+namespace azu {
+
+static azu_tracker_params sanitize(const azu_tracker_params& in) {
+    azu_tracker_params p = in;
+    if (!std::isfinite(p.angle_threshold)) p.angle_threshold = 30.0f;
+    else if (p.angle_threshold < 0.0f) p.angle_threshold = 0.0f;
+    else if (p.angle_threshold > 85.0f) p.angle_threshold = 85.0f;
+    return p;
+}
+
+static int alloc_levels(azu_tracker* t, int W, int H) {
+    for (int l = 0; l < 3; ++l) {
+        if (t->V[l]) cudaFree(t->V[l]);
+        if (t->N[l]) cudaFree(t->N[l]);
+        if (t->D[l]) cudaFree(t->D[l]);
+        t->V[l] = t->N[l] = t->D[l] = nullptr;
+    }
+    for (int l = 0; l < 3; ++l) {
+        const size_t n = static_cast<size_t>(W >> l) * (H >> l);
+        AZU_TRY_CUDA(cudaMalloc(&t->V[l], n * 3 * sizeof(float)));
+        AZU_TRY_CUDA(cudaMalloc(&t->N[l], n * 3 * sizeof(float)));
+        AZU_TRY_CUDA(cudaMalloc(&t->D[l], n * sizeof(float)));
+    }
+    t->W = W;
+    t->H = H;
+    return AZU_OK;
+}
+
+// Fills the launch arguments; the caller sets pose pointers and outputs.
+static void fill_args(azu_tracker* t, IcpArgs& a, const float* mv, const float* mn, int MW, int MH) {
+    std::memset(&a, 0, sizeof(a));
+    for (int l = 0; l < 3; ++l) a.lv[l] = IcpLevel{t->V[l], t->N[l], t->W >> l, t->H >> l};
+    a.mv = mv;
+    a.mn = mn;
+    a.MW = MW;
+    a.MH = MH;
+    // scaleIntrinsics (include/sensor/CameraIntrinsics.h:33-40) to the model size.
+    const azu_tracker_params& p = t->p;
+    if (MW == 640 && MH == 480) {
+        a.fx = p.fx; a.fy = p.fy; a.cx = p.cx; a.cy = p.cy;
+    } else {
+        const float sx = static_cast<float>(MW) / 640.0f, sy = static_cast<float>(MH) / 480.0f;
+        a.fx = p.fx * sx; a.fy = p.fy * sy; a.cx = (p.cx + 0.5f) * sx - 0.5f; a.cy = (p.cy + 0.5f) * sy - 0.5f;
+    }
+    a.dist2 = p.dist_threshold * p.dist_threshold;
+    a.angle_cos = static_cast<float>(std::cos(p.angle_threshold * M_PI / 180.0f));
+    for (int l = 0; l < 3; ++l) a.iters[l] = p.max_iterations[l];
+    a.precision = p.precision;
+    a.build_level = -1;
+    a.partials = t->partials;
+    a.ipartials = t->ipartials;
+    a.bar = t->bar;
+    a.err = t->bar + 2;
+}
+
+int icp_launch(azu_tracker* t, const IcpArgs& a, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(t->nblocks);
+    cfg.blockDim = dim3(kIcpThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    AZU_TRY_CUDA(cudaLaunchKernelEx(&cfg, icp_kernel, a));
+    return AZU_OK;
+}
+
+// Pipeline entry: track against device poses; result/grade stay on the device.
+int tracker_track_dev(azu_tracker* t, const float* mv, const float* mn, int MW, int MH, const float* d_estimate,
+                      const float* d_ref, const float* d_prev, float* d_pose_out, azu_icp_result* d_result,
+                      int* d_quality, int* d_gate, cudaStream_t s) {
+    IcpArgs a;
+    fill_args(t, a, mv, mn, MW, MH);
+    a.d_estimate = d_estimate;
+    a.d_ref = d_ref;
+    a.d_prev = d_prev;
+    a.d_pose_out = d_pose_out;
+    a.d_result = d_result;
+    a.d_quality = d_quality;
+    a.d_gate = d_gate;
+    return icp_launch(t, a, s);
+}
+
+int tracker_prepare_dev(azu_tracker* t, const float* d_depth, int W, int H, cudaStream_t s) {
+    return launch_prepare_live(d_depth, W, H, t->p.fx, t->p.fy, t->p.cx, t->p.cy, t->V, t->N, t->D, s);
+}
+
+}  // namespace azu
+
+using namespace azu;
+
+extern "C" int azu_tracker_create(int device, const azu_tracker_params* p, void* stream, azu_tracker** out) {
+    AZU_CHECK_ARG(out != nullptr && p != nullptr, "null argument");
+    *out = nullptr;
+    for (int l = 0; l < 3; ++l) AZU_CHECK_ARG(p->max_iterations[l] >= 0 && p->max_iterations[l] <= 1000, "max_iterations");
+    if (int rc = bind_device(device)) return rc;
+    azu_tracker* t = new azu_tracker();
+    t->device = device;
+    t->p = sanitize(*p);
+    int rc = t->stream.init(stream);
+    int sms = 0, occ = 0;
+    if (!rc) {
+        cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, icp_kernel, kIcpThreads, 0);
+        if (e != cudaSuccess || occ < 1) { set_error("ICP occupancy query failed"); rc = AZU_E_CUDA; }
+    }
+    if (!rc) {
+        t->nblocks = sms * std::min(occ, 2);
+        cudaError_t e = cudaMalloc(&t->partials, sizeof(double) * 2 * t->nblocks * kNF);
+        if (e == cudaSuccess) e = cudaMalloc(&t->ipartials, sizeof(int) * 2 * t->nblocks * kNI);
+        if (e == cudaSuccess) e = cudaMalloc(&t->bar, sizeof(unsigned) * 4);
+        if (e == cudaSuccess) e = cudaMemset(t->bar, 0, sizeof(unsigned) * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&t->d_est, sizeof(float) * 48);
+        if (e == cudaSuccess) e = cudaMalloc(&t->d_result, sizeof(azu_icp_result));
+        if (e == cudaSuccess) e = cudaMalloc(&t->d_build, sizeof(float) * 64);
+        if (e != cudaSuccess) { set_error("tracker allocation: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; }
+    }
+    if (!rc) rc = alloc_levels(t, 640, 480);
+    if (rc) { azu_tracker_destroy(t); return rc; }
+    *out = t;
+    return AZU_OK;
+}
+
+extern "C" int azu_tracker_destroy(azu_tracker* t) {
+    if (!t) return AZU_OK;
+    cudaSetDevice(t->device);
+    if (t->stream.s) cudaStreamSynchronize(t->stream.s);
+    for (int l = 0; l < 3; ++l) { cudaFree(t->V[l]); cudaFree(t->N[l]); cudaFree(t->D[l]); }
+    cudaFree(t->partials);
+    cudaFree(t->ipartials);
+    cudaFree(t->bar);
+    cudaFree(t->d_est);
+    cudaFree(t->d_result);
+    cudaFree(t->d_build);
+    t->stream.release();
+    delete t;
+    return AZU_OK;
+}
+
+extern "C" int azu_tracker_set_params(azu_tracker* t, const azu_tracker_params* p) {
+    AZU_CHECK_ARG(t != nullptr && p != nullptr, "null argument");
+    t->p = sanitize(*p);
+    return AZU_OK;
+}
+
+extern "C" int azu_tracker_prepare_live(azu_tracker* t, const float* d_depth_m, int width, int height) {
+    AZU_CHECK_ARG(t != nullptr && d_depth_m != nullptr, "null argument");
+    AZU_CHECK_ARG(width >= 8 && height >= 8 && width % 4 == 0 && height % 4 == 0,
+                  "width and height must be multiples of 4 (>= 8)");
+    AZU_TRY_CUDA(cudaSetDevice(t->device));
+    if (width != t->W || height != t->H) {
+        AZU_TRY_CUDA(cudaStreamSynchronize(t->stream.s));
+        if (int rc = alloc_levels(t, width, height)) return rc;
+    }
+    if (int rc = tracker_prepare_dev(t, d_depth_m, width, height, t->stream.s)) return rc;
+    t->prepared = true;
+    return AZU_OK;
+}
+
+extern "C" int azu_tracker_track_prepared(azu_tracker* t, int width, int height, const float* d_model_vertices,
+                                          const float* d_model_normals, int model_w, int model_h,
+                                          const float estimate[16], const float ref_pose[16], azu_icp_result* out) {
+    AZU_CHECK_ARG(t != nullptr && d_model_vertices != nullptr && d_model_normals != nullptr && estimate != nullptr &&
+                      ref_pose != nullptr && out != nullptr,
+                  "null argument");
+    AZU_CHECK_ARG(model_w > 0 && model_h > 0, "model size");
+    if (!t->prepared || width != t->W || height != t->H) {
+        set_error("track_prepared called without a matching prepare_live");
+        return AZU_E_STATE;
+    }
+    AZU_TRY_CUDA(cudaSetDevice(t->device));
+    if (int rc = set_pose_async(t->d_est, estimate, t->stream.s)) return rc;
+    if (int rc = set_pose_async(t->d_est + 16, ref_pose, t->stream.s)) return rc;
+    if (int rc = tracker_track_dev(t, d_model_vertices, d_model_normals, model_w, model_h, t->d_est, t->d_est + 16,
+                                   nullptr, nullptr, t->d_result, nullptr, nullptr, t->stream.s))
+        return rc;
+    AZU_TRY_CUDA(cudaMemcpyAsync(out, t->d_result, sizeof(azu_icp_result), cudaMemcpyDeviceToHost, t->stream.s));
+    AZU_TRY_CUDA(cudaStreamSynchronize(t->stream.s));
+    if (out->status == AZU_E_TIMEOUT) {
+        unsigned z = 0;
+        cudaMemcpy(t->bar + 2, &z, sizeof(z), cudaMemcpyHostToDevice);
+        set_error("ICP grid barrier timed out");
+        return AZU_E_TIMEOUT;
+    }
+    return AZU_OK;
+}
+
+extern "C" int azu_tracker_track(azu_tracker* t, const float* d_depth_m, int width, int height,
+                                 const float* d_model_vertices, const float* d_model_normals, int model_w, int model_h,
+                                 const float estimate[16], const float ref_pose[16], azu_icp_result* out) {
+    if (int rc = azu_tracker_prepare_live(t, d_depth_m, width, height)) return rc;
+    return azu_tracker_track_prepared(t, width, height, d_model_vertices, d_model_normals, model_w, model_h, estimate,
+                                      ref_pose, out);
+}
+
+extern "C" int azu_tracker_build_system(azu_tracker* t, int level, const float* d_model_vertices,
+                                        const float* d_model_normals, int model_w, int model_h, const float pose[16],
+                                        const float ref_pose[16], float A[36], float b[6], float* residual,
+                                        int counts[6]) {
+    AZU_CHECK_ARG(t != nullptr && d_model_vertices && d_model_normals && pose && ref_pose && A && b && residual &&
+                      counts,
+                  "null argument");
+    AZU_CHECK_ARG(level >= 0 && level < 3, "level");
+    if (!t->prepared) { set_error("build_system called before prepare_live"); return AZU_E_STATE; }
+    AZU_TRY_CUDA(cudaSetDevice(t->device));
+    if (int rc = set_pose_async(t->d_est, pose, t->stream.s)) return rc;
+    if (int rc = set_pose_async(t->d_est + 16, ref_pose, t->stream.s)) return rc;
+    IcpArgs a;
+    fill_args(t, a, d_model_vertices, d_model_normals, model_w, model_h);
+    a.d_estimate = t->d_est;
+    a.d_ref = t->d_est + 16;
+    a.build_level = level;
+    a.build_out = t->d_build;
+    if (int rc = icp_launch(t, a, t->stream.s)) return rc;
+    float out[49];
+    AZU_TRY_CUDA(cudaMemcpyAsync(out, t->d_build, sizeof(out), cudaMemcpyDeviceToHost, t->stream.s));
+    unsigned err = 0;
+    AZU_TRY_CUDA(cudaMemcpyAsync(&err, t->bar + 2, sizeof(err), cudaMemcpyDeviceToHost, t->stream.s));
+    AZU_TRY_CUDA(cudaStreamSynchronize(t->stream.s));
+    if (err) {
+        unsigned z = 0;
+        cudaMemcpy(t->bar + 2, &z, sizeof(z), cudaMemcpyHostToDevice);
+        set_error("ICP grid barrier timed out");
+        return AZU_E_TIMEOUT;
+    }
+    std::memcpy(A, out, 36 * sizeof(float));
+    std::memcpy(b, out + 36, 6 * sizeof(float));
+    *residual = out[42];
+    std::memcpy(counts, out + 43, 6 * sizeof(int));
+    return AZU_OK;
+}
+
+extern "C" int azu_tracker_live_maps(azu_tracker* t, int level, const float** d_vertices, const float** d_normals,
+                                     const float** d_depth_m) {
+    AZU_CHECK_ARG(t != nullptr && level >= 0 && level < 3, "argument");
+    if (d_vertices) *d_vertices = t->V[level];
+    if (d_normals) *d_normals = t->N[level];
+    if (d_depth_m) *d_depth_m = t->D[level];
+    return AZU_OK;
+}
+
+extern "C" int azu_tracker_load_live(azu_tracker* t, int level, const float* d_vertices, const float* d_normals,
+                                     int width, int height) {
+    AZU_CHECK_ARG(t != nullptr && d_vertices != nullptr && d_normals != nullptr, "null argument");
+    AZU_CHECK_ARG(level >= 0 && level < 3, "level");
+    AZU_CHECK_ARG(width >= 8 && height >= 8 && width % 4 == 0 && height % 4 == 0,
+                  "width and height must be multiples of 4 (>= 8)");
+    AZU_TRY_CUDA(cudaSetDevice(t->device));
+    if (width != t->W || height != t->H) {
+        AZU_TRY_CUDA(cudaStreamSynchronize(t->stream.s));
+        if (int rc = alloc_levels(t, width, height)) return rc;
+    }
+    const size_t n = static_cast<size_t>(width >> level) * (height >> level) * 3 * sizeof(float);
+    AZU_TRY_CUDA(cudaMemcpyAsync(t->V[level], d_vertices, n, cudaMemcpyDeviceToDevice, t->stream.s));
+    AZU_TRY_CUDA(cudaMemcpyAsync(t->N[level], d_normals, n, cudaMemcpyDeviceToDevice, t->stream.s));
+    t->prepared = true;
+    return AZU_OK;
+}

@@ -1,0 +1,704 @@
+// TSDF volume on the GPU: reset, voxel-projective integration, front-face
+// raycast and whole-volume transfers, behind the azu_volume_* C ABI.
+//
+// Semantics follow the reference CPU path (src/tsdf/TSDFVolume.cpp:112-525);
+// the reference's own CUDA twin (src/tsdf/TSDFVolume_cuda.cu) is not followed.
+//
+// Layout in HBM: one 8-byte record per voxel, {float tsdf, float weight}, in
+// z-major order (index z*res*res + y*res + x) — every consumer (integrate,
+// trilinear sampling, marching cubes) needs both fields of a voxel together.
+// The FP16 form packs {half tsdf, uint16 weight} into 4 bytes. Colour, when
+// enabled, is a separate float[3] per voxel.
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <cstdlib>
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "azu_internal.h"
+#include "kf_math.cuh"
+
+namespace azu {
+
+constexpr float kEmptyTsdf = 1.0f;
+constexpr float kEmptyColor = 128.0f / 255.0f;
+
+size_t voxel_bytes(int format) { return format == AZU_TSDF_FP16 ? 4 : 8; }
+
+// ---- voxel record access -----------------------------------------------
+template <bool kHalf>
+struct Vox;
+template <>
+struct Vox<false> {
+    using T = float2;
+    __device__ static __forceinline__ float2 load(const void* v, size_t i) {
+        return __ldg(static_cast<const float2*>(v) + i);
+    }
+    __device__ static __forceinline__ float2 load_rw(const void* v, size_t i) {
+        return static_cast<const float2*>(v)[i];
+    }
+    __device__ static __forceinline__ void store(void* v, size_t i, float t, float w) {
+        static_cast<float2*>(v)[i] = make_float2(t, w);
+    }
+};
+template <>
+struct Vox<true> {
+    using T = uint32_t;
+    __device__ static __forceinline__ float2 unpack(uint32_t u) {
+        return make_float2(__half2float(__ushort_as_half(static_cast<unsigned short>(u & 0xFFFFu))),
+                           static_cast<float>(u >> 16));
+    }
+    __device__ static __forceinline__ float2 load(const void* v, size_t i) {
+        return unpack(__ldg(static_cast<const uint32_t*>(v) + i));
+    }
+    __device__ static __forceinline__ float2 load_rw(const void* v, size_t i) {
+        return unpack(static_cast<const uint32_t*>(v)[i]);
+    }
+    __device__ static __forceinline__ void store(void* v, size_t i, float t, float w) {
+        const uint32_t h = __half_as_ushort(__float2half_rn(t));
+        static_cast<uint32_t*>(v)[i] = h | (static_cast<uint32_t>(w) << 16);
+    }
+};
+
+// ---- small kernels -------------------------------------------------------
+struct Pose16 {
+    float m[16];
+};
+__global__ void set_pose_kernel(float* dst, Pose16 p) {
+    if (threadIdx.x < 16) dst[threadIdx.x] = p.m[threadIdx.x];
+}
+
+template <bool kHalf>
+__global__ void reset_kernel(void* vox, float* color, size_t n) {
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        Vox<kHalf>::store(vox, i, kEmptyTsdf, 0.0f);
+        if (color) {
+            color[3 * i] = kEmptyColor;
+            color[3 * i + 1] = kEmptyColor;
+            color[3 * i + 2] = kEmptyColor;
+        }
+    }
+}
+
+// Frustum AABB and camera transform for one integration (TSDFVolume.cpp:238-264),
+// computed on the device so the pose may come from the tracker without a host
+// round trip. Same float expression trees as the CPU path.
+__global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res, float vs, float ox, float oy,
+                                       float oz, float trunc, float fx, float fy, float cx, float cy, int W, int H,
+                                       float max_d, IntegrateConsts* out, unsigned long long* counters) {
+    if (threadIdx.x != 0) return;
+    float P[16], inv[16], Rcw[9];
+    for (int i = 0; i < 16; ++i) P[i] = d_pose[i];
+    inverse4(P, inv);
+    IntegrateConsts ic;
+    rot_of(inv, ic.R_wc);
+    const F3 t_wc = trans_of(inv);
+    ic.t_wc[0] = t_wc.x; ic.t_wc[1] = t_wc.y; ic.t_wc[2] = t_wc.z;
+    rot_of(P, Rcw);
+    const F3 t_cw = trans_of(P);
+    const F3 origin = mk3(ox, oy, oz);
+    F3 lo = div3(sub3(t_cw, origin), vs);
+    F3 hi = lo;
+    const float z_far = fa(max_d, trunc);
+    const float cpx[4][2] = {{0.0f, 0.0f}, {float(W), 0.0f}, {0.0f, float(H)}, {float(W), float(H)}};
+    for (int k = 0; k < 4; ++k) {
+        const F3 ray = mk3(fm(fd(fs(cpx[k][0], cx), fx), z_far), fm(fd(fs(cpx[k][1], cy), fy), z_far), z_far);
+        const F3 v = div3(sub3(add3(mv3(Rcw, ray), t_cw), origin), vs);
+        lo = mk3(v.x < lo.x ? v.x : lo.x, v.y < lo.y ? v.y : lo.y, v.z < lo.z ? v.z : lo.z);
+        hi = mk3(hi.x < v.x ? v.x : hi.x, hi.y < v.y ? v.y : hi.y, hi.z < v.z ? v.z : hi.z);
+    }
+    ic.valid = finite3(lo) && finite3(hi);
+    auto clampIdx = [res](float f) {
+        const float top = static_cast<float>(res - 1);
+        const float a = f < top ? f : top;
+        return static_cast<int>(a > 0.0f ? a : 0.0f);
+    };
+    ic.x0 = ic.valid ? clampIdx(floorf(lo.x)) : 0;
+    ic.x1 = ic.valid ? clampIdx(ceilf(hi.x)) : -1;
+    ic.y0 = ic.valid ? clampIdx(floorf(lo.y)) : 0;
+    ic.y1 = ic.valid ? clampIdx(ceilf(hi.y)) : -1;
+    ic.z0 = ic.valid ? clampIdx(floorf(lo.z)) : 0;
+    ic.z1 = ic.valid ? clampIdx(ceilf(hi.z)) : -1;
+    ic.step_x[0] = fm(ic.R_wc[0], vs);
+    ic.step_x[1] = fm(ic.R_wc[3], vs);
+    ic.step_x[2] = fm(ic.R_wc[6], vs);
+    *out = ic;
+    counters[1] = 0;
+    counters[2] = 0;
+}
+
+// Voxel-projective integration (TSDFVolume.cpp:282-329).
+//
+// The CPU steps the camera coordinate of a voxel row incrementally along x
+// (c += R_wc.col(0) * vs from the AABB start x0), so the pixel a voxel lands in
+// depends on that rounded running sum. To reproduce it exactly and still touch
+// memory coalesced, a warp owns 32 voxel rows (32 consecutive y at one z) and
+// walks them in chunks of 32 x:
+//   phase 1 (lane = row): replay the sequential c-steps for the chunk, project,
+//            test, and park the signed distance (NaN = no update) in shared memory;
+//   phase 2 (lane = x):   for each of the 32 rows, update the voxels that have a
+//            parked distance with one coalesced read-modify-write.
+// Voxels that take no update are never read, so HBM traffic is 2 x record size
+// per updated voxel.
+constexpr int kIntWarps = 8;
+
+template <bool kHalf, bool kColor>
+__global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
+    void* __restrict__ vox, float* __restrict__ color, const IntegrateConsts* __restrict__ icp,
+    const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
+    float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
+    float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters) {
+    __shared__ float s_sdf[kIntWarps][32][33];
+    __shared__ int s_pix[kColor ? kIntWarps : 1][32][33];
+    if (gate && __ldg(gate) == 0) return;
+    if (!__ldg(&icp->valid)) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ngroups = (res + 31) >> 5;
+    const int item = blockIdx.x * kIntWarps + warp;
+    if (item >= res * ngroups) return;
+    const int z = item / ngroups;
+    const int ybase = (item - z * ngroups) << 5;
+    const int z0 = __ldg(&icp->z0), z1 = __ldg(&icp->z1), y0 = __ldg(&icp->y0), y1 = __ldg(&icp->y1);
+    if (z < z0 || z > z1 || ybase + 31 < y0 || ybase > y1) return;
+    const int x0 = __ldg(&icp->x0), x1 = __ldg(&icp->x1);
+    float R[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = __ldg(&icp->R_wc[i]);
+    const F3 t_wc = mk3(__ldg(&icp->t_wc[0]), __ldg(&icp->t_wc[1]), __ldg(&icp->t_wc[2]));
+    const F3 step = mk3(__ldg(&icp->step_x[0]), __ldg(&icp->step_x[1]), __ldg(&icp->step_x[2]));
+
+    const int y = ybase + lane;
+    const bool row_on = (y >= y0 && y <= y1);
+    F3 c = add3(mv3(R, add3(mk3(ox, oy, oz), mul3(mk3(float(x0), float(y), float(z)), vs))), t_wc);
+    const float fW = static_cast<float>(W), fH = static_cast<float>(H);
+    const float color_band = fm(0.5f, trunc);
+    const float qnan = __int_as_float(0x7fffffff);
+    unsigned long long n_new = 0, n_upd = 0, n_col = 0;
+    const size_t rr = static_cast<size_t>(res);
+
+    for (int xc = x0 & ~31; xc <= x1; xc += 32) {
+        // phase 1: lane = row
+        for (int k = 0; k < 32; ++k) {
+            const int x = xc + k;
+            float out = qnan;
+            int pix = -1;
+            if (row_on && x >= x0 && x <= x1) {
+                if (c.z > 0.0f) {
+                    const float inv_z = fd(1.0f, c.z);
+                    const float uf = floorf(fa(fa(fm(fm(fx, c.x), inv_z), cx), 0.5f));
+                    const float vf = floorf(fa(fa(fm(fm(fy, c.y), inv_z), cy), 0.5f));
+                    if (uf >= 0.0f && uf < fW && vf >= 0.0f && vf < fH) {
+                        pix = static_cast<int>(vf) * W + static_cast<int>(uf);
+                        const float d = __ldg(depth + pix);
+                        if (d >= min_d && d <= max_d) {
+                            const float sdf = fs(d, c.z);
+                            if (!(sdf < -trunc)) out = sdf;
+                        }
+                    }
+                }
+                c = add3(c, step);
+            }
+            s_sdf[warp][lane][k] = out;
+            if (kColor) s_pix[warp][lane][k] = pix;
+        }
+        __syncwarp();
+        // phase 2: lane = x
+        const int x = xc + lane;
+        for (int r = 0; r < 32; ++r) {
+            const float sdf = s_sdf[warp][r][lane];
+            if (sdf != sdf) continue;  // NaN: no update
+            const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + r)) * rr + x;
+            const float tsdf_new = fminf(1.0f, fd(sdf, trunc));
+            const float2 old = Vox<kHalf>::load_rw(vox, vi);
+            const float w_old = old.y;
+            n_new += (w_old == 0.0f);
+            ++n_upd;
+            const float wp1 = fa(w_old, 1.0f);
+            const float t = fd(fa(fm(old.x, w_old), tsdf_new), wp1);
+            const float w = fminf(wp1, max_w);
+            Vox<kHalf>::store(vox, vi, t, w);
+            if (kColor) {
+                if (rgb != nullptr && fabsf(sdf) < color_band) {
+                    const int pix = s_pix[warp][r][lane];
+                    const float inv = fd(1.0f, wp1);
+                    float* cv = color + 3 * vi;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        cv[k] = fm(fa(fm(cv[k], w_old), fd(static_cast<float>(rgb[3 * pix + k]), 255.0f)), inv);
+                    ++n_col;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    // warp totals -> global counters
+    for (int o = 16; o > 0; o >>= 1) {
+        n_new += __shfl_down_sync(0xffffffffu, n_new, o);
+        n_upd += __shfl_down_sync(0xffffffffu, n_upd, o);
+        n_col += __shfl_down_sync(0xffffffffu, n_col, o);
+    }
+    if (lane == 0) {
+        if (n_new) atomicAdd(&counters[0], n_new);
+        if (n_upd) atomicAdd(&counters[1], n_upd);
+        if (n_col) atomicAdd(&counters[2], n_col);
+    }
+}
+
+// ---- raycast ---------------------------------------------------------------
+struct VolView {
+    const void* vox;
+    const float* color;
+    int res;
+    float vs;
+    F3 origin;
+};
+
+// sampleTSDF (TSDFVolume.cpp:492-525): trilinear, valid only if all 8 corners
+// are observed.
+template <bool kHalf>
+__device__ __forceinline__ bool sample_tsdf(const VolView& v, F3 p, float& f) {
+    const F3 q = div3(sub3(p, v.origin), v.vs);
+    const float fx0 = floorf(q.x), fy0 = floorf(q.y), fz0 = floorf(q.z);
+    const float lim = static_cast<float>(v.res - 1);
+    if (!(fx0 >= 0.0f && fy0 >= 0.0f && fz0 >= 0.0f && fx0 < lim && fy0 < lim && fz0 < lim)) return false;
+    const int x0 = static_cast<int>(fx0), y0 = static_cast<int>(fy0), z0 = static_cast<int>(fz0);
+    const float tx = fs(q.x, fx0), ty = fs(q.y, fy0), tz = fs(q.z, fz0);
+    const size_t r = static_cast<size_t>(v.res);
+    const size_t b = (static_cast<size_t>(z0) * r + static_cast<size_t>(y0)) * r + static_cast<size_t>(x0);
+    const float2 c0 = Vox<kHalf>::load(v.vox, b), c1 = Vox<kHalf>::load(v.vox, b + 1);
+    const float2 c2 = Vox<kHalf>::load(v.vox, b + r), c3 = Vox<kHalf>::load(v.vox, b + r + 1);
+    const float2 c4 = Vox<kHalf>::load(v.vox, b + r * r), c5 = Vox<kHalf>::load(v.vox, b + r * r + 1);
+    const float2 c6 = Vox<kHalf>::load(v.vox, b + r * r + r), c7 = Vox<kHalf>::load(v.vox, b + r * r + r + 1);
+    if (!(c0.y > 0.0f) || !(c1.y > 0.0f) || !(c2.y > 0.0f) || !(c3.y > 0.0f) || !(c4.y > 0.0f) ||
+        !(c5.y > 0.0f) || !(c6.y > 0.0f) || !(c7.y > 0.0f))
+        return false;
+    const float ux = fs(1.0f, tx), uy = fs(1.0f, ty), uz = fs(1.0f, tz);
+    const float v00 = fa(fm(c0.x, ux), fm(c1.x, tx));
+    const float v10 = fa(fm(c2.x, ux), fm(c3.x, tx));
+    const float v01 = fa(fm(c4.x, ux), fm(c5.x, tx));
+    const float v11 = fa(fm(c6.x, ux), fm(c7.x, tx));
+    const float v0 = fa(fm(v00, uy), fm(v10, ty));
+    const float v1 = fa(fm(v01, uy), fm(v11, ty));
+    f = fa(fm(v0, uz), fm(v1, tz));
+    return true;
+}
+
+// computeNormal (TSDFVolume.cpp:478-490).
+template <bool kHalf>
+__device__ __forceinline__ bool compute_normal(const VolView& v, F3 p, F3& n_out) {
+    const float h = v.vs;
+    float s[6];
+    if (!sample_tsdf<kHalf>(v, mk3(fa(p.x, h), fa(p.y, 0.0f), fa(p.z, 0.0f)), s[0])) return false;
+    if (!sample_tsdf<kHalf>(v, mk3(fs(p.x, h), fs(p.y, 0.0f), fs(p.z, 0.0f)), s[1])) return false;
+    if (!sample_tsdf<kHalf>(v, mk3(fa(p.x, 0.0f), fa(p.y, h), fa(p.z, 0.0f)), s[2])) return false;
+    if (!sample_tsdf<kHalf>(v, mk3(fs(p.x, 0.0f), fs(p.y, h), fs(p.z, 0.0f)), s[3])) return false;
+    if (!sample_tsdf<kHalf>(v, mk3(fa(p.x, 0.0f), fa(p.y, 0.0f), fa(p.z, h)), s[4])) return false;
+    if (!sample_tsdf<kHalf>(v, mk3(fs(p.x, 0.0f), fs(p.y, 0.0f), fs(p.z, h)), s[5])) return false;
+    const F3 n = mk3(fs(s[0], s[1]), fs(s[2], s[3]), fs(s[4], s[5]));
+    const float len = norm3(n);
+    if (!(len > 1e-6f) || !isfinite(len)) return false;
+    n_out = div3(n, len);
+    return true;
+}
+
+// Front-face raycast (TSDFVolume.cpp:372-475): one thread per pixel; a warp is
+// 32 adjacent pixels of one row, so its rays march side by side and their
+// trilinear gathers share cache lines.
+template <bool kHalf>
+__global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __restrict__ d_pose, float fx,
+                                                     float fy, float cx, float cy, int W, int H, float trunc,
+                                                     float min_depth, float max_depth, float* __restrict__ vout,
+                                                     float* __restrict__ nout, uint8_t* __restrict__ cout,
+                                                     const int* __restrict__ gate) {
+    if (gate && __ldg(gate) == 0) return;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const int o = y * W + x;
+    float R[9];
+    R[0] = __ldg(d_pose + 0); R[1] = __ldg(d_pose + 1); R[2] = __ldg(d_pose + 2);
+    R[3] = __ldg(d_pose + 4); R[4] = __ldg(d_pose + 5); R[5] = __ldg(d_pose + 6);
+    R[6] = __ldg(d_pose + 8); R[7] = __ldg(d_pose + 9); R[8] = __ldg(d_pose + 10);
+    const F3 co = mk3(__ldg(d_pose + 3), __ldg(d_pose + 7), __ldg(d_pose + 11));
+    F3 vres = mk3(0.0f, 0.0f, 0.0f), nres = mk3(0.0f, 0.0f, 0.0f);
+    uint8_t col[3] = {0, 0, 0};
+
+    const float vs = v.vs;
+    const F3 box_lo = v.origin;
+    const float span = fm(static_cast<float>(v.res - 1), vs);
+    const F3 box_hi = add3(box_lo, mk3(span, span, span));
+    const float min_step = fm(0.5f, vs);
+    const float far_c = fm(0.8f, trunc);
+    const float far_step = min_step < far_c ? far_c : min_step;  // std::max(min_step, 0.8*trunc)
+
+    do {
+        const F3 ray = mk3(fd(fs(static_cast<float>(x), cx), fx), fd(fs(static_cast<float>(y), cy), fy), 1.0f);
+        const float ray_norm = norm3(ray);
+        const F3 dir = div3(mv3(R, ray), ray_norm);
+        float t_near = fm(min_depth, ray_norm);
+        float t_far = fm(max_depth, ray_norm);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float da = comp(dir, a), oa = comp(co, a), la = comp(box_lo, a), ha = comp(box_hi, a);
+            const float inv = fd(1.0f, da);
+            float t0 = fm(fs(la, oa), inv);
+            float t1 = fm(fs(ha, oa), inv);
+            if (t0 > t1) { const float tmp = t0; t0 = t1; t1 = tmp; }
+            if (isnan(t0) || isnan(t1)) {
+                if (oa < la || oa > ha) t_far = -1.0f;
+                continue;
+            }
+            t_near = (t_near < t0) ? t0 : t_near;  // std::max(t_near, t0)
+            t_far = (t1 < t_far) ? t1 : t_far;     // std::min(t_far, t1)
+        }
+        if (!(t_near < t_far)) break;
+
+        float t_prev = t_near, f_prev = 1.0f;
+        bool prev_valid = sample_tsdf<kHalf>(v, add3(co, mul3(dir, t_prev)), f_prev);
+        if (prev_valid && !isfinite(f_prev)) break;
+        if (prev_valid && f_prev < 0.0f) break;
+        bool found = false;
+        float t_hit = 0.0f;
+        while (t_prev < t_far) {
+            float step;
+            if (!prev_valid || f_prev >= 0.999f) {
+                step = far_step;
+            } else {
+                const float s = fm(fm(0.8f, f_prev), trunc);
+                step = min_step < s ? s : min_step;  // std::max(min_step, s)
+            }
+            const float tn = fa(t_prev, step);
+            const float t = (t_far < tn) ? t_far : tn;  // std::min(t_prev + step, t_far)
+            if (!(t > t_prev)) break;  // no progress (degenerate parameters): stop without a hit
+            float f = 1.0f;
+            const bool valid = sample_tsdf<kHalf>(v, add3(co, mul3(dir, t)), f);
+            if (valid && !isfinite(f)) break;
+            if (valid && prev_valid) {
+                if (f_prev > 0.0f && f <= 0.0f) {
+                    t_hit = fa(t_prev, fm(fs(t, t_prev), fd(f_prev, fs(f_prev, f))));
+                    found = true;
+                    break;
+                }
+                if (f_prev < 0.0f && f >= 0.0f) break;
+            } else if (valid && f < 0.0f) {
+                break;
+            }
+            t_prev = t;
+            f_prev = f;
+            prev_valid = valid;
+            if (t >= t_far) break;
+        }
+        if (!found) break;
+        const F3 hit = add3(co, mul3(dir, t_hit));
+        F3 nrm;
+        if (!compute_normal<kHalf>(v, hit, nrm)) break;
+        if (!finite3(hit)) break;
+        if (cout) {
+            const F3 q = div3(sub3(hit, v.origin), vs);
+            int vx, vy, vz;
+            if (floor_to_int(q.x, &vx) && floor_to_int(q.y, &vy) && floor_to_int(q.z, &vz) && vx >= 0 &&
+                vx < v.res && vy >= 0 && vy < v.res && vz >= 0 && vz < v.res) {
+                const size_t r = static_cast<size_t>(v.res);
+                const size_t vi = (static_cast<size_t>(vz) * r + vy) * r + vx;
+                if (Vox<kHalf>::load(v.vox, vi).y > 0.0f) {
+                    const float cr = v.color ? v.color[3 * vi] : kEmptyColor;
+                    const float cg = v.color ? v.color[3 * vi + 1] : kEmptyColor;
+                    const float cb = v.color ? v.color[3 * vi + 2] : kEmptyColor;
+                    uint8_t q0, q1, q2;
+                    if (!(srgb_to_byte(cr, &q0) && srgb_to_byte(cg, &q1) && srgb_to_byte(cb, &q2))) break;
+                    col[0] = q0; col[1] = q1; col[2] = q2;
+                }
+            }
+        }
+        vres = hit;
+        nres = nrm;
+    } while (false);
+    vout[3 * o] = vres.x; vout[3 * o + 1] = vres.y; vout[3 * o + 2] = vres.z;
+    nout[3 * o] = nres.x; nout[3 * o + 1] = nres.y; nout[3 * o + 2] = nres.z;
+    if (cout) { cout[3 * o] = col[0]; cout[3 * o + 1] = col[1]; cout[3 * o + 2] = col[2]; }
+}
+
+// ---- whole-volume transfers -------------------------------------------------
+template <bool kHalf>
+__global__ void unpack_kernel(const void* vox, size_t base, size_t n, float* t, float* w) {
+    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 r = Vox<kHalf>::load_rw(vox, base + i);
+    t[i] = r.x;
+    w[i] = r.y;
+}
+template <bool kHalf>
+__global__ void pack_kernel(void* vox, size_t base, size_t n, const float* t, const float* w) {
+    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Vox<kHalf>::store(vox, base + i, t[i], w[i]);
+}
+
+int set_pose_async(float* d_pose, const float* pose, cudaStream_t s) {
+    Pose16 p;
+    std::memcpy(p.m, pose, sizeof(p.m));
+    set_pose_kernel<<<1, 32, 0, s>>>(d_pose, p);
+    AZU_LAUNCH_CHECK();
+    return AZU_OK;
+}
+
+int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d_rgb, const float* d_pose, float fx,
+                         float fy, float cx, float cy, int W, int H, float min_d, float max_d, const int* d_gate,
+                         cudaStream_t s) {
+    const azu_volume_params& p = v->p;
+    integrate_setup_kernel<<<1, 32, 0, s>>>(d_pose, p.resolution, p.voxel_size, p.origin[0], p.origin[1],
+                                            p.origin[2], p.truncation, fx, fy, cx, cy, W, H, max_d, v->d_iconsts,
+                                            v->d_counters);
+    AZU_LAUNCH_CHECK();
+    const int ngroups = (p.resolution + 31) / 32;
+    const long items = static_cast<long>(p.resolution) * ngroups;
+    const int blocks = static_cast<int>((items + kIntWarps - 1) / kIntWarps);
+    const bool half = p.format == AZU_TSDF_FP16;
+    const bool col = v->color != nullptr;
+#define AZU_INT_ARGS                                                                                             \
+    v->vox, v->color, v->d_iconsts, d_depth_m, d_rgb, p.resolution, p.voxel_size, p.origin[0], p.origin[1],     \
+        p.origin[2], p.truncation, p.max_weight, fx, fy, cx, cy, W, H, min_d, max_d, d_gate, v->d_counters
+    if (!half && !col) integrate_kernel<false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    else if (!half && col) integrate_kernel<false, true><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    else if (half && !col) integrate_kernel<true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    else integrate_kernel<true, true><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+#undef AZU_INT_ARGS
+    AZU_LAUNCH_CHECK();
+    return AZU_OK;
+}
+
+int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, float cx, float cy, int W, int H,
+                       float* d_vertices, float* d_normals, uint8_t* d_colors, const int* d_gate, cudaStream_t s) {
+    const azu_volume_params& p = v->p;
+    VolView view{v->vox, v->color, p.resolution, p.voxel_size, mk3(p.origin[0], p.origin[1], p.origin[2])};
+    const dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
+    if (p.format == AZU_TSDF_FP16)
+        raycast_kernel<true><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
+                                                  p.max_depth, d_vertices, d_normals, d_colors, d_gate);
+    else
+        raycast_kernel<false><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
+                                                   p.max_depth, d_vertices, d_normals, d_colors, d_gate);
+    AZU_LAUNCH_CHECK();
+    return AZU_OK;
+}
+
+static int volume_alloc(azu_volume* v) {
+    const size_t n = static_cast<size_t>(v->p.resolution) * v->p.resolution * v->p.resolution;
+    AZU_TRY_CUDA(cudaMalloc(&v->vox, n * voxel_bytes(v->p.format)));
+    if (v->p.color) AZU_TRY_CUDA(cudaMalloc(&v->color, n * 3 * sizeof(float)));
+    return AZU_OK;
+}
+static void volume_free_storage(azu_volume* v) {
+    if (v->vox) cudaFree(v->vox);
+    if (v->color) cudaFree(v->color);
+    v->vox = nullptr;
+    v->color = nullptr;
+}
+static int check_params(const azu_volume_params* p) {
+    AZU_CHECK_ARG(p != nullptr, "params is null");
+    AZU_CHECK_ARG(p->resolution >= 2 && p->resolution <= 2048, "resolution must be in [2, 2048]");
+    AZU_CHECK_ARG(p->voxel_size > 0.0f && std::isfinite(p->voxel_size), "voxel_size must be > 0");
+    AZU_CHECK_ARG(p->truncation > 0.0f && std::isfinite(p->truncation), "truncation must be > 0");
+    AZU_CHECK_ARG(p->max_weight >= 1.0f && p->max_weight <= 65535.0f, "max_weight must be in [1, 65535]");
+    AZU_CHECK_ARG(p->format == AZU_TSDF_FP32 || p->format == AZU_TSDF_FP16, "format");
+    return AZU_OK;
+}
+
+}  // namespace azu
+
+using namespace azu;
+
+extern "C" int azu_volume_reset(azu_volume* v) {
+    AZU_CHECK_ARG(v != nullptr, "volume is null");
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    const size_t n = static_cast<size_t>(v->p.resolution) * v->p.resolution * v->p.resolution;
+    const int blocks = static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 32));
+    if (v->p.format == AZU_TSDF_FP16) reset_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
+    else reset_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
+    AZU_LAUNCH_CHECK();
+    AZU_TRY_CUDA(cudaMemsetAsync(v->d_counters, 0, 4 * sizeof(unsigned long long), v->stream.s));
+    v->integrated_frames = 0;
+    return AZU_OK;
+}
+
+extern "C" int azu_volume_create(int device, const azu_volume_params* p, void* stream, azu_volume** out) {
+    AZU_CHECK_ARG(out != nullptr, "out is null");
+    *out = nullptr;
+    if (int rc = check_params(p)) return rc;
+    if (int rc = bind_device(device)) return rc;
+    azu_volume* v = new azu_volume();
+    v->device = device;
+    v->p = *p;
+    int rc = v->stream.init(stream);
+    if (!rc) rc = volume_alloc(v);
+    if (!rc) { cudaError_t e = cudaMalloc(&v->d_pose, 16 * sizeof(float)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
+    if (!rc) { cudaError_t e = cudaMalloc(&v->d_iconsts, sizeof(IntegrateConsts)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
+    if (!rc) { cudaError_t e = cudaMalloc(&v->d_counters, 4 * sizeof(unsigned long long)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
+    if (!rc) rc = azu_volume_reset(v);
+    if (rc) {
+        azu_volume_destroy(v);
+        return rc;
+    }
+    *out = v;
+    return AZU_OK;
+}
+
+extern "C" int azu_volume_destroy(azu_volume* v) {
+    if (!v) return AZU_OK;
+    cudaSetDevice(v->device);
+    if (v->stream.s) cudaStreamSynchronize(v->stream.s);
+    volume_free_storage(v);
+    if (v->d_pose) cudaFree(v->d_pose);
+    if (v->d_iconsts) cudaFree(v->d_iconsts);
+    if (v->d_counters) cudaFree(v->d_counters);
+    if (v->d_depth_stage) cudaFree(v->d_depth_stage);
+    if (v->d_rgb_stage) cudaFree(v->d_rgb_stage);
+    v->stream.release();
+    delete v;
+    return AZU_OK;
+}
+
+extern "C" int azu_volume_set_params(azu_volume* v, const azu_volume_params* p) {
+    AZU_CHECK_ARG(v != nullptr, "volume is null");
+    if (int rc = check_params(p)) return rc;
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    const bool realloc = p->resolution != v->p.resolution || p->format != v->p.format || (!!p->color) != (!!v->p.color);
+    if (realloc) {
+        AZU_TRY_CUDA(cudaStreamSynchronize(v->stream.s));
+        volume_free_storage(v);
+        v->p = *p;
+        if (int rc = volume_alloc(v)) return rc;
+    } else {
+        v->p = *p;
+    }
+    return azu_volume_reset(v);
+}
+
+extern "C" int azu_volume_get_params(const azu_volume* v, azu_volume_params* p) {
+    AZU_CHECK_ARG(v != nullptr && p != nullptr, "null argument");
+    *p = v->p;
+    return AZU_OK;
+}
+
+extern "C" int azu_volume_integrate(azu_volume* v, const float* d_depth_m, const uint8_t* d_rgb, const float pose[16],
+                                    float fx, float fy, float cx, float cy, int width, int height, float min_depth,
+                                    float max_depth) {
+    AZU_CHECK_ARG(v != nullptr && d_depth_m != nullptr && pose != nullptr, "null argument");
+    AZU_CHECK_ARG(width > 0 && height > 0, "image size");
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    if (int rc = set_pose_async(v->d_pose, pose, v->stream.s)) return rc;
+    if (int rc = volume_integrate_dev(v, d_depth_m, d_rgb, v->d_pose, fx, fy, cx, cy, width, height, min_depth,
+                                      max_depth, nullptr, v->stream.s))
+        return rc;
+    v->integrated_frames++;
+    return AZU_OK;
+}
+
+extern "C" int azu_volume_integrate_host(azu_volume* v, const float* h_depth_m, const uint8_t* h_rgb,
+                                         const float pose[16], float fx, float fy, float cx, float cy, int width,
+                                         int height, float min_depth, float max_depth) {
+    AZU_CHECK_ARG(v != nullptr && h_depth_m != nullptr && pose != nullptr, "null argument");
+    AZU_CHECK_ARG(width > 0 && height > 0, "image size");
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    const size_t n = static_cast<size_t>(width) * height;
+    if (n > v->stage_pixels) {
+        AZU_TRY_CUDA(cudaStreamSynchronize(v->stream.s));
+        if (v->d_depth_stage) cudaFree(v->d_depth_stage);
+        if (v->d_rgb_stage) cudaFree(v->d_rgb_stage);
+        v->d_depth_stage = nullptr;
+        v->d_rgb_stage = nullptr;
+        v->stage_pixels = 0;
+        AZU_TRY_CUDA(cudaMalloc(&v->d_depth_stage, n * sizeof(float)));
+        AZU_TRY_CUDA(cudaMalloc(&v->d_rgb_stage, n * 3));
+        v->stage_pixels = n;
+    }
+    AZU_TRY_CUDA(cudaMemcpyAsync(v->d_depth_stage, h_depth_m, n * sizeof(float), cudaMemcpyHostToDevice, v->stream.s));
+    if (h_rgb) AZU_TRY_CUDA(cudaMemcpyAsync(v->d_rgb_stage, h_rgb, n * 3, cudaMemcpyHostToDevice, v->stream.s));
+    // Pageable sources: the copies above have returned once the data is staged.
+    AZU_TRY_CUDA(cudaStreamSynchronize(v->stream.s));
+    return azu_volume_integrate(v, v->d_depth_stage, h_rgb ? v->d_rgb_stage : nullptr, pose, fx, fy, cx, cy, width,
+                                height, min_depth, max_depth);
+}
+
+extern "C" int azu_volume_raycast(azu_volume* v, const float pose[16], float fx, float fy, float cx, float cy,
+                                  int width, int height, float* d_vertices, float* d_normals, uint8_t* d_colors) {
+    AZU_CHECK_ARG(v != nullptr && pose != nullptr && d_vertices != nullptr && d_normals != nullptr,
+                  "null argument");
+    AZU_CHECK_ARG(width > 0 && height > 0, "image size");
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    if (int rc = set_pose_async(v->d_pose, pose, v->stream.s)) return rc;
+    return volume_raycast_dev(v, v->d_pose, fx, fy, cx, cy, width, height, d_vertices, d_normals, d_colors, nullptr,
+                              v->stream.s);
+}
+
+extern "C" int azu_volume_get_stats(azu_volume* v, azu_volume_stats* s) {
+    AZU_CHECK_ARG(v != nullptr && s != nullptr, "null argument");
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    unsigned long long c[4];
+    AZU_TRY_CUDA(cudaMemcpyAsync(c, v->d_counters, sizeof(c), cudaMemcpyDeviceToHost, v->stream.s));
+    AZU_TRY_CUDA(cudaStreamSynchronize(v->stream.s));
+    s->integrated_frames = v->integrated_frames;
+    s->observed_voxels = static_cast<int64_t>(c[0]);
+    s->last_voxels_updated = static_cast<int64_t>(c[1]);
+    s->last_color_updates = static_cast<int64_t>(c[2]);
+    s->voxels = static_cast<int64_t>(v->p.resolution) * v->p.resolution * v->p.resolution;
+    return AZU_OK;
+}
+
+static int transfer(azu_volume* v, float* ht, float* hw, float* hc, const float* ut, const float* uw,
+                    const float* uc, bool download) {
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    const size_t n = static_cast<size_t>(v->p.resolution) * v->p.resolution * v->p.resolution;
+    const size_t chunk = std::min<size_t>(n, size_t(1) << 24);
+    float *dt = nullptr, *dw = nullptr;
+    AZU_TRY_CUDA(cudaStreamSynchronize(v->stream.s));
+    cudaError_t e = cudaMalloc(&dt, chunk * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&dw, chunk * sizeof(float));
+    const bool half = v->p.format == AZU_TSDF_FP16;
+    for (size_t base = 0; e == cudaSuccess && base < n; base += chunk) {
+        const size_t m = std::min(chunk, n - base);
+        const int blocks = static_cast<int>((m + 255) / 256);
+        if (download) {
+            if (half) unpack_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+            else unpack_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+            e = cudaGetLastError();
+            if (e == cudaSuccess && ht) e = cudaMemcpyAsync(ht + base, dt, m * sizeof(float), cudaMemcpyDeviceToHost, v->stream.s);
+            if (e == cudaSuccess && hw) e = cudaMemcpyAsync(hw + base, dw, m * sizeof(float), cudaMemcpyDeviceToHost, v->stream.s);
+        } else {
+            e = cudaMemcpyAsync(dt, ut + base, m * sizeof(float), cudaMemcpyHostToDevice, v->stream.s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(dw, uw + base, m * sizeof(float), cudaMemcpyHostToDevice, v->stream.s);
+            if (e == cudaSuccess) {
+                if (half) pack_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+                else pack_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+                e = cudaGetLastError();
+            }
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(v->stream.s);
+    }
+    if (e == cudaSuccess && v->color) {
+        if (download && hc) e = cudaMemcpy(hc, v->color, 3 * n * sizeof(float), cudaMemcpyDeviceToHost);
+        if (!download && uc) e = cudaMemcpy(v->color, uc, 3 * n * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (dt) cudaFree(dt);
+    if (dw) cudaFree(dw);
+    if (e != cudaSuccess) {
+        set_error("volume transfer: %s", cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? AZU_E_NOMEM : AZU_E_CUDA;
+    }
+    return AZU_OK;
+}
+
+extern "C" int azu_volume_download(azu_volume* v, float* h_tsdf, float* h_weight, float* h_color) {
+    AZU_CHECK_ARG(v != nullptr, "volume is null");
+    return transfer(v, h_tsdf, h_weight, h_color, nullptr, nullptr, nullptr, true);
+}
+
+extern "C" int azu_volume_upload(azu_volume* v, const float* h_tsdf, const float* h_weight, const float* h_color) {
+    AZU_CHECK_ARG(v != nullptr && h_tsdf != nullptr && h_weight != nullptr, "null argument");
+    return transfer(v, nullptr, nullptr, nullptr, h_tsdf, h_weight, h_color, false);
+}
+
+extern "C" void* azu_volume_device_voxels(azu_volume* v) { return v ? v->vox : nullptr; }

@@ -1,0 +1,304 @@
+/* azu_gpu.h — C ABI of the GB300 KinectFusion backend (libazu_gb300.so).
+ *
+ * The reference (iphands/azu) selects its GPU path at run time through
+ * `--backend cuda` and `#ifdef CUDA_ENABLED` member functions of four classes:
+ * sensor::Preprocessor, tracking::ICPTracker, tsdf::TSDFVolume and
+ * meshing::MarchingCubes. Each entry point below replaces one of those member
+ * functions; the comment names the file:line of the reference declaration. A
+ * C++ adapter in the reference keeps its class and forwards to these calls.
+ *
+ * Conventions
+ *  - Every function returns an int status: AZU_OK (0) or a negative AZU_E_*
+ *    code; nothing throws across the ABI. azu_last_error() describes the last
+ *    failure on the calling thread.
+ *  - Handles own their device memory. Work is ordered on the handle's stream
+ *    (the `stream` argument at creation, a cudaStream_t; NULL makes a private
+ *    non-blocking stream). Calls that return results to the host synchronise
+ *    that stream; the others only enqueue.
+ *  - Poses are row-major float[16], world-from-camera (element (r, c) at
+ *    [4 r + c]); Eigen's Matrix4f::data() is column-major, so an adapter passes
+ *    the transpose.
+ *  - Vertex / normal maps are float[3 * W * H] (packed float3 per pixel, the
+ *    reference's float3 device maps), colours uint8[3 * W * H].
+ *  - Images are row-major, W = 640, H = 480 at level 0.
+ *  - "d_" pointers are device memory; "h_" pointers are host memory.
+ */
+#ifndef AZU_GPU_H
+#define AZU_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    AZU_OK = 0,
+    AZU_E_INVALID = -1,      /* bad argument (null handle, size, parameter) */
+    AZU_E_CUDA = -2,         /* CUDA runtime error */
+    AZU_E_NOMEM = -3,        /* device allocation failed */
+    AZU_E_TIMEOUT = -4,      /* a bounded device-side wait gave up */
+    AZU_E_UNSUPPORTED = -5,  /* no sm_103 device, or feature not built */
+    AZU_E_STATE = -6         /* call out of order (e.g. track before prepare) */
+};
+
+const char* azu_last_error(void);
+/* Library version string. */
+const char* azu_version(void);
+
+/* GPU selection (src/app/GpuSelect_cuda.cu:18-71 selectCudaDevice): picks the
+ * sm_103 device with the most free memory that has at least `min_free_bytes`
+ * free; returns its ordinal in *device. */
+int azu_select_device(size_t min_free_bytes, int* device);
+
+/* ------------------------------------------------------------------------ */
+/* TSDF volume — tsdf::TSDFVolume (include/tsdf/TSDFVolume.h:69-190).        */
+/* ------------------------------------------------------------------------ */
+
+typedef struct azu_volume azu_volume;
+
+enum { AZU_TSDF_FP32 = 0, AZU_TSDF_FP16 = 1 };
+
+typedef struct {
+    int   resolution;   /* voxels per axis (TSDFParams::resolution) */
+    float voxel_size;   /* metres */
+    float truncation;   /* metres */
+    float max_weight;
+    float origin[3];    /* world position of voxel (0,0,0) */
+    float min_depth;    /* raycast band, camera Z-depth (TSDFParams::min_depth) */
+    float max_depth;    /* TSDFParams::max_depth */
+    int   format;       /* AZU_TSDF_FP32: float tsdf + float weight (8 B/voxel);
+                           AZU_TSDF_FP16: half tsdf + uint16 weight (4 B/voxel) */
+    int   color;        /* nonzero: keep float sRGB colour per voxel (12 B/voxel) */
+} azu_volume_params;
+
+/* Constructor + TSDFVolume::initGPU (TSDFVolume.h:141): allocates the volume on
+ * `device` and resets it (tsdf 1, weight 0, colour 128/255). */
+int azu_volume_create(int device, const azu_volume_params* p, void* stream, azu_volume** out);
+/* TSDFVolume::freeGPU + destructor. */
+int azu_volume_destroy(azu_volume* v);
+/* TSDFVolume::reset (TSDFVolume.h:120). */
+int azu_volume_reset(azu_volume* v);
+/* TSDFVolume::setParams (TSDFVolume.h:82-85): any change clears the volume; a
+ * resolution or format change reallocates. */
+int azu_volume_set_params(azu_volume* v, const azu_volume_params* p);
+int azu_volume_get_params(const azu_volume* v, azu_volume_params* p);
+
+/* TSDFVolume::integrateGPU (TSDFVolume.h:145-153): voxel-projective update from
+ * a device depth map in metres (d_rgb may be NULL). Enqueue only. */
+int azu_volume_integrate(azu_volume* v, const float* d_depth_m, const uint8_t* d_rgb, const float pose[16],
+                         float fx, float fy, float cx, float cy, int width, int height, float min_depth,
+                         float max_depth);
+/* TSDFVolume::integrate (TSDFVolume.h:92-100) with GPU enabled: host depth (and
+ * optional host rgb) copied to the device, then integrateGPU. Enqueue only
+ * (the host buffers are read before return). */
+int azu_volume_integrate_host(azu_volume* v, const float* h_depth_m, const uint8_t* h_rgb, const float pose[16],
+                              float fx, float fy, float cx, float cy, int width, int height, float min_depth,
+                              float max_depth);
+/* TSDFVolume::raycastGPU (TSDFVolume.h:154-158): model vertex/normal (and
+ * optional colour) maps in world coordinates into device buffers. Misses are
+ * zero. Enqueue only. */
+int azu_volume_raycast(azu_volume* v, const float pose[16], float fx, float fy, float cx, float cy, int width,
+                       int height, float* d_vertices, float* d_normals, uint8_t* d_colors);
+
+typedef struct {
+    int     integrated_frames;   /* TSDFVolume::integratedFrames */
+    int64_t observed_voxels;     /* voxels first observed since reset (observedFraction numerator) */
+    int64_t last_voxels_updated; /* voxels updated by the last integrate */
+    int64_t last_color_updates;
+    int64_t voxels;              /* res^3 */
+} azu_volume_stats;
+/* Synchronises the volume's stream. */
+int azu_volume_get_stats(azu_volume* v, azu_volume_stats* s);
+
+/* TSDFVolume::syncFromGPU / syncToGPU (TSDFVolume.h:143-144): whole-volume
+ * copies as separate float arrays of res^3 (colour: 3 res^3, may be NULL).
+ * FP16 volumes convert on the device. Synchronous. */
+int azu_volume_download(azu_volume* v, float* h_tsdf, float* h_weight, float* h_color);
+int azu_volume_upload(azu_volume* v, const float* h_tsdf, const float* h_weight, const float* h_color);
+/* TSDFVolume::getGPUVoxels (TSDFVolume.h:163): device voxel array (float2
+ * {tsdf, weight} for FP32, uint32 {half, u16} for FP16). */
+void* azu_volume_device_voxels(azu_volume* v);
+
+/* ------------------------------------------------------------------------ */
+/* ICP tracker — tracking::ICPTracker (include/tracking/ICPTracker.h:80-126). */
+/* ------------------------------------------------------------------------ */
+
+typedef struct azu_tracker azu_tracker;
+
+typedef struct {
+    int   max_iterations[3]; /* per level 0,1,2 (ICPParams: {10, 5, 4}) */
+    float dist_threshold;    /* metres */
+    float angle_threshold;   /* degrees, sanitised to [0, 85] like setParams */
+    float min_depth, max_depth;
+    float fx, fy, cx, cy;    /* camera intrinsics at 640x480 (setIntrinsics) */
+    int   precision;         /* 0: FP32 reduction + FP32 solve (reference semantics);
+                                1: compensated FP32 per-block sums, FP64 cross-block
+                                sum, FP64 Cholesky and SE(3) update */
+} azu_tracker_params;
+
+/* Mirrors ICPResult (ICPTracker.h:27-47); pose row-major. */
+typedef struct {
+    float pose[16];
+    float error;
+    int   inliers;
+    int   converged;
+    int   tracking_ok;
+    float final_step;
+    float information[36];
+    int   valid_live_points, valid_model_points, projected_points, dist_filtered, angle_filtered;
+    int   iterations[3];     /* accepted solves per level */
+    int   status;            /* AZU_OK or AZU_E_TIMEOUT from the device */
+} azu_icp_result;
+
+/* initGPU (ICPTracker.h:114). */
+int azu_tracker_create(int device, const azu_tracker_params* p, void* stream, azu_tracker** out);
+/* freeGPU (ICPTracker.h:115). */
+int azu_tracker_destroy(azu_tracker* t);
+int azu_tracker_set_params(azu_tracker* t, const azu_tracker_params* p);
+/* prepareLiveGPU (ICPTracker.h:101): vertices, normals and the 3-level
+ * jump-guarded pyramid from a device depth map in metres (band-gated, 0 =
+ * invalid). Enqueue only. */
+int azu_tracker_prepare_live(azu_tracker* t, const float* d_depth_m, int width, int height);
+/* trackPreparedGPU (ICPTracker.h:102-106): coarse-to-fine ICP against a model
+ * image (device float3 maps of model_w x model_h, raycast at ref_pose). The
+ * whole solve runs in one persistent kernel; synchronises and fills *out. */
+int azu_tracker_track_prepared(azu_tracker* t, int width, int height, const float* d_model_vertices,
+                               const float* d_model_normals, int model_w, int model_h, const float estimate[16],
+                               const float ref_pose[16], azu_icp_result* out);
+/* trackGPU (ICPTracker.h:94-100) = prepare_live + track_prepared. */
+int azu_tracker_track(azu_tracker* t, const float* d_depth_m, int width, int height, const float* d_model_vertices,
+                      const float* d_model_normals, int model_w, int model_h, const float estimate[16],
+                      const float ref_pose[16], azu_icp_result* out);
+/* One association + reduction pass (ICPTracker::buildLinearSystem,
+ * src/tracking/ICPTracker.cpp:136-354) at a pyramid level, for parity checks:
+ * A (36, row-major), b (6), residual, counts {inliers, valid_live, valid_model,
+ * projected, dist_filtered, angle_filtered}. Synchronous. */
+int azu_tracker_build_system(azu_tracker* t, int level, const float* d_model_vertices, const float* d_model_normals,
+                             int model_w, int model_h, const float pose[16], const float ref_pose[16], float A[36],
+                             float b[6], float* residual, int counts[6]);
+/* Loads a prebuilt live pyramid level (device float3 vertex and normal maps of
+ * (width >> level) x (height >> level)), the GPU counterpart of handing
+ * ICPTracker::track a FramePyramid built elsewhere (ICPTracker.h:89-92). Marks
+ * the tracker prepared for width x height. Enqueue only. */
+int azu_tracker_load_live(azu_tracker* t, int level, const float* d_vertices, const float* d_normals, int width,
+                          int height);
+/* Device pointers of the live pyramid (float3 maps and depth) at a level. */
+int azu_tracker_live_maps(azu_tracker* t, int level, const float** d_vertices, const float** d_normals,
+                          const float** d_depth_m);
+
+/* ------------------------------------------------------------------------ */
+/* Preprocessor — sensor::Preprocessor / CUDAPreprocessor                    */
+/* (include/sensor/Preprocessor.h:23-53, :76-113).                          */
+/* ------------------------------------------------------------------------ */
+
+typedef struct azu_preprocessor azu_preprocessor;
+
+enum { AZU_PRE_FULL = 0, AZU_PRE_MINIMAL = 1 };
+
+/* makePreprocessor(CUDA) (Preprocessor.h:115-118). mode: AZU_PRE_FULL runs the
+ * RGB guidance chain, depth median, hole fill, guided joint-bilateral filter and
+ * temporal EMA; AZU_PRE_MINIMAL (AZU_PREPROCESS=minimal) the median only. */
+int azu_preprocessor_create(int device, int mode, void* stream, azu_preprocessor** out);
+int azu_preprocessor_destroy(azu_preprocessor* p);
+/* Preprocessor::reset / resetTemporalState (Preprocessor.h:27-28). */
+int azu_preprocessor_reset(azu_preprocessor* p);
+int azu_preprocessor_reset_temporal(azu_preprocessor* p);
+/* Preprocessor::process (Preprocessor.h:29): RawFrame depth (640x480 raw
+ * Kinect codes) and rgb (640x480x3) processed in place on the host, device
+ * copies left for getGPUDepthMeters/getGPURgb. Synchronous. */
+int azu_preprocessor_process(azu_preprocessor* p, uint16_t* h_depth, uint8_t* h_rgb, float min_depth,
+                             float max_depth);
+/* Same from device buffers (no host round trip; outputs stay on the device). */
+int azu_preprocessor_process_device(azu_preprocessor* p, const uint16_t* d_depth, const uint8_t* d_rgb,
+                                    float min_depth, float max_depth);
+/* getGPUDepthMeters (Preprocessor.h:44): band-gated metres of the processed
+ * frame (what buildFrameData computes), valid until the next process/reset. */
+float* azu_preprocessor_depth_meters(azu_preprocessor* p);
+/* getGPURgb (Preprocessor.h:45): processed RGB (bilateral + median). */
+uint8_t* azu_preprocessor_rgb(azu_preprocessor* p);
+/* Processed raw depth codes and guidance luma on the device. */
+uint16_t* azu_preprocessor_depth_raw(azu_preprocessor* p);
+float* azu_preprocessor_luma(azu_preprocessor* p);
+
+/* ------------------------------------------------------------------------ */
+/* Marching cubes — meshing::MarchingCubes (include/meshing/MarchingCubes.h). */
+/* ------------------------------------------------------------------------ */
+
+typedef struct azu_mesher azu_mesher;
+
+typedef struct {
+    int64_t n_vertices;   /* welded vertices */
+    int64_t n_indices;    /* 3 x triangles */
+    int     truncated;    /* MeshData::truncated */
+} azu_mesh_info;
+
+int azu_mesher_create(int device, void* stream, azu_mesher** out);
+int azu_mesher_destroy(azu_mesher* m);
+/* setMaxTriangles (MarchingCubes.h:58). Default 2,000,000. */
+int azu_mesher_set_max_triangles(azu_mesher* m, int64_t max_triangles);
+/* extractGPU (MarchingCubes.h:62): classify, scan, emit and the exact-edge weld
+ * on the device; results stay on the device until copied out. Synchronous
+ * (returns the counts). */
+int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* info);
+/* Copies the last extraction into host buffers sized from azu_mesh_info
+ * (positions/normals 3 floats per vertex, colours 3 bytes, indices uint32). */
+int azu_mesher_copy_out(azu_mesher* m, float* h_positions, float* h_normals, uint8_t* h_colors,
+                        uint32_t* h_indices);
+/* Device pointers of the last extraction. */
+int azu_mesher_device_buffers(azu_mesher* m, const float** d_positions, const float** d_normals,
+                              const uint8_t** d_colors, const uint32_t** d_indices);
+
+/* ------------------------------------------------------------------------ */
+/* Per-frame pipeline — the GPU branch of PipelineController's tracking and  */
+/* integration workers (src/app/PipelineController.cpp:1003-1406, 1624-1905) */
+/* run in lockstep (the azu_replay offline mode).                            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct azu_pipeline azu_pipeline;
+
+typedef struct {
+    azu_volume_params  volume;
+    azu_tracker_params tracker;
+    int   preprocess_mode;   /* AZU_PRE_FULL / AZU_PRE_MINIMAL */
+    float min_depth;         /* depth band for preprocessing and frame building */
+    float max_depth;
+    int   input_is_mm;       /* 1: input depth is uint16 millimetres (skips the
+                                Kinect preprocessor, depth_m = mm * 1e-3);
+                                0: Kinect raw codes through the preprocessor */
+    int   use_graph;         /* capture the per-frame work in a CUDA graph */
+} azu_pipeline_params;
+
+typedef struct {
+    float pose[16];          /* camera pose after tracking (world-from-camera) */
+    azu_icp_result icp;      /* the solve that produced it */
+    int   quality;           /* 0 Good (integrated), 1 Poor, 2 Failed, -1 first frame */
+    int   integrated;        /* 1 when the frame was fused */
+    int   frame_index;
+} azu_frame_result;
+
+int azu_pipeline_create(int device, const azu_pipeline_params* p, azu_pipeline** out);
+int azu_pipeline_destroy(azu_pipeline* p);
+int azu_pipeline_reset(azu_pipeline* p);
+/* One frame from host buffers: H2D of depth (and rgb, may be NULL), the whole
+ * frame on the device, D2H of the result. Synchronous. */
+int azu_pipeline_process_frame(azu_pipeline* p, const uint16_t* h_depth, const uint8_t* h_rgb,
+                               azu_frame_result* out);
+/* Same from device buffers; out may be NULL (no host sync: the frame is only
+ * enqueued and the result stays on the device). */
+int azu_pipeline_process_frame_device(azu_pipeline* p, const uint16_t* d_depth, const uint8_t* d_rgb,
+                                      azu_frame_result* out);
+/* Reads back the result of the last enqueued frame (synchronises). */
+int azu_pipeline_last_result(azu_pipeline* p, azu_frame_result* out);
+azu_volume* azu_pipeline_volume(azu_pipeline* p);
+azu_tracker* azu_pipeline_tracker(azu_pipeline* p);
+/* Model maps of the last raycast (device float3, 640x480). */
+int azu_pipeline_model_maps(azu_pipeline* p, const float** d_vertices, const float** d_normals);
+/* The pipeline's stream (cudaStream_t). */
+void* azu_pipeline_stream(azu_pipeline* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AZU_GPU_H */

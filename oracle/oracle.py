@@ -1,0 +1,286 @@
+"""Oracle (test infrastructure only): ctypes binding of oracle/_build/liborc.so,
+the CPU restatement of Azu's KinectFusion hot path. Imported by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg only, as the checker.
+
+Arrays are numpy; poses are row-major (4, 4) float32 world-from-camera.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+class TsdfParams(C.Structure):
+    _fields_ = [("res", C.c_int), ("voxel_size", C.c_float), ("truncation", C.c_float),
+                ("max_weight", C.c_float), ("origin", C.c_float * 3),
+                ("min_depth", C.c_float), ("max_depth", C.c_float)]
+
+
+class Intr(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float)]
+
+
+class IcpParams(C.Structure):
+    _fields_ = [("max_iterations", C.c_int * 3), ("dist_threshold", C.c_float),
+                ("angle_threshold", C.c_float), ("fold_threads", C.c_int)]
+
+
+class IcpResult(C.Structure):
+    _fields_ = [("pose", C.c_float * 16), ("error", C.c_float), ("inliers", C.c_int),
+                ("converged", C.c_int), ("tracking_ok", C.c_int), ("final_step", C.c_float),
+                ("information", C.c_float * 36), ("valid_live_points", C.c_int),
+                ("valid_model_points", C.c_int), ("projected_points", C.c_int),
+                ("dist_filtered", C.c_int), ("angle_filtered", C.c_int), ("iterations", C.c_int * 3)]
+
+    def as_dict(self):
+        return dict(pose=np.array(self.pose, np.float32).reshape(4, 4), error=self.error,
+                    inliers=self.inliers, converged=bool(self.converged),
+                    tracking_ok=bool(self.tracking_ok), final_step=self.final_step,
+                    information=np.array(self.information, np.float32).reshape(6, 6),
+                    valid_live_points=self.valid_live_points,
+                    valid_model_points=self.valid_model_points,
+                    projected_points=self.projected_points, dist_filtered=self.dist_filtered,
+                    angle_filtered=self.angle_filtered, iterations=list(self.iterations))
+
+
+class MeshInfo(C.Structure):
+    _fields_ = [("n_vertices", C.c_int64), ("n_indices", C.c_int64), ("truncated", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB_PATH)
+    return _lib
+
+
+def _p(a, t=C.c_float):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def _pose(p):
+    return np.ascontiguousarray(np.asarray(p, np.float32).reshape(16))
+
+
+def tsdf_params(res=None, voxel_size=0.01, truncation=0.03, max_weight=128.0, origin=(0, 0, 0), min_depth=0.3,
+                max_depth=5.0, resolution=None, format=0):
+    res = resolution if res is None else res
+    return TsdfParams(int(res), float(voxel_size), float(truncation), float(max_weight),
+                      (C.c_float * 3)(*[float(v) for v in origin]), float(min_depth), float(max_depth))
+
+
+def intr(fx, fy, cx, cy):
+    return Intr(float(fx), float(fy), float(cx), float(cy))
+
+
+def set_threads(n: int):
+    lib().orc_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return lib().orc_get_threads()
+
+
+class Volume:
+    """Host volume: separate tsdf / weight (/ colour) arrays, z-major like the reference."""
+
+    def __init__(self, p: TsdfParams, color: bool = False):
+        self.p = p
+        n = p.res ** 3
+        self.tsdf = np.empty(n, np.float32)
+        self.weight = np.empty(n, np.float32)
+        self.color = np.empty(3 * n, np.float32) if color else None
+        self.reset()
+
+    def reset(self):
+        lib().orc_tsdf_reset(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.color))
+
+    def integrate(self, depth_m, pose, K, W, H, min_depth, max_depth, rgb=None):
+        st = np.zeros(9, np.int64)
+        depth_m = np.ascontiguousarray(depth_m, np.float32)
+        rgbp = None if rgb is None else np.ascontiguousarray(rgb, np.uint8)
+        lib().orc_tsdf_integrate(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.color),
+                                 _p(depth_m), _p(rgbp, C.c_uint8), _p(_pose(pose)), K, int(W), int(H),
+                                 C.c_float(min_depth), C.c_float(max_depth), _p(st, C.c_int64))
+        return dict(newly_observed=int(st[0]), voxels_updated=int(st[1]), color_updates=int(st[2]),
+                    aabb=[int(v) for v in st[3:9]])
+
+    def raycast(self, pose, K, W, H, colors=False):
+        v = np.zeros((H * W * 3), np.float32)
+        n = np.zeros((H * W * 3), np.float32)
+        c = np.zeros((H * W * 3), np.uint8) if colors else None
+        s = C.c_int64(0)
+        lib().orc_tsdf_raycast(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.color),
+                               _p(_pose(pose)), K, int(W), int(H), _p(v), _p(n), _p(c, C.c_uint8),
+                               C.byref(s))
+        out = dict(vertices=v.reshape(H, W, 3), normals=n.reshape(H, W, 3), samples=s.value)
+        if colors:
+            out["colors"] = c.reshape(H, W, 3)
+        return out
+
+    def extract_mesh(self, max_triangles=2_000_000):
+        info = MeshInfo()
+        lib().orc_mc_extract(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.color),
+                             C.c_int64(max_triangles), C.byref(info), None, None, None, None)
+        nv, ni = info.n_vertices, info.n_indices
+        pos = np.zeros(3 * max(nv, 1), np.float32)
+        nrm = np.zeros(3 * max(nv, 1), np.float32)
+        col = np.zeros(3 * max(nv, 1), np.uint8)
+        idx = np.zeros(max(ni, 1), np.uint32)
+        lib().orc_mc_extract(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.color),
+                             C.c_int64(max_triangles), C.byref(info), _p(pos), _p(nrm),
+                             _p(col, C.c_uint8), _p(idx, C.c_uint32))
+        return dict(positions=pos[:3 * nv].reshape(-1, 3), normals=nrm[:3 * nv].reshape(-1, 3),
+                    colors=col[:3 * nv].reshape(-1, 3), indices=idx[:ni],
+                    truncated=bool(info.truncated))
+
+
+def build_frame_raw(raw, K, min_depth, max_depth):
+    H, W = raw.shape
+    raw = np.ascontiguousarray(raw, np.uint16)
+    d = np.zeros(W * H, np.float32)
+    v = np.zeros(W * H * 3, np.float32)
+    n = np.zeros(W * H * 3, np.float32)
+    lib().orc_build_frame(_p(raw, C.c_uint16), W, H, K, C.c_float(min_depth), C.c_float(max_depth),
+                          _p(d), _p(v), _p(n))
+    return d.reshape(H, W), v.reshape(H, W, 3)
+
+
+def vertices_from_depth(depth_m, K):
+    H, W = depth_m.shape
+    d = np.ascontiguousarray(depth_m, np.float32)
+    v = np.zeros(W * H * 3, np.float32)
+    lib().orc_vertices_from_depth(_p(d), W, H, K, _p(v))
+    return v.reshape(H, W, 3)
+
+
+def compute_normals(depth_m, vertices):
+    H, W = depth_m.shape
+    n = np.zeros(W * H * 3, np.float32)
+    lib().orc_compute_normals(_p(np.ascontiguousarray(depth_m, np.float32)),
+                              _p(np.ascontiguousarray(vertices, np.float32)), W, H, _p(n))
+    return n.reshape(H, W, 3)
+
+
+def downsample(depth_m, vertices, normals):
+    H, W = depth_m.shape
+    h, w = H // 2, W // 2
+    d = np.zeros(w * h, np.float32)
+    v = np.zeros(w * h * 3, np.float32)
+    n = np.zeros(w * h * 3, np.float32)
+    lib().orc_downsample(_p(np.ascontiguousarray(depth_m, np.float32)),
+                         _p(np.ascontiguousarray(vertices, np.float32)),
+                         _p(np.ascontiguousarray(normals, np.float32)), W, H, _p(d), _p(v), _p(n))
+    return d.reshape(h, w), v.reshape(h, w, 3), n.reshape(h, w, 3)
+
+
+def frame_pyramid_from_depth(depth_m, K):
+    """Level 0 from metres (vertices + normals), then two jump-guarded halvings."""
+    v0 = vertices_from_depth(depth_m, K)
+    n0 = compute_normals(depth_m, v0)
+    levels = [(np.ascontiguousarray(depth_m, np.float32), v0, n0)]
+    for _ in range(2):
+        levels.append(downsample(*levels[-1]))
+    return levels
+
+
+def icp_params(iters=(10, 5, 4), dist=0.1, angle=30.0, fold_threads=1):
+    return IcpParams((C.c_int * 3)(*iters), float(dist), float(angle), int(fold_threads))
+
+
+def icp_build_system(prm, K, live_v, live_n, model_v, model_n, pose, ref_pose):
+    H, W = live_v.shape[:2]
+    MH, MW = model_v.shape[:2]
+    A = np.zeros(36, np.float32)
+    b = np.zeros(6, np.float32)
+    r = C.c_float(0)
+    counts = np.zeros(6, np.int32)
+    ok = lib().orc_icp_build_system(
+        C.byref(prm), K, _p(np.ascontiguousarray(live_v, np.float32)),
+        _p(np.ascontiguousarray(live_n, np.float32)), W, H,
+        _p(np.ascontiguousarray(model_v, np.float32)), _p(np.ascontiguousarray(model_n, np.float32)),
+        MW, MH, _p(_pose(pose)), _p(_pose(ref_pose)), _p(A), _p(b), C.byref(r), _p(counts, C.c_int))
+    return dict(ok=bool(ok), A=A.reshape(6, 6), b=b, residual=r.value,
+                inliers=int(counts[0]), valid_live=int(counts[1]), valid_model=int(counts[2]),
+                projected=int(counts[3]), dist_filtered=int(counts[4]), angle_filtered=int(counts[5]))
+
+
+def icp_track(prm, K, levels, model_v, model_n, estimate, ref_pose):
+    """levels: [(depth, vertices, normals)] x 3 as from frame_pyramid_from_depth."""
+    H, W = levels[0][1].shape[:2]
+    MH, MW = model_v.shape[:2]
+    keep = [np.ascontiguousarray(lv[1], np.float32) for lv in levels] + \
+           [np.ascontiguousarray(lv[2], np.float32) for lv in levels]
+    PV = (C.POINTER(C.c_float) * 3)(*[_p(a) for a in keep[:3]])
+    PN = (C.POINTER(C.c_float) * 3)(*[_p(a) for a in keep[3:]])
+    res = IcpResult()
+    lib().orc_icp_track(C.byref(prm), K, PV, PN, W, H,
+                        _p(np.ascontiguousarray(model_v, np.float32)),
+                        _p(np.ascontiguousarray(model_n, np.float32)), MW, MH,
+                        _p(_pose(estimate)), _p(_pose(ref_pose)), C.byref(res))
+    return res
+
+
+def classify_tracking(res: IcpResult, prev_pose) -> int:
+    return lib().orc_classify_tracking(C.byref(res), _p(_pose(prev_pose)))
+
+
+class Preprocessor:
+    """SignalConditioner CPU path on 640x480 frames (EMA state kept here)."""
+
+    def __init__(self, minimal=False):
+        self.minimal = minimal
+        self.ema = np.zeros(640 * 480, np.float32)
+
+    def reset_temporal(self):
+        self.ema[:] = 0
+
+    def process(self, depth_raw, rgb, min_depth, max_depth):
+        d = np.ascontiguousarray(depth_raw, np.uint16).copy()
+        c = np.ascontiguousarray(rgb, np.uint8).copy()
+        luma = np.zeros(640 * 480, np.float32)
+        lib().orc_preprocess(_p(d, C.c_uint16), _p(c, C.c_uint8), _p(self.ema), _p(luma),
+                             C.c_float(min_depth), C.c_float(max_depth), int(self.minimal))
+        return d.reshape(480, 640), c.reshape(480, 640, 3), luma.reshape(480, 640)
+
+
+def pre_stage(name, depth, *args):
+    d = np.ascontiguousarray(depth, np.uint16).copy()
+    f = getattr(lib(), "orc_pre_" + name)
+    conv = [_p(a) if isinstance(a, np.ndarray) else C.c_float(a) for a in args]
+    f(_p(d, C.c_uint16), *conv)
+    return d
+
+
+def raw_to_meters(raw):
+    lib().orc_raw_to_meters.restype = C.c_float
+    return lib().orc_raw_to_meters(C.c_uint16(int(raw)))
+
+
+def cpu_depth_meters(raw, lo, hi):
+    lib().orc_cpu_depth_meters.restype = C.c_float
+    return lib().orc_cpu_depth_meters(C.c_uint16(int(raw)), C.c_float(lo), C.c_float(hi))
+
+
+def meters_to_raw(m, lo, hi):
+    lib().orc_meters_to_raw.restype = C.c_uint16
+    return lib().orc_meters_to_raw(C.c_float(m), C.c_float(lo), C.c_float(hi))

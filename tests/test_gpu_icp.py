@@ -1,0 +1,126 @@
+"""GPU parity of frame geometry (vertices, normals, pyramid) and ICP against the
+oracle. Geometry and association counts are bit-exact; the normal equations
+are within float reduction-order tolerance; the tracked pose within 1e-6
+rad / 1e-6 m of the oracle's from the same input pose."""
+import numpy as np
+import pytest
+
+import fixtures as F
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def seq():
+    from azu_gb300 import synth
+    return synth.sequence("c1", frames=12)
+
+
+@pytest.fixture(scope="module")
+def model(seq, orc):
+    """Oracle volume of the first 8 frames and its raycast at frame 8."""
+    from azu_gb300 import synth
+    s = seq
+    prm = dict(s.volume, min_depth=s.min_depth, max_depth=s.max_depth)
+    prm.pop("format")
+    o = orc.Volume(orc.tsdf_params(**prm))
+    K = orc.intr(s.fx, s.fy, s.cx, s.cy)
+    for k in range(9):
+        o.integrate(synth.mm_to_meters(s.depth_mm[k]), s.poses[k], K, 640, 480, s.min_depth, s.max_depth)
+    r = o.raycast(s.poses[8], K, 640, 480)
+    return r["vertices"], r["normals"], s.poses[8]
+
+
+def _tracker(**kw):
+    from azu_gb300 import api
+    return api.ICPTracker(api.tracker_params(**kw))
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def test_frame_pyramid_bit_exact(cuda_lib, orc, seq):
+    from azu_gb300 import synth
+    dm = synth.mm_to_meters(seq.depth_mm[3])
+    t = _tracker()
+    t.prepare_live(_dev(dm), 640, 480)
+    levels = orc.frame_pyramid_from_depth(dm, orc.intr(525, 525, 319.5, 239.5))
+    for l in range(3):
+        d, v, n = t.live_maps(l, 640, 480)
+        od, ov, on = levels[l]
+        assert np.array_equal(d.view(np.uint32), od.view(np.uint32)), l
+        assert np.array_equal(v.view(np.uint32), ov.view(np.uint32)), l
+        assert np.array_equal(n.view(np.uint32), on.view(np.uint32)), l
+
+
+def test_build_system_counts_exact(cuda_lib, orc, seq, model):
+    from azu_gb300 import synth
+    mv, mn, ref = model
+    dm = synth.mm_to_meters(seq.depth_mm[9])
+    t = _tracker()
+    t.prepare_live(_dev(dm), 640, 480)
+    levels = orc.frame_pyramid_from_depth(dm, orc.intr(525, 525, 319.5, 239.5))
+    prm = orc.icp_params(fold_threads=1)
+    K = orc.intr(525, 525, 319.5, 239.5)
+    dmv, dmn = _dev(mv), _dev(mn)
+    for level in range(3):
+        for pose in (ref, seq.poses[9]):
+            g = t.build_system(level, dmv, dmn, 640, 480, pose, ref)
+            o = orc.icp_build_system(prm, K, levels[level][1], levels[level][2], mv, mn, pose, ref)
+            for key in ("inliers", "valid_live", "valid_model", "projected", "dist_filtered", "angle_filtered"):
+                assert g[key] == o[key], (level, key)
+            assert g["inliers"] > 100
+            scale = np.abs(o["A"]).max()
+            assert np.abs(g["A"] - o["A"]).max() <= 2e-5 * scale
+            assert np.abs(g["b"] - o["b"]).max() <= 2e-5 * max(np.abs(o["b"]).max(), 1e-3 * scale)
+            assert abs(g["residual"] - o["residual"]) <= 2e-5 * abs(o["residual"]) + 1e-9
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_track_pose_parity(cuda_lib, orc, seq, model, precision):
+    from azu_gb300 import synth
+    mv, mn, ref = model
+    K = orc.intr(525, 525, 319.5, 239.5)
+    prm = orc.icp_params(fold_threads=1)
+    t = _tracker(precision=precision)
+    for k in (9, 10):
+        dm = synth.mm_to_meters(seq.depth_mm[k])
+        t.prepare_live(_dev(dm), 640, 480)
+        g = t.track_prepared(640, 480, _dev(mv), _dev(mn), 640, 480, seq.poses[8], ref)
+        o = orc.icp_track(prm, K, orc.frame_pyramid_from_depth(dm, K), mv, mn, seq.poses[8], ref).as_dict()
+        assert g["status"] == 0
+        assert g["tracking_ok"] == o["tracking_ok"] and g["converged"] == o["converged"]
+        rot, trans = F.rel_pose_error(g["pose"], o["pose"])
+        assert rot <= 1e-6 and trans <= 1e-6, (rot, trans)
+        assert abs(g["inliers"] - o["inliers"]) <= max(3, 1e-4 * o["inliers"])
+        # and against the ground-truth trajectory, tracking works
+        rot_gt, trans_gt = F.rel_pose_error(g["pose"], seq.poses[k])
+        assert rot_gt < 2e-3 and trans_gt < 5e-3
+
+
+def test_icp_weighting_contract_gpu(cuda_lib):
+    lv, ln, mv, mn = F.icp_weighting_fixture()
+    t = _tracker(iters=(1, 0, 0))
+    z1 = np.zeros((240, 320, 3), np.float32)
+    z2 = np.zeros((120, 160, 3), np.float32)
+    t.load_live(0, _dev(lv), _dev(ln), 640, 480)
+    t.load_live(1, _dev(z1), _dev(z1), 640, 480)
+    t.load_live(2, _dev(z2), _dev(z2), 640, 480)
+    r = t.track_prepared(640, 480, _dev(mv), _dev(mn), 640, 480, np.eye(4), np.eye(4))
+    assert r["valid_live_points"] == 11 and r["valid_model_points"] == 11 and r["projected_points"] == 11
+    assert r["inliers"] == 11 and r["dist_filtered"] == 0 and r["angle_filtered"] == 0
+    assert abs(r["pose"][2, 3] - F.ICP_TZ) <= 5e-6
+    assert abs(r["error"] - F.ICP_ERR) <= 5e-6
+    r2 = t.track_prepared(640, 480, _dev(mv), _dev(mn), 640, 480, np.eye(4), np.eye(4))
+    assert np.array_equal(r["pose"], r2["pose"]) and r["error"] == r2["error"]
+
+
+def test_track_without_prepare_is_a_state_error(cuda_lib):
+    from azu_gb300 import _abi
+    t = _tracker()
+    mv = _dev(np.zeros((480, 640, 3), np.float32))
+    with pytest.raises(_abi.AzuError) as e:
+        t.track_prepared(640, 480, mv, mv, 640, 480, np.eye(4), np.eye(4))
+    assert e.value.code == _abi.AZU_E_STATE
