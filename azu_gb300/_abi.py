@@ -34,7 +34,7 @@ class VolumeParams(C.Structure):
 class VolumeStats(C.Structure):
     _fields_ = [("integrated_frames", C.c_int), ("observed_voxels", C.c_int64),
                 ("last_voxels_updated", C.c_int64), ("last_color_updates", C.c_int64),
-                ("voxels", C.c_int64)]
+                ("voxels", C.c_int64), ("total_voxels_updated", C.c_int64)]
 
 
 class TrackerParams(C.Structure):
@@ -131,6 +131,9 @@ SIGNATURES = {
     "azu_pipeline_tracker": (vp, [vp]),
     "azu_pipeline_model_maps": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
     "azu_pipeline_stream": (vp, [vp]),
+    "azu_pipeline_set_profiling": (C.c_int, [vp, C.c_int]),
+    "azu_pipeline_stage_times": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "azu_pipeline_uses_graph": (C.c_int, [vp]),
 }
 
 

@@ -1,0 +1,348 @@
+// Per-frame KinectFusion pipeline on one GPU, behind the azu_pipeline_* ABI:
+// the GPU branch of the reference's tracking and integration workers run in
+// lockstep, as its offline replay drives them (src/app/PipelineController.cpp:
+// 1003-1406 tracking, 1624-1905 integration; tools/azu_replay.cpp).
+//
+// Frame 0: pose = identity, integrate, raycast the model.
+// Frame k > 0, all on the device with no host round trip:
+//   input      preprocess Kinect raw codes (or mm -> metres)
+//   frame      vertices, normals, 3-level pyramid
+//   predict    constant velocity: pred = cur * (last^-1 * cur); prev = cur; last = cur
+//   track      persistent ICP from pred against the model; on a Failed grade it
+//              retries from prev; Good/Poor move cur, Failed keeps it
+//   integrate  only when the grade is Good (a device flag gates the kernels)
+//   raycast    the new model at cur (same gate)
+// Frames k > 0 replay one captured CUDA graph; host inputs and the result are
+// copied outside it.
+#include <cstring>
+
+#include "azu_internal.h"
+#include "kf_math.cuh"
+
+struct azu_preprocessor;
+
+namespace azu {
+int preprocess_enqueue(azu_preprocessor* p, float lo, float hi, cudaStream_t s);
+int mm_to_meters_enqueue(const uint16_t* d_mm, float* d_out, int n, float lo, float hi, cudaStream_t s);
+uint16_t* preprocess_input(azu_preprocessor* p);
+uint8_t* preprocess_rgb_input(azu_preprocessor* p);
+float* preprocess_depth_m(azu_preprocessor* p);
+int tracker_prepare_dev(azu_tracker* t, const float* d_depth, int W, int H, cudaStream_t s);
+int tracker_track_dev(azu_tracker* t, const float* mv, const float* mn, int MW, int MH, const float* d_estimate,
+                      const float* d_ref, const float* d_prev, float* d_pose_out, azu_icp_result* d_result,
+                      int* d_quality, int* d_gate, cudaStream_t s);
+
+// Device-resident pose state of the pipeline.
+struct PoseState {
+    float cur[16];
+    float last[16];
+    float pred[16];
+    float prev[16];
+    float model_pose[16];
+    int quality;
+    int gate;
+    int frame_index;
+    int integrated;
+};
+
+// PipelineController.cpp:1175-1177 (velocity model off, the default).
+__global__ void predict_kernel(PoseState* st) {
+    if (threadIdx.x != 0) return;
+    float inv[16], m[16];
+    for (int i = 0; i < 16; ++i) st->prev[i] = st->cur[i];
+    inverse4(st->last, inv);
+    mm4(inv, st->cur, m);
+    mm4(st->cur, m, st->pred);
+    for (int i = 0; i < 16; ++i) st->last[i] = st->cur[i];
+}
+
+// After a gated integrate + raycast: the model now shows the scene at cur.
+__global__ void commit_kernel(PoseState* st) {
+    if (threadIdx.x != 0) return;
+    st->integrated = st->gate;
+    if (st->gate)
+        for (int i = 0; i < 16; ++i) st->model_pose[i] = st->cur[i];
+    st->frame_index += 1;
+}
+
+__global__ void first_frame_kernel(PoseState* st) {
+    if (threadIdx.x != 0) return;
+    for (int i = 0; i < 16; ++i) {
+        const float v = (i % 5 == 0) ? 1.0f : 0.0f;
+        st->cur[i] = st->last[i] = st->pred[i] = st->prev[i] = st->model_pose[i] = v;
+    }
+    st->quality = -1;
+    st->gate = 1;
+    st->frame_index = 0;
+    st->integrated = 0;
+}
+
+}  // namespace azu
+
+struct azu_pipeline {
+    int device = 0;
+    azu_pipeline_params p{};
+    cudaStream_t s = nullptr;
+    azu_preprocessor* pre = nullptr;
+    azu_tracker* trk = nullptr;
+    azu_volume* vol = nullptr;
+    uint16_t* d_in = nullptr;   // mm input when input_is_mm
+    float* d_depth_m = nullptr; // mm path output
+    float* d_model_v = nullptr;
+    float* d_model_n = nullptr;
+    azu::PoseState* d_st = nullptr;
+    azu_icp_result* d_icp = nullptr;
+    int frames = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev[6] = {};
+    double stage_ms[5] = {0, 0, 0, 0, 0};
+    int stage_frames = 0;
+    bool profiling = false;
+    int graph_failed = 0;
+};
+
+namespace azu {
+
+static const float* depth_source(azu_pipeline* pl) {
+    return pl->p.input_is_mm ? pl->d_depth_m : preprocess_depth_m(pl->pre);
+}
+
+static int mark(azu_pipeline* pl, int k) {
+    if (pl->profiling) AZU_TRY_CUDA(cudaEventRecord(pl->ev[k], pl->s));
+    return AZU_OK;
+}
+
+// The work of one frame after the inputs are on the device.
+static int enqueue_frame(azu_pipeline* pl, bool first) {
+    cudaStream_t s = pl->s;
+    const azu_pipeline_params& P = pl->p;
+    const float lo = P.min_depth, hi = P.max_depth;
+    const int W = 640, H = 480;
+    const azu_tracker_params& T = P.tracker;
+    if (int rc = mark(pl, 0)) return rc;
+    if (P.input_is_mm) {
+        if (int rc = mm_to_meters_enqueue(pl->d_in, pl->d_depth_m, W * H, lo, hi, s)) return rc;
+    } else {
+        if (int rc = preprocess_enqueue(pl->pre, lo, hi, s)) return rc;
+    }
+    if (int rc = mark(pl, 1)) return rc;
+    const float* dm = depth_source(pl);
+    if (int rc = tracker_prepare_dev(pl->trk, dm, W, H, s)) return rc;
+    if (int rc = mark(pl, 2)) return rc;
+    PoseState* st = pl->d_st;
+    if (first) {
+        first_frame_kernel<<<1, 32, 0, s>>>(st);
+        AZU_LAUNCH_CHECK();
+    } else {
+        predict_kernel<<<1, 32, 0, s>>>(st);
+        AZU_LAUNCH_CHECK();
+        if (int rc = tracker_track_dev(pl->trk, pl->d_model_v, pl->d_model_n, W, H, st->pred, st->model_pose,
+                                       st->prev, st->cur, pl->d_icp, &st->quality, &st->gate, s))
+            return rc;
+    }
+    if (int rc = mark(pl, 3)) return rc;
+    if (int rc = volume_integrate_dev(pl->vol, dm, nullptr, st->cur, T.fx, T.fy, T.cx, T.cy, W, H, lo, hi, &st->gate, s))
+        return rc;
+    if (int rc = mark(pl, 4)) return rc;
+    if (int rc = volume_raycast_dev(pl->vol, st->cur, T.fx, T.fy, T.cx, T.cy, W, H, pl->d_model_v, pl->d_model_n,
+                                    nullptr, &st->gate, s))
+        return rc;
+    commit_kernel<<<1, 32, 0, s>>>(st);
+    AZU_LAUNCH_CHECK();
+    if (int rc = mark(pl, 5)) return rc;
+    return AZU_OK;
+}
+
+static int run_frame(azu_pipeline* pl) {
+    const bool first = pl->frames == 0;
+    if (first || !pl->p.use_graph) {
+        if (int rc = enqueue_frame(pl, first)) return rc;
+    } else {
+        if (!pl->exec) {
+            AZU_TRY_CUDA(cudaStreamBeginCapture(pl->s, cudaStreamCaptureModeThreadLocal));
+            const int rc = enqueue_frame(pl, false);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(pl->s, &g);
+            cudaError_t ei = cudaErrorUnknown;
+            if (!rc && e == cudaSuccess) ei = cudaGraphInstantiate(&pl->exec, g, 0);
+            if (rc || e != cudaSuccess || ei != cudaSuccess) {
+                // Capture is an optimisation only: run this and later frames eagerly.
+                if (g) cudaGraphDestroy(g);
+                pl->exec = nullptr;
+                cudaGetLastError();
+                pl->p.use_graph = 0;
+                pl->graph_failed = 1;
+                if (int rc2 = enqueue_frame(pl, false)) return rc2;
+                pl->frames++;
+                pl->vol->integrated_frames++;
+                return AZU_OK;
+            }
+            pl->graph = g;
+        }
+        AZU_TRY_CUDA(cudaGraphLaunch(pl->exec, pl->s));
+    }
+    pl->frames++;
+    pl->vol->integrated_frames++;
+    return AZU_OK;
+}
+
+static int upload_inputs(azu_pipeline* pl, const uint16_t* depth, const uint8_t* rgb, cudaMemcpyKind kind) {
+    const size_t n = 640 * 480;
+    if (pl->p.input_is_mm) {
+        AZU_TRY_CUDA(cudaMemcpyAsync(pl->d_in, depth, n * 2, kind, pl->s));
+    } else {
+        AZU_TRY_CUDA(cudaMemcpyAsync(preprocess_input(pl->pre), depth, n * 2, kind, pl->s));
+        if (rgb) AZU_TRY_CUDA(cudaMemcpyAsync(preprocess_rgb_input(pl->pre), rgb, n * 3, kind, pl->s));
+    }
+    return AZU_OK;
+}
+
+static int read_result(azu_pipeline* pl, azu_frame_result* out) {
+    PoseState st;
+    AZU_TRY_CUDA(cudaMemcpyAsync(&st, pl->d_st, sizeof(st), cudaMemcpyDeviceToHost, pl->s));
+    AZU_TRY_CUDA(cudaMemcpyAsync(&out->icp, pl->d_icp, sizeof(azu_icp_result), cudaMemcpyDeviceToHost, pl->s));
+    AZU_TRY_CUDA(cudaStreamSynchronize(pl->s));
+    if (pl->profiling) {
+        for (int k = 0; k < 5; ++k) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, pl->ev[k], pl->ev[k + 1]) == cudaSuccess) pl->stage_ms[k] += ms;
+        }
+        pl->stage_frames++;
+    }
+    std::memcpy(out->pose, st.cur, sizeof(out->pose));
+    out->quality = st.quality;
+    out->integrated = st.integrated;
+    out->frame_index = st.frame_index - 1;
+    if (st.quality == -1) std::memset(&out->icp, 0, sizeof(out->icp));
+    if (out->icp.status == AZU_E_TIMEOUT) {
+        set_error("ICP grid barrier timed out");
+        return AZU_E_TIMEOUT;
+    }
+    return AZU_OK;
+}
+
+}  // namespace azu
+
+using namespace azu;
+
+extern "C" int azu_pipeline_destroy(azu_pipeline* pl) {
+    if (!pl) return AZU_OK;
+    cudaSetDevice(pl->device);
+    if (pl->s) cudaStreamSynchronize(pl->s);
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    azu_preprocessor_destroy(pl->pre);
+    azu_tracker_destroy(pl->trk);
+    azu_volume_destroy(pl->vol);
+    for (void* q : {(void*)pl->d_in, (void*)pl->d_depth_m, (void*)pl->d_model_v, (void*)pl->d_model_n,
+                    (void*)pl->d_st, (void*)pl->d_icp})
+        if (q) cudaFree(q);
+    for (cudaEvent_t e : pl->ev) if (e) cudaEventDestroy(e);
+    if (pl->s) cudaStreamDestroy(pl->s);
+    delete pl;
+    return AZU_OK;
+}
+
+extern "C" int azu_pipeline_create(int device, const azu_pipeline_params* p, azu_pipeline** out) {
+    AZU_CHECK_ARG(p != nullptr && out != nullptr, "null argument");
+    *out = nullptr;
+    if (int rc = bind_device(device)) return rc;
+    azu_pipeline* pl = new azu_pipeline();
+    pl->device = device;
+    pl->p = *p;
+    int rc = AZU_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&pl->s, cudaStreamNonBlocking);
+    if (e) { set_error("stream: %s", cudaGetErrorString(e)); rc = AZU_E_CUDA; }
+    if (!rc) rc = azu_volume_create(device, &p->volume, pl->s, &pl->vol);
+    if (!rc) rc = azu_tracker_create(device, &p->tracker, pl->s, &pl->trk);
+    if (!rc && !p->input_is_mm) rc = azu_preprocessor_create(device, p->preprocess_mode, pl->s, &pl->pre);
+    if (!rc) {
+        const size_t n = 640 * 480;
+        e = cudaMalloc(&pl->d_in, n * 2);
+        if (!e) e = cudaMalloc(&pl->d_depth_m, n * 4);
+        if (!e) e = cudaMalloc(&pl->d_model_v, n * 12);
+        if (!e) e = cudaMalloc(&pl->d_model_n, n * 12);
+        if (!e) e = cudaMalloc(&pl->d_st, sizeof(PoseState));
+        if (!e) e = cudaMalloc(&pl->d_icp, sizeof(azu_icp_result));
+        if (!e) e = cudaMemsetAsync(pl->d_icp, 0, sizeof(azu_icp_result), pl->s);
+        for (int k = 0; !e && k < 6; ++k) e = cudaEventCreate(&pl->ev[k]);
+        if (e) { set_error("pipeline allocation: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; }
+    }
+    if (rc) { azu_pipeline_destroy(pl); return rc; }
+    *out = pl;
+    return AZU_OK;
+}
+
+extern "C" int azu_pipeline_reset(azu_pipeline* pl) {
+    AZU_CHECK_ARG(pl != nullptr, "null handle");
+    AZU_TRY_CUDA(cudaSetDevice(pl->device));
+    if (int rc = azu_volume_reset(pl->vol)) return rc;
+    if (pl->pre) if (int rc = azu_preprocessor_reset(pl->pre)) return rc;
+    pl->frames = 0;
+    pl->vol->integrated_frames = 0;
+    return AZU_OK;
+}
+
+extern "C" int azu_pipeline_process_frame(azu_pipeline* pl, const uint16_t* h_depth, const uint8_t* h_rgb,
+                                          azu_frame_result* out) {
+    AZU_CHECK_ARG(pl != nullptr && h_depth != nullptr && out != nullptr, "null argument");
+    AZU_CHECK_ARG(pl->p.input_is_mm || h_rgb != nullptr, "the raw-code path needs the RGB frame for guidance");
+    AZU_TRY_CUDA(cudaSetDevice(pl->device));
+    if (int rc = upload_inputs(pl, h_depth, h_rgb, cudaMemcpyHostToDevice)) return rc;
+    if (int rc = run_frame(pl)) return rc;
+    return read_result(pl, out);
+}
+
+extern "C" int azu_pipeline_process_frame_device(azu_pipeline* pl, const uint16_t* d_depth, const uint8_t* d_rgb,
+                                                 azu_frame_result* out) {
+    AZU_CHECK_ARG(pl != nullptr && d_depth != nullptr, "null argument");
+    AZU_CHECK_ARG(pl->p.input_is_mm || d_rgb != nullptr, "the raw-code path needs the RGB frame for guidance");
+    AZU_TRY_CUDA(cudaSetDevice(pl->device));
+    if (int rc = upload_inputs(pl, d_depth, d_rgb, cudaMemcpyDeviceToDevice)) return rc;
+    if (int rc = run_frame(pl)) return rc;
+    if (out) return read_result(pl, out);
+    return AZU_OK;
+}
+
+extern "C" int azu_pipeline_last_result(azu_pipeline* pl, azu_frame_result* out) {
+    AZU_CHECK_ARG(pl != nullptr && out != nullptr, "null argument");
+    AZU_TRY_CUDA(cudaSetDevice(pl->device));
+    return read_result(pl, out);
+}
+
+extern "C" azu_volume* azu_pipeline_volume(azu_pipeline* pl) { return pl ? pl->vol : nullptr; }
+extern "C" azu_tracker* azu_pipeline_tracker(azu_pipeline* pl) { return pl ? pl->trk : nullptr; }
+
+extern "C" int azu_pipeline_model_maps(azu_pipeline* pl, const float** d_vertices, const float** d_normals) {
+    AZU_CHECK_ARG(pl != nullptr, "null handle");
+    if (d_vertices) *d_vertices = pl->d_model_v;
+    if (d_normals) *d_normals = pl->d_model_n;
+    return AZU_OK;
+}
+
+extern "C" void* azu_pipeline_stream(azu_pipeline* pl) { return pl ? static_cast<void*>(pl->s) : nullptr; }
+
+extern "C" int azu_pipeline_set_profiling(azu_pipeline* pl, int on) {
+    AZU_CHECK_ARG(pl != nullptr, "null handle");
+    if ((on != 0) != pl->profiling) {
+        // Event records are part of the captured graph: recapture.
+        if (pl->exec) { cudaGraphExecDestroy(pl->exec); pl->exec = nullptr; }
+        if (pl->graph) { cudaGraphDestroy(pl->graph); pl->graph = nullptr; }
+    }
+    pl->profiling = on != 0;
+    for (double& v : pl->stage_ms) v = 0.0;
+    pl->stage_frames = 0;
+    return AZU_OK;
+}
+
+extern "C" int azu_pipeline_stage_times(azu_pipeline* pl, double ms_total[5], int* frames) {
+    AZU_CHECK_ARG(pl != nullptr && ms_total != nullptr, "null argument");
+    for (int k = 0; k < 5; ++k) ms_total[k] = pl->stage_ms[k];
+    if (frames) *frames = pl->stage_frames;
+    return AZU_OK;
+}
+
+extern "C" int azu_pipeline_uses_graph(azu_pipeline* pl) {
+    return pl ? (pl->p.use_graph && !pl->graph_failed ? 1 : 0) : 0;
+}

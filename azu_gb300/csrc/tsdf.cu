@@ -242,7 +242,10 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     }
     if (lane == 0) {
         if (n_new) atomicAdd(&counters[0], n_new);
-        if (n_upd) atomicAdd(&counters[1], n_upd);
+        if (n_upd) {
+            atomicAdd(&counters[1], n_upd);
+            atomicAdd(&counters[3], n_upd);
+        }
         if (n_col) atomicAdd(&counters[2], n_col);
     }
 }
@@ -645,6 +648,7 @@ extern "C" int azu_volume_get_stats(azu_volume* v, azu_volume_stats* s) {
     s->last_voxels_updated = static_cast<int64_t>(c[1]);
     s->last_color_updates = static_cast<int64_t>(c[2]);
     s->voxels = static_cast<int64_t>(v->p.resolution) * v->p.resolution * v->p.resolution;
+    s->total_voxels_updated = static_cast<int64_t>(c[3]);
     return AZU_OK;
 }
 

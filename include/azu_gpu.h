@@ -108,6 +108,7 @@ typedef struct {
     int64_t last_voxels_updated; /* voxels updated by the last integrate */
     int64_t last_color_updates;
     int64_t voxels;              /* res^3 */
+    int64_t total_voxels_updated; /* voxel updates since reset (sum over integrations) */
 } azu_volume_stats;
 /* Synchronises the volume's stream. */
 int azu_volume_get_stats(azu_volume* v, azu_volume_stats* s);
@@ -297,6 +298,17 @@ azu_tracker* azu_pipeline_tracker(azu_pipeline* p);
 int azu_pipeline_model_maps(azu_pipeline* p, const float** d_vertices, const float** d_normals);
 /* The pipeline's stream (cudaStream_t). */
 void* azu_pipeline_stream(azu_pipeline* p);
+/* Per-stage device timing (the reference's FrameTrace ms_preprocess / ms_icp /
+ * ms_integrate / ms_raycast columns, include/app/FrameTrace.h:40-88): when on,
+ * CUDA events bracket the stages of every frame and each synchronous call adds
+ * the frame's stage times to running totals. Turning it on or off clears the
+ * totals (and recaptures the frame graph). */
+int azu_pipeline_set_profiling(azu_pipeline* p, int on);
+/* Totals in ms for {input (preprocess), frame (vertices/normals/pyramid),
+ * track (predict + ICP), integrate, raycast} and the frames they cover. */
+int azu_pipeline_stage_times(azu_pipeline* p, double ms_total[5], int* frames);
+/* 1 when frames k > 0 replay a captured CUDA graph. */
+int azu_pipeline_uses_graph(azu_pipeline* p);
 
 #ifdef __cplusplus
 }

@@ -224,6 +224,22 @@ def icp_build_system(prm, K, live_v, live_n, model_v, model_n, pose, ref_pose):
                 projected=int(counts[3]), dist_filtered=int(counts[4]), angle_filtered=int(counts[5]))
 
 
+def icp_build_system_f64(prm, K, live_v, live_n, model_v, model_n, pose, ref_pose):
+    """The same association with the per-pixel float terms summed in double."""
+    H, W = live_v.shape[:2]
+    MH, MW = model_v.shape[:2]
+    A = np.zeros(36, np.float64)
+    b = np.zeros(6, np.float64)
+    counts = np.zeros(6, np.int32)
+    lib().orc_icp_build_system_f64(
+        C.byref(prm), K, _p(np.ascontiguousarray(live_v, np.float32)),
+        _p(np.ascontiguousarray(live_n, np.float32)), W, H,
+        _p(np.ascontiguousarray(model_v, np.float32)), _p(np.ascontiguousarray(model_n, np.float32)),
+        MW, MH, _p(_pose(pose)), _p(_pose(ref_pose)), _p(A, C.c_double), _p(b, C.c_double),
+        _p(counts, C.c_int))
+    return dict(A=A.reshape(6, 6), b=b, inliers=int(counts[0]))
+
+
 def icp_track(prm, K, levels, model_v, model_n, estimate, ref_pose):
     """levels: [(depth, vertices, normals)] x 3 as from frame_pyramid_from_depth."""
     H, W = levels[0][1].shape[:2]
@@ -284,3 +300,88 @@ def cpu_depth_meters(raw, lo, hi):
 def meters_to_raw(m, lo, hi):
     lib().orc_meters_to_raw.restype = C.c_uint16
     return lib().orc_meters_to_raw(C.c_float(m), C.c_float(lo), C.c_float(hi))
+
+
+def predict(cur, last):
+    out = np.zeros(16, np.float32)
+    lib().orc_predict(_p(_pose(cur)), _p(_pose(last)), _p(out))
+    return out.reshape(4, 4)
+
+
+class Lockstep:
+    """The CPU pipeline in lockstep, as the reference's offline replay drives its
+    tracking and integration workers (src/app/PipelineController.cpp:1003-1406,
+    1624-1905): frame 0 at identity; constant-velocity prediction; ICP against
+    the last raycast model (ref = model pose); a Failed grade retries from the
+    previous pose; Good frames are integrated and the model is raycast at the
+    new pose; Poor frames move the pose only; Failed keeps it.
+
+    depth is uint16 mm (input_is_mm) or Kinect raw codes (preprocessed with rgb).
+    Stage wall times (s) accumulate in self.times.
+    """
+
+    def __init__(self, vol: dict, K=(525.0, 525.0, 319.5, 239.5), W=640, H=480, min_depth=0.3, max_depth=2.5,
+                 icp=None, input_is_mm=True, minimal=False, fold_threads=1):
+        import time
+        self._clock = time.perf_counter
+        prm = dict(vol)
+        prm.pop("format", None)
+        self.vol = Volume(tsdf_params(**prm, min_depth=min_depth, max_depth=max_depth))
+        self.K = intr(*K)
+        self.W, self.H = W, H
+        self.lo, self.hi = min_depth, max_depth
+        self.icp = icp or icp_params(fold_threads=fold_threads)
+        self.input_is_mm = input_is_mm
+        self.pre = None if input_is_mm else Preprocessor(minimal=minimal)
+        self.cur = np.eye(4, dtype=np.float32)
+        self.last = np.eye(4, dtype=np.float32)
+        self.model = None
+        self.model_pose = np.eye(4, dtype=np.float32)
+        self.frames = 0
+        self.times = dict(preprocess=0.0, frame=0.0, track=0.0, integrate=0.0, raycast=0.0)
+
+    def depth_meters(self, depth, rgb=None):
+        if self.input_is_mm:
+            m = depth.astype(np.float32) * np.float32(0.001)
+            return np.where(np.isfinite(m) & (m >= np.float32(self.lo)) & (m <= np.float32(self.hi)), m,
+                            np.float32(0)).astype(np.float32)
+        d, _, _ = self.pre.process(depth, rgb, self.lo, self.hi)
+        return build_frame_raw(d, self.K, self.lo, self.hi)[0]
+
+    def process(self, depth, rgb=None) -> dict:
+        t0 = self._clock()
+        dm = self.depth_meters(depth, rgb)
+        t1 = self._clock()
+        levels = frame_pyramid_from_depth(dm, self.K)
+        t2 = self._clock()
+        quality, res = -1, None
+        if self.frames == 0:
+            self.cur = np.eye(4, dtype=np.float32)
+            gate = True
+        else:
+            prev = self.cur.copy()
+            pred = predict(self.cur, self.last)
+            self.last = self.cur.copy()
+            mv, mn = self.model
+            res = icp_track(self.icp, self.K, levels, mv, mn, pred, self.model_pose)
+            if classify_tracking(res, prev) == 2:
+                res = icp_track(self.icp, self.K, levels, mv, mn, prev, self.model_pose)
+            quality = classify_tracking(res, prev)
+            if quality != 2:
+                self.cur = np.array(res.pose, np.float32).reshape(4, 4)
+            gate = quality == 0
+        t3 = self._clock()
+        if gate:
+            self.vol.integrate(dm, self.cur, self.K, self.W, self.H, self.lo, self.hi)
+        t4 = self._clock()
+        if gate:
+            r = self.vol.raycast(self.cur, self.K, self.W, self.H)
+            self.model = (r["vertices"], r["normals"])
+            self.model_pose = self.cur.copy()
+        t5 = self._clock()
+        for k, a, b in (("preprocess", t0, t1), ("frame", t1, t2), ("track", t2, t3), ("integrate", t3, t4),
+                        ("raycast", t4, t5)):
+            self.times[k] += b - a
+        self.frames += 1
+        return dict(pose=self.cur.copy(), quality=quality, integrated=bool(gate),
+                    icp=None if res is None else res.as_dict())

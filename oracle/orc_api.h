@@ -91,6 +91,14 @@ int orc_icp_build_system(const orc_icp_params* prm, orc_intrinsics camK,
                          const float pose[16], const float ref_pose[16],
                          float A[36], float b[6], float* residual, int counts[6]);
 
+/* The same pass with the per-pixel float terms accumulated in double (the FP64
+ * reduction oracle). */
+int orc_icp_build_system_f64(const orc_icp_params* prm, orc_intrinsics camK,
+                             const float* live_v, const float* live_n, int W, int H,
+                             const float* model_v, const float* model_n, int MW, int MH,
+                             const float pose[16], const float ref_pose[16],
+                             double A[36], double b[6], int counts[6]);
+
 /* ICPTracker::track (src/tracking/ICPTracker.cpp:40-134) over a 3-level live
  * pyramid: live_v[l], live_n[l] at (W >> l) x (H >> l). */
 void orc_icp_track(const orc_icp_params* prm, orc_intrinsics camK,
@@ -101,6 +109,10 @@ void orc_icp_track(const orc_icp_params* prm, orc_intrinsics camK,
 /* tracking::classifyTracking (include/tracking/TrackingPolicy.h:70-112):
  * 0 = Good, 1 = Poor, 2 = Failed. */
 int orc_classify_tracking(const orc_icp_result* r, const float prev_pose[16]);
+
+/* Constant-velocity prediction (src/app/PipelineController.cpp:1175-1177):
+ * pred = cur * (last^-1 * cur). */
+void orc_predict(const float cur[16], const float last[16], float pred[16]);
 
 /* MarchingCubes::extract (src/meshing/MarchingCubes.cpp:174-382). Two-phase:
  * call with positions == NULL to get counts (n_vertices, n_indices, truncated),

@@ -192,14 +192,23 @@ M3 angleAxis(float angle, V3 axis) {
     return r;
 }
 
+// S = float: the reference's per-thread float partial sums. S = double: the
+// same per-pixel float terms accumulated in double (the FP64 reduction oracle).
+template <typename S>
 struct Acc {
-    float A[21], b[6], residual;
+    S A[21], b[6], residual;
     int count, valid_live, valid_model, projected, dist_f, angle_f;
     Acc() : residual(0), count(0), valid_live(0), valid_model(0), projected(0), dist_f(0), angle_f(0) {
-        for (float& v : A) v = 0;
-        for (float& v : b) v = 0;
+        for (S& v : A) v = 0;
+        for (S& v : b) v = 0;
     }
 };
+
+template <typename S>
+int build_system_impl(const orc_icp_params* prm, orc_intrinsics camK, const float* live_v, const float* live_n,
+                      int W, int H, const float* model_v, const float* model_n, int MW, int MH,
+                      const float pose_rm[16], const float ref_rm[16], float Aout[36], float bout[6],
+                      float* residual, int counts[6], double* A64, double* b64);
 
 }  // namespace
 
@@ -208,6 +217,28 @@ extern "C" int orc_icp_build_system(const orc_icp_params* prm, orc_intrinsics ca
                                     const float* model_n, int MW, int MH, const float pose_rm[16],
                                     const float ref_rm[16], float Aout[36], float bout[6], float* residual,
                                     int counts[6]) {
+    if (prm->fold_threads <= 0)
+        return build_system_impl<double>(prm, camK, live_v, live_n, W, H, model_v, model_n, MW, MH, pose_rm, ref_rm,
+                                         Aout, bout, residual, counts, nullptr, nullptr);
+    return build_system_impl<float>(prm, camK, live_v, live_n, W, H, model_v, model_n, MW, MH, pose_rm, ref_rm,
+                                    Aout, bout, residual, counts, nullptr, nullptr);
+}
+
+extern "C" int orc_icp_build_system_f64(const orc_icp_params* prm, orc_intrinsics camK, const float* live_v,
+                                        const float* live_n, int W, int H, const float* model_v,
+                                        const float* model_n, int MW, int MH, const float pose_rm[16],
+                                        const float ref_rm[16], double A64[36], double b64[6], int counts[6]) {
+    float A[36], b[6], r;
+    return build_system_impl<double>(prm, camK, live_v, live_n, W, H, model_v, model_n, MW, MH, pose_rm, ref_rm, A,
+                                     b, &r, counts, A64, b64);
+}
+
+namespace {
+template <typename S>
+int build_system_impl(const orc_icp_params* prm, orc_intrinsics camK, const float* live_v, const float* live_n,
+                      int W, int H, const float* model_v, const float* model_n, int MW, int MH,
+                      const float pose_rm[16], const float ref_rm[16], float Aout[36], float bout[6],
+                      float* residual, int counts[6], double* A64, double* b64) {
     for (int i = 0; i < 36; ++i) Aout[i] = 0;
     for (int i = 0; i < 6; ++i) { bout[i] = 0; counts[i] = 0; }
     *residual = 0;
@@ -230,8 +261,8 @@ extern "C" int orc_icp_build_system(const orc_icp_params* prm, orc_intrinsics ca
     const V3 t_rel = R_rc * t_cw + t_rc;
     const M3 R_cwT = R_cw.T();
 
-    const int T = std::max(1, prm->fold_threads);
-    std::vector<Acc> local(T);
+    const int T = prm->fold_threads > 0 ? prm->fold_threads : 64;
+    std::vector<Acc<S>> local(T);
     const int nrows = std::max(0, H - 2);
 #pragma omp parallel for schedule(static)
     for (int tid = 0; tid < T; ++tid) {
@@ -239,7 +270,7 @@ extern "C" int orc_icp_build_system(const orc_icp_params* prm, orc_intrinsics ca
         int q = nrows / T, t = nrows % T;
         if (tid < t) { t = 0; ++q; }
         const int s0 = q * tid + t, e0 = s0 + q;
-        Acc& acc = local[tid];
+        Acc<S>& acc = local[tid];
         for (int yy = s0; yy < e0; ++yy) {
             const int y = 1 + yy;
             for (int x = 1; x < W - 1; ++x) {
@@ -281,24 +312,24 @@ extern "C" int orc_icp_build_system(const orc_icp_params* prm, orc_intrinsics ca
                 const float we = err * w;
                 int k = 0;
                 for (int i = 0; i < 6; ++i) {
-                    for (int j = i; j < 6; ++j) acc.A[k++] += w * J[i] * J[j];
-                    acc.b[i] -= J[i] * we;
+                    for (int j = i; j < 6; ++j) acc.A[k++] += static_cast<S>(w * J[i] * J[j]);
+                    acc.b[i] -= static_cast<S>(J[i] * we);
                 }
-                acc.residual += huberLoss(ae);
+                acc.residual += static_cast<S>(huberLoss(ae));
                 acc.count++;
             }
         }
     }
-    float res = 0;
-    for (const Acc& a : local) {
+    S As[36] = {0}, bs[6] = {0}, res = 0;
+    for (const Acc<S>& a : local) {
         int k = 0;
         for (int i = 0; i < 6; ++i) {
             for (int j = i; j < 6; ++j) {
-                const float v = a.A[k++];
-                Aout[i * 6 + j] += v;
-                if (i != j) Aout[j * 6 + i] += v;
+                const S v = a.A[k++];
+                As[i * 6 + j] += v;
+                if (i != j) As[j * 6 + i] += v;
             }
-            bout[i] += a.b[i];
+            bs[i] += a.b[i];
         }
         res += a.residual;
         counts[0] += a.count;
@@ -308,9 +339,18 @@ extern "C" int orc_icp_build_system(const orc_icp_params* prm, orc_intrinsics ca
         counts[4] += a.dist_f;
         counts[5] += a.angle_f;
     }
-    *residual = res;
+    for (int i = 0; i < 36; ++i) {
+        Aout[i] = static_cast<float>(As[i]);
+        if (A64) A64[i] = static_cast<double>(As[i]);
+    }
+    for (int i = 0; i < 6; ++i) {
+        bout[i] = static_cast<float>(bs[i]);
+        if (b64) b64[i] = static_cast<double>(bs[i]);
+    }
+    *residual = static_cast<float>(res);
     return counts[0] > 0;
 }
+}  // namespace
 
 extern "C" void orc_icp_track(const orc_icp_params* prm, orc_intrinsics camK, const float* const live_v[3],
                               const float* const live_n[3], int W, int H, const float* model_v,
@@ -405,4 +445,12 @@ extern "C" int orc_classify_tracking(const orc_icp_result* r, const float prev_r
     const float ang = std::acos(c);
     if (!(trans <= 0.15f && ang <= 0.52f)) return 2;
     return q;
+}
+
+// Constant-velocity motion model (src/app/PipelineController.cpp:1175-1177):
+// predicted = current * (last^-1 * current).
+extern "C" void orc_predict(const float cur_rm[16], const float last_rm[16], float pred_rm[16]) {
+    const M4 cur = M4::from(cur_rm);
+    const M4 p = cur * (inverse4(M4::from(last_rm)) * cur);
+    p.to(pred_rm);
 }

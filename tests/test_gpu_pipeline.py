@@ -1,0 +1,58 @@
+"""The whole per-frame GPU pipeline (preprocess -> pyramid -> ICP -> integrate ->
+raycast, CUDA-graph replayed) against the oracle's lockstep CPU pipeline on
+the same frames: identical grades and integration decisions, poses within
+1e-5 rad / 1e-5 m after the whole sequence (FP32 solves on both sides, so
+per-frame rounding differences accumulate along the trajectory)."""
+import numpy as np
+import pytest
+
+import fixtures as F
+
+pytestmark = pytest.mark.gpu
+
+
+def _pipeline(seq, input_is_mm, use_graph=True, precision=0):
+    from azu_gb300 import api
+    v = seq.volume
+    vp = api.volume_params(v["resolution"], v["voxel_size"], v["truncation"], v["max_weight"], v["origin"],
+                           seq.min_depth, seq.max_depth, v["format"])
+    tp = api.tracker_params(min_depth=seq.min_depth, max_depth=seq.max_depth, precision=precision)
+    return api.Pipeline(api.pipeline_params(vp, tp, 0, seq.min_depth, seq.max_depth, input_is_mm, use_graph))
+
+
+@pytest.fixture(scope="module")
+def seq():
+    from azu_gb300 import synth
+    return synth.sequence("c1", frames=10)
+
+
+@pytest.mark.parametrize("input_is_mm", [False, True])
+def test_pipeline_matches_lockstep_oracle(cuda_lib, orc, seq, input_is_mm):
+    from azu_gb300 import synth
+    pl = _pipeline(seq, input_is_mm)
+    L = orc.Lockstep(seq.volume, input_is_mm=input_is_mm, fold_threads=0)
+    rgb = synth.grey_rgb()
+    for k in range(len(seq.poses)):
+        d = seq.depth_mm[k] if input_is_mm else synth.encode_raw(seq.depth_mm[k])
+        g = pl.process_frame(d, None if input_is_mm else rgb)
+        o = L.process(d, rgb)
+        assert g["frame_index"] == k
+        assert g["quality"] == o["quality"], k
+        assert g["integrated"] == o["integrated"], k
+        rot, trans = F.rel_pose_error(g["pose"], o["pose"])
+        assert rot <= 1e-5 and trans <= 1e-5, (k, rot, trans)
+        if k:
+            assert g["icp"]["status"] == 0
+            assert abs(g["icp"]["inliers"] - o["icp"]["inliers"]) <= max(5, 2e-4 * o["icp"]["inliers"])
+            rot_gt, trans_gt = F.rel_pose_error(g["pose"], seq.poses[k])
+            assert rot_gt < 5e-3 and trans_gt < 1e-2, (k, rot_gt, trans_gt)
+
+
+def test_graph_replay_equals_eager(cuda_lib, seq):
+    a = _pipeline(seq, True, use_graph=True)
+    b = _pipeline(seq, True, use_graph=False)
+    for k in range(5):
+        ra = a.process_frame(seq.depth_mm[k])
+        rb = b.process_frame(seq.depth_mm[k])
+        assert np.array_equal(ra["pose"], rb["pose"]) and ra["quality"] == rb["quality"]
+    assert a.lib.azu_pipeline_uses_graph(a.h) == 1
