@@ -54,7 +54,7 @@ class IcpResult(C.Structure):
 
 
 class MeshInfo(C.Structure):
-    _fields_ = [("n_vertices", C.c_int64), ("n_indices", C.c_int64), ("truncated", C.c_int)]
+    _fields_ = [("n_vertices", C.c_int64), ("n_indices", C.c_int64), ("truncated", C.c_int), ("launches", C.c_int)]
 
 
 class PipelineParams(C.Structure):

@@ -38,9 +38,29 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None else None
 
 
+_lib_stream = None
+
+
+def lib_stream():
+    """The torch stream every handle of this module enqueues on (never the legacy
+    default stream, whose NULL handle would make the library create a private one)."""
+    global _lib_stream
+    if _lib_stream is None:
+        _lib_stream = _torch().cuda.Stream()
+    return _lib_stream
+
+
 def _stream_handle():
-    torch = _torch()
-    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return C.c_void_p(lib_stream().cuda_stream)
+
+
+def _ready():
+    """Inputs written on the caller's torch stream are complete before library work."""
+    _torch().cuda.current_stream().synchronize()
+
+
+def _done():
+    lib_stream().synchronize()
 
 
 def volume_params(resolution, voxel_size, truncation, max_weight=64.0, origin=(0, 0, 0), min_depth=0.3,
@@ -93,6 +113,7 @@ class TSDFVolume:
         self.params = p
 
     def integrate_gpu(self, d_depth, pose, K, W, H, min_depth, max_depth, d_rgb=None):
+        _ready()
         check(self.lib.azu_volume_integrate(self.h, _ptr(d_depth), _ptr(d_rgb), _pose(pose), *map(float, K), W, H,
                                             float(min_depth), float(max_depth)), "integrate")
 
@@ -109,12 +130,14 @@ class TSDFVolume:
         v = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
         n = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
         c = torch.empty((H, W, 3), dtype=torch.uint8, device="cuda") if colors else None
+        _ready()
         check(self.lib.azu_volume_raycast(self.h, _pose(pose), *map(float, K), W, H, _ptr(v), _ptr(n), _ptr(c)),
               "raycast")
         return v, n, c
 
     def raycast(self, pose, K, W, H, colors=False):
         v, n, c = self.raycast_gpu(pose, K, W, H, colors)
+        _done()
         out = dict(vertices=v.cpu().numpy(), normals=n.cpu().numpy())
         if colors:
             out["colors"] = c.cpu().numpy()
@@ -158,18 +181,22 @@ class ICPTracker:
     __del__ = close
 
     def prepare_live(self, d_depth, W, H):
+        _ready()
         check(self.lib.azu_tracker_prepare_live(self.h, _ptr(d_depth), W, H), "prepare_live")
 
     def load_live(self, level, d_v, d_n, W, H):
+        _ready()
         check(self.lib.azu_tracker_load_live(self.h, level, _ptr(d_v), _ptr(d_n), W, H), "load_live")
 
     def track_prepared(self, W, H, d_mv, d_mn, MW, MH, estimate, ref_pose) -> dict:
+        _ready()
         r = _abi.IcpResult()
         check(self.lib.azu_tracker_track_prepared(self.h, W, H, _ptr(d_mv), _ptr(d_mn), MW, MH, _pose(estimate),
                                                   _pose(ref_pose), C.byref(r)), "track_prepared")
         return result_dict(r)
 
     def build_system(self, level, d_mv, d_mn, MW, MH, pose, ref_pose) -> dict:
+        _ready()
         A = (C.c_float * 36)()
         b = (C.c_float * 6)()
         res = C.c_float()
@@ -200,7 +227,8 @@ class _DevArray:
 
 def device_to_host(ptr: int, shape, dtype) -> np.ndarray:
     torch = _torch()
-    torch.cuda.current_stream().synchronize()
+    _done()
+    torch.cuda.synchronize()
     return torch.as_tensor(_DevArray(ptr, shape, dtype), device="cuda").cpu().numpy().copy()
 
 
@@ -242,11 +270,19 @@ class Preprocessor:
 
 
 class MarchingCubes:
-    def __init__(self, device: int = 0, max_triangles: int = 2_000_000):
+    def __init__(self, device: int = 0, max_triangles: int = 2_000_000, stream: int | None = None):
         self.lib = _abi.load()
         self.h = C.c_void_p()
-        check(self.lib.azu_mesher_create(device, _stream_handle(), C.byref(self.h)), "azu_mesher_create")
+        st = C.c_void_p(stream) if stream is not None else _stream_handle()
+        check(self.lib.azu_mesher_create(device, st, C.byref(self.h)), "azu_mesher_create")
         self.set_max_triangles(max_triangles)
+
+    def extract_counts(self, vol_handle) -> dict:
+        """extractGPU without the host copy: counts only, mesh stays on the device."""
+        info = _abi.MeshInfo()
+        check(self.lib.azu_mesher_extract(self.h, vol_handle, C.byref(info)), "extract")
+        return dict(n_vertices=info.n_vertices, n_indices=info.n_indices, truncated=bool(info.truncated),
+                    launches=info.launches)
 
     def close(self):
         if self.h:
@@ -292,12 +328,52 @@ class Pipeline:
 
     __del__ = close
 
+    @staticmethod
+    def _frame(r: _abi.FrameResult) -> dict:
+        return dict(pose=np.array(r.pose, np.float32).reshape(4, 4), icp=result_dict(r.icp), quality=r.quality,
+                    integrated=bool(r.integrated), frame_index=r.frame_index)
+
     def process_frame(self, depth: np.ndarray, rgb: np.ndarray | None = None) -> dict:
+        """One frame from host buffers (H2D, whole frame on the device, D2H)."""
         r = _abi.FrameResult()
         d = np.ascontiguousarray(depth, np.uint16)
         c = None if rgb is None else np.ascontiguousarray(rgb, np.uint8)
         check(self.lib.azu_pipeline_process_frame(self.h, d.ctypes.data_as(C.c_void_p),
                                                   None if c is None else c.ctypes.data_as(C.c_void_p),
                                                   C.byref(r)), "process_frame")
-        return dict(pose=np.array(r.pose, np.float32).reshape(4, 4), icp=result_dict(r.icp), quality=r.quality,
-                    integrated=bool(r.integrated), frame_index=r.frame_index)
+        return self._frame(r)
+
+    def process_frame_device(self, d_depth_ptr: int, d_rgb_ptr: int | None = None, sync: bool = False):
+        """One frame from device buffers; only enqueued unless sync."""
+        r = _abi.FrameResult() if sync else None
+        check(self.lib.azu_pipeline_process_frame_device(self.h, C.c_void_p(d_depth_ptr),
+                                                         None if d_rgb_ptr is None else C.c_void_p(d_rgb_ptr),
+                                                         C.byref(r) if sync else None), "process_frame_device")
+        return self._frame(r) if sync else None
+
+    def last_result(self) -> dict:
+        r = _abi.FrameResult()
+        check(self.lib.azu_pipeline_last_result(self.h, C.byref(r)), "last_result")
+        return self._frame(r)
+
+    @property
+    def stream(self) -> int:
+        return self.lib.azu_pipeline_stream(self.h)
+
+    def set_profiling(self, on: bool):
+        check(self.lib.azu_pipeline_set_profiling(self.h, int(bool(on))), "set_profiling")
+
+    def stage_times(self):
+        ms = (C.c_double * 5)()
+        n = C.c_int()
+        check(self.lib.azu_pipeline_stage_times(self.h, ms, C.byref(n)), "stage_times")
+        return dict(zip(("input", "frame", "track", "integrate", "raycast"), list(ms))), n.value
+
+    def volume_stats(self) -> dict:
+        s = _abi.VolumeStats()
+        check(self.lib.azu_volume_get_stats(self.lib.azu_pipeline_volume(self.h), C.byref(s)), "stats")
+        return dict(observed_voxels=s.observed_voxels, total_voxels_updated=s.total_voxels_updated,
+                    last_voxels_updated=s.last_voxels_updated)
+
+    def volume_handle(self):
+        return C.c_void_p(self.lib.azu_pipeline_volume(self.h))

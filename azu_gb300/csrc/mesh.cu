@@ -325,6 +325,9 @@ __global__ void weld_write_kernel(unsigned nslots, const unsigned* __restrict__ 
     }
 }
 
+// Kernels launched by the current extraction (reported in azu_mesh_info).
+static thread_local int t_launches = 0;
+
 // ---- generic exclusive scan of uint32 (in place), multi-level -----------------
 constexpr int kScanThreads = 512, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
 
@@ -380,14 +383,17 @@ int exclusive_scan(unsigned* data, size_t n, unsigned* scratch, unsigned* total_
     if (tiles == 1) {
         scan_tile_kernel<<<1, kScanThreads, 0, s>>>(data, n, total_dev);
         AZU_LAUNCH_CHECK();
+        ++t_launches;
         return AZU_OK;
     }
     unsigned* sums = scratch;
     scan_tile_kernel<<<static_cast<unsigned>(tiles), kScanThreads, 0, s>>>(data, n, sums);
     AZU_LAUNCH_CHECK();
+    ++t_launches;
     if (int rc = exclusive_scan(sums, tiles, scratch + tiles, total_dev, s)) return rc;
     scan_add_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(data, n, sums);
     AZU_LAUNCH_CHECK();
+    ++t_launches;
     return AZU_OK;
 }
 
@@ -510,7 +516,8 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     cudaStream_t s = m->stream.s;
     // The volume may be written on its own stream: order after it.
     if (v->stream.s != s) AZU_TRY_CUDA(cudaStreamSynchronize(v->stream.s));
-    *info = azu_mesh_info{0, 0, 0};
+    *info = azu_mesh_info{0, 0, 0, 0};
+    t_launches = 0;
     const int res = v->p.resolution;
     const long long cr = res - 1;
     const long long ncubes = cr * cr * cr;
@@ -522,6 +529,7 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     if (int rc = grow(m->scratch, m->scratch_cap, scan_scratch_words(std::max<size_t>(nblocks, 1 << 24)))) return rc;
     mc_classify_kernel<<<static_cast<unsigned>(nblocks), kCubeBlock, 0, s>>>(mv, ncubes, m->counts, m->block_sums);
     AZU_LAUNCH_CHECK();
+    ++t_launches;
     if (int rc = exclusive_scan(m->block_sums, nblocks, m->scratch, m->d_scalars, s)) return rc;
     unsigned total = 0;
     AZU_TRY_CUDA(cudaMemcpyAsync(&total, m->d_scalars, 4, cudaMemcpyDeviceToHost, s));
@@ -529,12 +537,13 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     const unsigned cap = static_cast<unsigned>(std::min<int64_t>(m->max_triangles, total));
     const size_t nslots = 3 * static_cast<size_t>(cap);
     info->truncated = total > cap ? 1 : 0;
-    if (cap == 0) { m->last = *info; return AZU_OK; }
+    if (cap == 0) { info->launches = t_launches; m->last = *info; return AZU_OK; }
     if (int rc = ensure_slots(m, nslots)) return rc;
     mc_emit_kernel<<<static_cast<unsigned>(nblocks), kCubeBlock, 0, s>>>(mv, ncubes, m->counts, m->block_sums, cap,
                                                                          m->slot_key, m->slot_pos, m->slot_nrm,
                                                                          m->slot_col);
     AZU_LAUNCH_CHECK();
+    ++t_launches;
     size_t tsize = 1024;
     while (tsize < 2 * nslots) tsize <<= 1;
     if (tsize > m->table_cap || !m->tkeys) {
@@ -557,17 +566,20 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     weld_flag_kernel<<<g, 256, 0, s>>>(m->slot_key, static_cast<unsigned>(nslots), m->tkeys, m->tvals, mask,
                                        m->first_slot, m->vid);
     AZU_LAUNCH_CHECK();
+    t_launches += 2;
     if (int rc = grow(m->scratch, m->scratch_cap, std::max(m->scratch_cap, scan_scratch_words(nslots)))) return rc;
     if (int rc = exclusive_scan(m->vid, nslots, m->scratch, m->d_scalars + 1, s)) return rc;
     weld_write_kernel<<<g, 256, 0, s>>>(static_cast<unsigned>(nslots), m->first_slot, m->vid, m->slot_pos,
                                         m->slot_nrm, m->slot_col, m->indices, m->pos, m->nrm, m->col);
     AZU_LAUNCH_CHECK();
+    ++t_launches;
     unsigned sc[3];
     AZU_TRY_CUDA(cudaMemcpyAsync(sc, m->d_scalars, sizeof(sc), cudaMemcpyDeviceToHost, s));
     AZU_TRY_CUDA(cudaStreamSynchronize(s));
     if (sc[2]) { set_error("weld table overflow"); return AZU_E_CUDA; }
     info->n_vertices = sc[1];
     info->n_indices = static_cast<int64_t>(nslots);
+    info->launches = t_launches;
     m->last = *info;
     return AZU_OK;
 }

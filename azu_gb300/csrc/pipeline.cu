@@ -109,7 +109,8 @@ static const float* depth_source(azu_pipeline* pl) {
 }
 
 static int mark(azu_pipeline* pl, int k) {
-    if (pl->profiling) AZU_TRY_CUDA(cudaEventRecord(pl->ev[k], pl->s));
+    // External records stay ordinary, host-visible events when captured into the graph.
+    if (pl->profiling) AZU_TRY_CUDA(cudaEventRecordWithFlags(pl->ev[k], pl->s, cudaEventRecordExternal));
     return AZU_OK;
 }
 
@@ -204,11 +205,15 @@ static int read_result(azu_pipeline* pl, azu_frame_result* out) {
     AZU_TRY_CUDA(cudaMemcpyAsync(&out->icp, pl->d_icp, sizeof(azu_icp_result), cudaMemcpyDeviceToHost, pl->s));
     AZU_TRY_CUDA(cudaStreamSynchronize(pl->s));
     if (pl->profiling) {
-        for (int k = 0; k < 5; ++k) {
-            float ms = 0.0f;
-            if (cudaEventElapsedTime(&ms, pl->ev[k], pl->ev[k + 1]) == cudaSuccess) pl->stage_ms[k] += ms;
+        float ms[5];
+        bool ok = true;
+        for (int k = 0; k < 5 && ok; ++k) ok = cudaEventElapsedTime(&ms[k], pl->ev[k], pl->ev[k + 1]) == cudaSuccess;
+        if (ok) {
+            for (int k = 0; k < 5; ++k) pl->stage_ms[k] += ms[k];
+            pl->stage_frames++;
+        } else {
+            cudaGetLastError();  // an unreadable frame is skipped, not a sticky error
         }
-        pl->stage_frames++;
     }
     std::memcpy(out->pose, st.cur, sizeof(out->pose));
     out->quality = st.quality;

@@ -233,6 +233,7 @@ typedef struct {
     int64_t n_vertices;   /* welded vertices */
     int64_t n_indices;    /* 3 x triangles */
     int     truncated;    /* MeshData::truncated */
+    int     launches;     /* kernels the extraction launched */
 } azu_mesh_info;
 
 int azu_mesher_create(int device, void* stream, azu_mesher** out);

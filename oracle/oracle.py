@@ -385,3 +385,19 @@ class Lockstep:
         self.frames += 1
         return dict(pose=self.cur.copy(), quality=quality, integrated=bool(gate),
                     icp=None if res is None else res.as_dict())
+
+
+class PrecisionVolume(Volume):
+    """FP16-storage emulation (half_storage=True) or FP32, plus the FP64 running
+    average of the same updates in `tsdf64`."""
+
+    def __init__(self, p: TsdfParams, half_storage: bool, fp64: bool = True):
+        super().__init__(p)
+        self.half = bool(half_storage)
+        self.tsdf64 = np.ones(p.res ** 3, np.float64) if fp64 else None
+
+    def integrate(self, depth_m, pose, K, W, H, min_depth, max_depth, rgb=None):
+        depth_m = np.ascontiguousarray(depth_m, np.float32)
+        lib().orc_tsdf_integrate_prec(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.tsdf64, C.c_double),
+                                      _p(depth_m), _p(_pose(pose)), K, int(W), int(H), C.c_float(min_depth),
+                                      C.c_float(max_depth), int(self.half))

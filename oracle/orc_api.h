@@ -41,6 +41,14 @@ void orc_tsdf_integrate(const orc_tsdf_params* p, float* tsdf, float* weight, fl
                         orc_intrinsics K, int W, int H, float min_depth, float max_depth,
                         int64_t stats[9]);
 
+/* Precision form of orc_tsdf_integrate (same projections and decisions):
+ * half_storage != 0 stores the tsdf rounded to IEEE half after each update (the
+ * FP16 + u16 volume); tsdf64 (may be NULL) carries the same running average in
+ * double (the FP64 reference). No colour. */
+void orc_tsdf_integrate_prec(const orc_tsdf_params* p, float* tsdf, float* weight, double* tsdf64,
+                             const float* depth_m, const float pose[16], orc_intrinsics K, int W, int H,
+                             float min_depth, float max_depth, int half_storage);
+
 /* TSDFVolume::raycast (src/tsdf/TSDFVolume.cpp:348-476). colors_out may be NULL;
  * color may be NULL (every voxel then carries EMPTY_COLOR). samples_out (may
  * be NULL) receives the number of trilinear samples taken. */

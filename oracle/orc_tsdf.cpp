@@ -299,3 +299,69 @@ extern "C" int orc_get_threads(void) {
     return 1;
 #endif
 }
+
+// Precision form of the same integration: identical projections and decisions
+// (float camera stepping), with
+//   half_storage != 0: the tsdf stored rounded to IEEE half (round to nearest
+//                      even) after every update, i.e. the FP16 + u16 volume;
+//   tsdf64 != NULL:    the running average of the same float tsdf_new values
+//                      carried in double (the FP64 reference).
+extern "C" void orc_tsdf_integrate_prec(const orc_tsdf_params* p, float* tsdf, float* weight, double* tsdf64,
+                                        const float* depth_m, const float pose_rm[16], orc_intrinsics K, int width,
+                                        int height, float min_depth, float max_depth, int half_storage) {
+    const float trunc = p->truncation, max_w = p->max_weight, vs = p->voxel_size;
+    const int res = p->res;
+    const V3 origin = originOf(p);
+    const M4 pose = M4::from(pose_rm);
+    const M4 world_to_cam = inverse4(pose);
+    const M3 R_wc = world_to_cam.R();
+    const V3 t_wc = world_to_cam.t();
+    const M3 R_cw = pose.R();
+    const V3 t_cw = pose.t();
+    V3 lo = (t_cw - origin) / vs, hi = lo;
+    const float z_far = max_depth + trunc;
+    const float corner_px[4][2] = {{0.0f, 0.0f}, {float(width), 0.0f}, {0.0f, float(height)},
+                                   {float(width), float(height)}};
+    for (const auto& c : corner_px) {
+        const V3 ray((c[0] - K.cx) / K.fx * z_far, (c[1] - K.cy) / K.fy * z_far, z_far);
+        const V3 v = ((R_cw * ray + t_cw) - origin) / vs;
+        lo = vmin(lo, v);
+        hi = vmax(hi, v);
+    }
+    if (!finite3(lo) || !finite3(hi)) return;
+    auto clampIdx = [res](float f) {
+        return static_cast<int>(std::max(0.0f, std::min(static_cast<float>(res - 1), f)));
+    };
+    const int x0 = clampIdx(std::floor(lo.x)), x1 = clampIdx(std::ceil(hi.x));
+    const int y0 = clampIdx(std::floor(lo.y)), y1 = clampIdx(std::ceil(hi.y));
+    const int z0 = clampIdx(std::floor(lo.z)), z1 = clampIdx(std::ceil(hi.z));
+    const V3 step_x = R_wc.col(0) * vs;
+    const size_t rr = static_cast<size_t>(res);
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
+    for (int z = z0; z <= z1; ++z) {
+        for (int y = y0; y <= y1; ++y) {
+            V3 c = R_wc * (origin + V3(float(x0), float(y), float(z)) * vs) + t_wc;
+            for (int x = x0; x <= x1; ++x, c = c + step_x) {
+                if (c.z <= 0.0f) continue;
+                const float inv_z = 1.0f / c.z;
+                const float uf = std::floor(K.fx * c.x * inv_z + K.cx + 0.5f);
+                const float vf = std::floor(K.fy * c.y * inv_z + K.cy + 0.5f);
+                if (!(uf >= 0.0f && uf < static_cast<float>(width) && vf >= 0.0f && vf < static_cast<float>(height)))
+                    continue;
+                const float d = depth_m[static_cast<int>(vf) * width + static_cast<int>(uf)];
+                if (!(d >= min_depth && d <= max_depth)) continue;
+                const float sdf = d - c.z;
+                if (sdf < -trunc) continue;
+                const float tsdf_new = std::min(1.0f, sdf / trunc);
+                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(y)) * rr + static_cast<size_t>(x);
+                const float w_old = weight[vi];
+                const float t = (tsdf[vi] * w_old + tsdf_new) / (w_old + 1.0f);
+                tsdf[vi] = half_storage ? static_cast<float>(static_cast<_Float16>(t)) : t;
+                if (tsdf64)
+                    tsdf64[vi] = (tsdf64[vi] * static_cast<double>(w_old) + static_cast<double>(tsdf_new)) /
+                                 (static_cast<double>(w_old) + 1.0);
+                weight[vi] = std::min(w_old + 1.0f, max_w);
+            }
+        }
+    }
+}

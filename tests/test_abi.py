@@ -76,3 +76,21 @@ def test_synth_sequences_are_seeded():
     assert np.allclose(a.poses[0], np.eye(4))
     v = a.depth_mm[0]
     assert 0.3 < (v > 0).mean() < 0.9
+
+
+def test_header_compiles_as_c_and_cxx_and_links(lib_path, tmp_path):
+    """A C program and a C++ program including include/azu_gpu.h link against the
+    library (the reference-side adapters are C++)."""
+    src = tmp_path / "use.c"
+    src.write_text('#include "azu_gpu.h"\n#include <stdio.h>\n'
+                   'int main(void) { azu_volume* v = 0; azu_volume_params p = {0};\n'
+                   '  int rc = azu_volume_create(0, &p, 0, &v);\n'
+                   '  printf("%s %d\\n", azu_version(), rc == AZU_E_INVALID); return 0; }\n')
+    inc = os.path.join(ROOT, "include")
+    libdir = os.path.dirname(lib_path)
+    for cc, extra in (("gcc", ["-std=c99"]), ("g++", ["-std=c++17", "-x", "c++"])):
+        exe = tmp_path / ("use_" + cc.replace("+", "x"))
+        subprocess.run([cc] + extra + ["-Wall", "-Werror", "-I", inc, str(src), "-L", libdir, "-lazu_gb300",
+                                        "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+        out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+        assert "sm_103a" in out and out.strip().endswith("1")
