@@ -101,6 +101,9 @@ SIGNATURES = {
     "azu_tracker_build_system": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.c_int, fp, fp, fp, fp, fp,
                                            C.POINTER(C.c_int)]),
     "azu_tracker_load_live": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.c_int]),
+    "azu_icp_build_system_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int,
+                                               C.POINTER(TrackerParams), fp, fp, vp, fp, fp, fp,
+                                               C.POINTER(C.c_int)]),
     "azu_tracker_live_maps": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     # preprocessor
     "azu_preprocessor_create": (C.c_int, [C.c_int, C.c_int, vp, C.POINTER(vp)]),

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "azu_internal.h"
 #include "kf_math.cuh"
@@ -977,5 +978,154 @@ extern "C" int azu_tracker_load_live(azu_tracker* t, int level, const float* d_v
     AZU_TRY_CUDA(cudaMemcpyAsync(t->V[level], d_vertices, n, cudaMemcpyDeviceToDevice, t->stream.s));
     AZU_TRY_CUDA(cudaMemcpyAsync(t->N[level], d_normals, n, cudaMemcpyDeviceToDevice, t->stream.s));
     t->prepared = true;
+    return AZU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free association + reduction pass.
+//
+// For callers that must not allocate device memory once they run: a real-time
+// tracking loop that fixes its device-memory budget at start-up, or a host whose
+// device memory belongs to its own pool or arena that this library cannot draw
+// from (cudaMalloc also synchronises the device, which such loops avoid). The
+// caller passes the live and model maps (device) and the host outputs; the block
+// partials, barrier words, poses and result staging live in one file-scope
+// device array that every GPU loading the library holds until exit.
+//
+// Limit: the array holds partials for kStaticMaxBlocks (512) cooperative
+// blocks; the launch uses one block per 256 threads of co-resident occupancy
+// (at most 2 per SM, 304 on a GB300), and a device that would need more is
+// rejected with AZU_E_UNSUPPORTED. Images may be up to 8192 x 8192.
+//
+// The first call on a device resolves the array's device address with that
+// device current; make that first call before any stream capture. Every call
+// shares the one array and leaves its contents behind: the barrier words are
+// cleared at the start of each call, everything else is overwritten. Calls
+// that overlap on the GPU (other streams or threads) race on the array.
+namespace {
+constexpr int kStaticMaxBlocks = 512;
+constexpr size_t kStaticScratchBytes = 256 * 1024;
+constexpr size_t kOffPoses = 0;      // 32 floats: pose, ref_pose
+constexpr size_t kOffOut = 256;      // 49 words: A, b, residual, counts
+constexpr size_t kOffBar = 512;      // 4 words: arrivals, generation, error
+constexpr size_t kOffPartials = 1024;
+constexpr size_t kOffIPartials = kOffPartials + 2ull * kStaticMaxBlocks * azu::kNF * sizeof(double);
+static_assert(kOffIPartials + 2ull * kStaticMaxBlocks * azu::kNI * sizeof(int) <= kStaticScratchBytes,
+              "static scratch layout");
+constexpr int kStaticMaxDevices = 64;
+struct StaticSlot {
+    unsigned char* base = nullptr;
+    int nblocks = 0;
+};
+std::mutex g_static_mu;
+StaticSlot g_static_slot[kStaticMaxDevices];
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_icp_static_scratch[kStaticScratchBytes];
+
+static int static_slot_for_current_device(StaticSlot& out) {
+    int dev = -1;
+    AZU_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kStaticMaxDevices) {
+        set_error("device ordinal %d beyond the %d supported", dev, kStaticMaxDevices);
+        return AZU_E_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    StaticSlot& s = g_static_slot[dev];
+    if (!s.base) {
+        cudaDeviceProp prop;
+        AZU_TRY_CUDA(cudaGetDeviceProperties(&prop, dev));
+        if (prop.major * 10 + prop.minor != 103) {
+            set_error("device %d is sm_%d%d; this library is built for sm_103a (GB300) only", dev, prop.major,
+                      prop.minor);
+            return AZU_E_UNSUPPORTED;
+        }
+        void* p = nullptr;
+        AZU_TRY_CUDA(cudaGetSymbolAddress(&p, g_icp_static_scratch));
+        int occ = 0;
+        AZU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, icp_kernel, kIcpThreads, 0));
+        s.nblocks = prop.multiProcessorCount * std::min(occ, 2);
+        s.base = static_cast<unsigned char*>(p);
+    }
+    out = s;
+    return AZU_OK;
+}
+
+extern "C" int azu_icp_build_system_noalloc(const float* d_live_vertices, const float* d_live_normals, int width,
+                                            int height, const float* d_model_vertices, const float* d_model_normals,
+                                            int model_w, int model_h, const azu_tracker_params* params,
+                                            const float pose[16], const float ref_pose[16], void* stream,
+                                            float A[36], float b[6], float* residual, int counts[6]) {
+    AZU_CHECK_ARG(d_live_vertices && d_live_normals && d_model_vertices && d_model_normals && params && pose &&
+                      ref_pose && A && b && residual && counts,
+                  "null argument");
+    AZU_CHECK_ARG(width >= 3 && height >= 3 && width <= 8192 && height <= 8192, "live size must be in [3, 8192]");
+    AZU_CHECK_ARG(model_w > 0 && model_h > 0 && model_w <= 8192 && model_h <= 8192,
+                  "model size must be in [1, 8192]");
+    StaticSlot slot;
+    if (int rc = static_slot_for_current_device(slot)) return rc;
+    if (slot.nblocks > kStaticMaxBlocks) {
+        set_error("this device needs partials for %d blocks; the static scratch holds %d", slot.nblocks,
+                  kStaticMaxBlocks);
+        return AZU_E_UNSUPPORTED;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    float* d_poses = reinterpret_cast<float*>(slot.base + kOffPoses);
+    float* d_out = reinterpret_cast<float*>(slot.base + kOffOut);
+    unsigned* d_bar = reinterpret_cast<unsigned*>(slot.base + kOffBar);
+    if (int rc = set_pose_async(d_poses, pose, s)) return rc;
+    if (int rc = set_pose_async(d_poses + 16, ref_pose, s)) return rc;
+    AZU_TRY_CUDA(cudaMemsetAsync(d_bar, 0, 4 * sizeof(unsigned), s));
+
+    const azu_tracker_params p = sanitize(*params);
+    IcpArgs a;
+    std::memset(&a, 0, sizeof(a));
+    for (int l = 0; l < 3; ++l) a.lv[l] = IcpLevel{d_live_vertices, d_live_normals, width, height};
+    a.mv = d_model_vertices;
+    a.mn = d_model_normals;
+    a.MW = model_w;
+    a.MH = model_h;
+    if (model_w == 640 && model_h == 480) {
+        a.fx = p.fx; a.fy = p.fy; a.cx = p.cx; a.cy = p.cy;
+    } else {
+        const float sx = static_cast<float>(model_w) / 640.0f, sy = static_cast<float>(model_h) / 480.0f;
+        a.fx = p.fx * sx; a.fy = p.fy * sy; a.cx = (p.cx + 0.5f) * sx - 0.5f; a.cy = (p.cy + 0.5f) * sy - 0.5f;
+    }
+    a.dist2 = p.dist_threshold * p.dist_threshold;
+    a.angle_cos = static_cast<float>(std::cos(p.angle_threshold * M_PI / 180.0f));
+    for (int l = 0; l < 3; ++l) a.iters[l] = p.max_iterations[l];
+    a.precision = p.precision;
+    a.build_level = 0;
+    a.d_estimate = d_poses;
+    a.d_ref = d_poses + 16;
+    a.partials = reinterpret_cast<double*>(slot.base + kOffPartials);
+    a.ipartials = reinterpret_cast<int*>(slot.base + kOffIPartials);
+    a.bar = d_bar;
+    a.err = d_bar + 2;
+    a.build_out = d_out;
+
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(slot.nblocks);
+    cfg.blockDim = dim3(kIcpThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    AZU_TRY_CUDA(cudaLaunchKernelEx(&cfg, icp_kernel, a));
+    float out[49];
+    unsigned err = 0;
+    AZU_TRY_CUDA(cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s));
+    AZU_TRY_CUDA(cudaMemcpyAsync(&err, d_bar + 2, sizeof(err), cudaMemcpyDeviceToHost, s));
+    AZU_TRY_CUDA(cudaStreamSynchronize(s));
+    if (err) {
+        set_error("ICP grid barrier timed out");
+        return AZU_E_TIMEOUT;
+    }
+    std::memcpy(A, out, 36 * sizeof(float));
+    std::memcpy(b, out + 36, 6 * sizeof(float));
+    *residual = out[42];
+    std::memcpy(counts, out + 43, 6 * sizeof(int));
     return AZU_OK;
 }

@@ -185,6 +185,24 @@ int azu_tracker_build_system(azu_tracker* t, int level, const float* d_model_ver
  * the tracker prepared for width x height. Enqueue only. */
 int azu_tracker_load_live(azu_tracker* t, int level, const float* d_vertices, const float* d_normals, int width,
                           int height);
+/* No counterpart in the reference. The association + reduction pass of
+ * azu_tracker_build_system for callers that must not allocate device memory
+ * once they run (a real-time loop with a device-memory budget fixed at
+ * start-up, or a host whose device memory belongs to its own pool): it needs
+ * no handle and calls no cudaMalloc. Live maps (width x height) and model maps
+ * are device float3 maps; poses and outputs are host memory; `stream` may be
+ * NULL (the legacy default stream). Its scratch is one file-scope device array
+ * of 256 KiB (partials for at most 512 cooperative blocks) that every GPU
+ * loading the library keeps until exit; a device needing more blocks is
+ * rejected with AZU_E_UNSUPPORTED, images larger than 8192 x 8192 with
+ * AZU_E_INVALID. The first call on a device sets the array up (with that
+ * device current) and should come before any stream capture. All calls share
+ * the array: calls that overlap on the GPU race. Synchronous. */
+int azu_icp_build_system_noalloc(const float* d_live_vertices, const float* d_live_normals, int width, int height,
+                                 const float* d_model_vertices, const float* d_model_normals, int model_w,
+                                 int model_h, const azu_tracker_params* params, const float pose[16],
+                                 const float ref_pose[16], void* stream, float A[36], float b[6], float* residual,
+                                 int counts[6]);
 /* Device pointers of the live pyramid (float3 maps and depth) at a level. */
 int azu_tracker_live_maps(azu_tracker* t, int level, const float** d_vertices, const float** d_normals,
                           const float** d_depth_m);
