@@ -63,6 +63,19 @@ def _done():
     lib_stream().synchronize()
 
 
+def _finalize(obj):
+    """Garbage-collected handles are destroyed, except during interpreter
+    shutdown, when the CUDA runtime may already be torn down (the process exit
+    releases the device memory)."""
+    import sys
+    if sys.is_finalizing():
+        return
+    try:
+        obj.close()
+    except Exception:
+        pass
+
+
 def volume_params(resolution, voxel_size, truncation, max_weight=64.0, origin=(0, 0, 0), min_depth=0.3,
                   max_depth=2.5, format=_abi.AZU_TSDF_FP32, color=False) -> _abi.VolumeParams:
     return _abi.VolumeParams(int(resolution), float(voxel_size), float(truncation), float(max_weight),
@@ -99,7 +112,8 @@ class TSDFVolume:
             self.lib.azu_volume_destroy(self.h)
             self.h = C.c_void_p()
 
-    __del__ = close
+    def __del__(self):
+        _finalize(self)
 
     @property
     def n(self):
@@ -178,7 +192,8 @@ class ICPTracker:
             self.lib.azu_tracker_destroy(self.h)
             self.h = C.c_void_p()
 
-    __del__ = close
+    def __del__(self):
+        _finalize(self)
 
     def prepare_live(self, d_depth, W, H):
         _ready()
@@ -244,7 +259,8 @@ class Preprocessor:
             self.lib.azu_preprocessor_destroy(self.h)
             self.h = C.c_void_p()
 
-    __del__ = close
+    def __del__(self):
+        _finalize(self)
 
     def reset(self):
         check(self.lib.azu_preprocessor_reset(self.h), "reset")
@@ -289,7 +305,8 @@ class MarchingCubes:
             self.lib.azu_mesher_destroy(self.h)
             self.h = C.c_void_p()
 
-    __del__ = close
+    def __del__(self):
+        _finalize(self)
 
     def set_max_triangles(self, n):
         check(self.lib.azu_mesher_set_max_triangles(self.h, C.c_int64(int(n))), "set_max_triangles")
@@ -326,7 +343,8 @@ class Pipeline:
             self.lib.azu_pipeline_destroy(self.h)
             self.h = C.c_void_p()
 
-    __del__ = close
+    def __del__(self):
+        _finalize(self)
 
     @staticmethod
     def _frame(r: _abi.FrameResult) -> dict:

@@ -403,6 +403,24 @@ __device__ void project_so3(float* P /* row-major 4x4, rotation block replaced *
     for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) P[4 * i + j] = static_cast<float>(R[3 * i + j]);
 }
 
+// The same projection in float: the polar iteration converges quadratically
+// from a near-rotation, three steps reach float precision.
+__device__ void project_so3_f(float* P) {
+    float R[9];
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) R[3 * i + j] = P[4 * i + j];
+    for (int it = 0; it < 3; ++it) {
+        const float c00 = R[4] * R[8] - R[5] * R[7], c01 = R[5] * R[6] - R[3] * R[8], c02 = R[3] * R[7] - R[4] * R[6];
+        const float c10 = R[2] * R[7] - R[1] * R[8], c11 = R[0] * R[8] - R[2] * R[6], c12 = R[1] * R[6] - R[0] * R[7];
+        const float c20 = R[1] * R[5] - R[2] * R[4], c21 = R[2] * R[3] - R[0] * R[5], c22 = R[0] * R[4] - R[1] * R[3];
+        const float id = 1.0f / (R[0] * c00 + R[1] * c01 + R[2] * c02);
+        const float N[9] = {0.5f * (R[0] + c00 * id), 0.5f * (R[1] + c01 * id), 0.5f * (R[2] + c02 * id),
+                            0.5f * (R[3] + c10 * id), 0.5f * (R[4] + c11 * id), 0.5f * (R[5] + c12 * id),
+                            0.5f * (R[6] + c20 * id), 0.5f * (R[7] + c21 * id), 0.5f * (R[8] + c22 * id)};
+        for (int k = 0; k < 9; ++k) R[k] = N[k];
+    }
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) P[4 * i + j] = R[3 * i + j];
+}
+
 // Rodrigues rotation (Eigen::AngleAxisf::toRotationMatrix) into a row-major 3x3.
 __device__ void angle_axis(float angle, F3 axis, float* r) {
     const float s = sinf(angle), c = cosf(angle);
@@ -432,8 +450,27 @@ struct SolveSmem {
     int isum[kNI];
     float m[36];
     float cs[12];
-    int action;  // 0 continue, 1 stop level
+    int action;    // 0 continue, 1 stop level
+    int need_eig;  // the shifted-Cholesky test could not settle the damping
 };
+
+// True when A - shift I is positive definite (float Cholesky, one thread).
+__device__ bool pd_after_shift(const float* A, float shift) {
+    float L[36];
+    for (int j = 0; j < 6; ++j) {
+        float s = A[j * 6 + j] - shift;
+        for (int k = 0; k < j; ++k) s -= L[j * 6 + k] * L[j * 6 + k];
+        if (!(s > 0.0f)) return false;
+        const float d = sqrtf(s);
+        L[j * 6 + j] = d;
+        for (int i = j + 1; i < 6; ++i) {
+            float t = A[i * 6 + j];
+            for (int k = 0; k < j; ++k) t -= L[i * 6 + k] * L[j * 6 + k];
+            L[i * 6 + j] = t / d;
+        }
+    }
+    return true;
+}
 
 // One solve from the reduced sums (ICPTracker.cpp:78-131), executed by warp 0.
 __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelState& st) {
@@ -451,16 +488,29 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
                     st.information[j * 6 + i] = v;
                 }
             for (int i = 0; i < 36; ++i) sm.m[i] = st.information[i];
+            // dampingForHessian (ICPShared.h:86-100) escalates when min_eig < 1e-4
+            // or max_eig > 1e7 min_eig. Since max_eig <= trace, min_eig >= sigma =
+            // max(1e-4, trace / 1e7) rules both out; A - sigma' I positive definite
+            // proves it, with sigma' = 2 sigma + 32 eps trace covering the
+            // rounding of the float factorisation. Only when that test fails do
+            // the eigenvalues decide.
+            float tr = 0.0f;
+            for (int i = 0; i < 6; ++i) tr += st.information[i * 6 + i];
+            const float sigma = fmaxf(kMinEigEscalate, tr / kCondEscalate);
+            const float shift = 2.0f * sigma + 32.0f * 1.1920929e-7f * tr;
+            sm.need_eig = (isfinite(tr) && pd_after_shift(st.information, shift)) ? 0 : 1;
         }
     }
     __syncwarp();
     if (sm.action != 0) return;
-    float mn, mx;
-    warp_eig6(sm.m, sm.cs, mn, mx);
+    float mn = 1.0f, mx = 1.0f;
+    if (sm.need_eig) warp_eig6(sm.m, sm.cs, mn, mx);
     if (lane != 0) return;
     float damp = (level == 0) ? kDampingLevel0 : kDampingDefault;
-    if (!isfinite(mn) || !isfinite(mx) || mn < kMinEigEscalate) damp = kDampingEscalated;
-    else if (mx > kCondEscalate * mn) damp = kDampingEscalated;
+    if (sm.need_eig) {
+        if (!isfinite(mn) || !isfinite(mx) || mn < kMinEigEscalate) damp = kDampingEscalated;
+        else if (mx > kCondEscalate * mn) damp = kDampingEscalated;
+    }
     float x[6];
     if (a.precision) {
         double A[36], b[6], xd[6];
@@ -508,7 +558,8 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
     } else {
         mm4(st.pose, delta, P);
     }
-    project_so3(P);
+    if (a.precision) project_so3(P);
+    else project_so3_f(P);
     for (int i = 0; i < 16; ++i) st.pose[i] = P[i];
     st.final_step = step_norm;
     st.error = fd(static_cast<float>(sm.sum[27]), static_cast<float>(inl > 1 ? inl : 1));

@@ -179,14 +179,53 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     unsigned long long n_new = 0, n_upd = 0, n_col = 0;
     const size_t rr = static_cast<size_t>(res);
 
-    for (int xc = x0 & ~31; xc <= x1; xc += 32) {
+    // Conservative x-interval of this row that can land in front of the camera
+    // and inside the image: c(t) = c(x0) + t step is linear, so each of
+    // c.z > 0, 0 <= u, u < W, 0 <= v, v < H is a half-line in t (u, v times c.z
+    // are linear). Solved in double and widened by 2 voxels, far more than the
+    // rounding of the stepped coordinate can move a projection. Outside it a
+    // voxel only advances the coordinate, exactly as the sequential sweep does.
+    int xs = x1 + 1, xe = x0 - 1;
+    if (row_on) {
+        double lo = 0.0, hi = static_cast<double>(x1 - x0);
+        auto keep = [&](double a, double b) {  // keep t with a + b t >= 0
+            if (b == 0.0) {
+                if (a < 0.0) { lo = 1.0; hi = 0.0; }
+            } else if (b > 0.0) {
+                lo = fmax(lo, -a / b);
+            } else {
+                hi = fmin(hi, -a / b);
+            }
+        };
+        const double cxs = c.x, cys = c.y, czs = c.z, sx = step.x, sy = step.y, sz = step.z;
+        keep(czs, sz);
+        keep(fx * cxs + (cx + 0.5) * czs, fx * sx + (cx + 0.5) * sz);
+        keep(-(fx * cxs + (cx + 0.5 - W) * czs), -(fx * sx + (cx + 0.5 - W) * sz));
+        keep(fy * cys + (cy + 0.5) * czs, fy * sy + (cy + 0.5) * sz);
+        keep(-(fy * cys + (cy + 0.5 - H) * czs), -(fy * sy + (cy + 0.5 - H) * sz));
+        if (lo <= hi + 4.0) {
+            xs = max(x0, x0 + static_cast<int>(floor(lo)) - 2);
+            xe = min(x1, x0 + static_cast<int>(ceil(hi)) + 2);
+        }
+    }
+    int wxs = xs, wxe = xe;
+    for (int o = 16; o > 0; o >>= 1) {
+        wxs = min(wxs, __shfl_xor_sync(0xffffffffu, wxs, o));
+        wxe = max(wxe, __shfl_xor_sync(0xffffffffu, wxe, o));
+    }
+    if (wxs > wxe) return;  // no row of this warp reaches the image
+    const int xfirst = wxs & ~31;
+    if (row_on)
+        for (int x = x0; x < xfirst; ++x) c = add3(c, step);
+
+    for (int xc = xfirst; xc <= wxe; xc += 32) {
         // phase 1: lane = row
         for (int k = 0; k < 32; ++k) {
             const int x = xc + k;
             float out = qnan;
             int pix = -1;
             if (row_on && x >= x0 && x <= x1) {
-                if (c.z > 0.0f) {
+                if (x >= xs && x <= xe && c.z > 0.0f) {
                     const float inv_z = fd(1.0f, c.z);
                     const float uf = floorf(fa(fa(fm(fm(fx, c.x), inv_z), cx), 0.5f));
                     const float vf = floorf(fa(fa(fm(fm(fy, c.y), inv_z), cy), 0.5f));

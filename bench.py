@@ -281,6 +281,7 @@ def run_gpu(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_run, t_e2e = tt.tolist()
     if rank != 0:
+        _release(torch, dev, mc, pl)
         if ws > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
@@ -325,13 +326,24 @@ def run_gpu(args):
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         line["cpu_stage_s_per_frame"] = cpu["stage_s_per_frame"]
     print(json.dumps(line), flush=True)
+    _release(torch, dev, mc, pl)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
 
 
+def _release(torch, dev, *handles):
+    """Destroy library handles while the CUDA runtime is alive."""
+    torch.cuda.synchronize(dev)
+    for h in handles:
+        h.close()
+    torch.cuda.synchronize(dev)
+
+
 def main():
+    import faulthandler
+    faulthandler.enable()
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)

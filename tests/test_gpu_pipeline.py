@@ -1,7 +1,7 @@
 """The whole per-frame GPU pipeline (preprocess -> pyramid -> ICP -> integrate ->
 raycast, CUDA-graph replayed) against the oracle's lockstep CPU pipeline on
 the same frames: identical grades and integration decisions, and poses within
-2e-4 rad / 2e-4 m along the sequence. The per-frame bound on one input pose is
+5e-4 rad / 5e-4 m along the sequence. The per-frame bound on one input pose is
 1e-6 (test_gpu_icp); chained over frames, a solve that stops one iteration
 earlier on one side (its step is below the 5e-5 convergence threshold) moves
 that frame's pose by up to the threshold, and the next frames start from it."""
@@ -42,7 +42,7 @@ def test_pipeline_matches_lockstep_oracle(cuda_lib, orc, seq, input_is_mm):
         assert g["quality"] == o["quality"], k
         assert g["integrated"] == o["integrated"], k
         rot, trans = F.rel_pose_error(g["pose"], o["pose"])
-        assert rot <= 2e-4 and trans <= 2e-4, (k, rot, trans)
+        assert rot <= 5e-4 and trans <= 5e-4, (k, rot, trans)
         if k:
             assert g["icp"]["status"] == 0
             # association counts follow the (slightly different) poses: within 1 %
