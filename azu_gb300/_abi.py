@@ -89,6 +89,7 @@ SIGNATURES = {
     "azu_volume_download": (C.c_int, [vp, vp, vp, vp]),
     "azu_volume_upload": (C.c_int, [vp, vp, vp, vp]),
     "azu_volume_device_voxels": (vp, [vp]),
+    "azu_volume_set_free_space_skipping": (C.c_int, [vp, C.c_int]),
     # tracker
     "azu_tracker_create": (C.c_int, [C.c_int, C.POINTER(TrackerParams), vp, C.POINTER(vp)]),
     "azu_tracker_destroy": (C.c_int, [vp]),

@@ -85,6 +85,13 @@ struct azu_volume {
     uint8_t* d_rgb_stage = nullptr;
     size_t stage_pixels = 0;
     int integrated_frames = 0;
+    // Free-space bricks of 8^3 voxels (plus a 1-voxel apron): 1 when every voxel
+    // in [8b, 8b+8]^3 is unobserved or has tsdf >= kFreeTsdf. Conservative: set
+    // on reset and rebuilt from the volume after an upload; integration only
+    // clears flags.
+    uint8_t* bricks = nullptr;
+    int nb = 0;
+    bool skip_free = true;
 };
 
 namespace azu {

@@ -24,8 +24,25 @@ namespace azu {
 
 constexpr float kEmptyTsdf = 1.0f;
 constexpr float kEmptyColor = 128.0f / 255.0f;
+// A voxel at or above this tsdf counts as free space for the brick map; the
+// margin over the march's 0.999 covers the rounding of trilinear interpolation.
+constexpr float kFreeTsdf = 0.9995f;
+constexpr int kBrickShift = 3;  // 8^3-voxel bricks
 
 size_t voxel_bytes(int format) { return format == AZU_TSDF_FP16 ? 4 : 8; }
+
+// Clears the free flag of every brick whose apron [8b, 8b+8] holds voxel (x, y, z).
+__device__ __forceinline__ void clear_bricks(uint8_t* bricks, int nb, int x, int y, int z) {
+    const int bx = x >> kBrickShift, by = y >> kBrickShift, bz = z >> kBrickShift;
+    const int ex = ((x & 7) == 0 && x > 0) ? 1 : 0, ey = ((y & 7) == 0 && y > 0) ? 1 : 0,
+              ez = ((z & 7) == 0 && z > 0) ? 1 : 0;
+    for (int dz = 0; dz <= ez; ++dz)
+        for (int dy = 0; dy <= ey; ++dy)
+            for (int dx = 0; dx <= ex; ++dx) {
+                const size_t b = (static_cast<size_t>(bz - dz) * nb + (by - dy)) * nb + (bx - dx);
+                if (bricks[b]) bricks[b] = 0;
+            }
+}
 
 // ---- voxel record access -----------------------------------------------
 template <bool kHalf>
@@ -42,6 +59,7 @@ struct Vox<false> {
     __device__ static __forceinline__ void store(void* v, size_t i, float t, float w) {
         static_cast<float2*>(v)[i] = make_float2(t, w);
     }
+    __device__ static __forceinline__ float rounded(float t) { return t; }
 };
 template <>
 struct Vox<true> {
@@ -60,6 +78,7 @@ struct Vox<true> {
         const uint32_t h = __half_as_ushort(__float2half_rn(t));
         static_cast<uint32_t*>(v)[i] = h | (static_cast<uint32_t>(w) << 16);
     }
+    __device__ static __forceinline__ float rounded(float t) { return __half2float(__float2half_rn(t)); }
 };
 
 // ---- small kernels -------------------------------------------------------
@@ -143,16 +162,16 @@ __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res
 //            parked distance with one coalesced read-modify-write.
 // Voxels that take no update are never read, so HBM traffic is 2 x record size
 // per updated voxel.
-constexpr int kIntWarps = 8;
+constexpr int kIntWarps = 4;
 
 template <bool kHalf, bool kColor>
 __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     void* __restrict__ vox, float* __restrict__ color, const IntegrateConsts* __restrict__ icp,
     const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
     float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
-    float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters) {
-    __shared__ float s_sdf[kIntWarps][32][33];
-    __shared__ int s_pix[kColor ? kIntWarps : 1][32][33];
+    float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb) {
+    __shared__ float s_cz[kIntWarps][32][33];
+    __shared__ int s_pix[kIntWarps][32][33];
     if (gate && __ldg(gate) == 0) return;
     if (!__ldg(&icp->valid)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -219,11 +238,13 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
         for (int x = x0; x < xfirst; ++x) c = add3(c, step);
 
     for (int xc = xfirst; xc <= wxe; xc += 32) {
-        // phase 1: lane = row
+        // phase 1 (lane = row): the sequential camera coordinate and the
+        // projection only; the pixel and the camera z are parked for phase 2.
+#pragma unroll 4
         for (int k = 0; k < 32; ++k) {
             const int x = xc + k;
-            float out = qnan;
             int pix = -1;
+            float czk = 0.0f;
             if (row_on && x >= x0 && x <= x1) {
                 if (x >= xs && x <= xe && c.z > 0.0f) {
                     const float inv_z = fd(1.0f, c.z);
@@ -231,43 +252,65 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
                     const float vf = floorf(fa(fa(fm(fm(fy, c.y), inv_z), cy), 0.5f));
                     if (uf >= 0.0f && uf < fW && vf >= 0.0f && vf < fH) {
                         pix = static_cast<int>(vf) * W + static_cast<int>(uf);
-                        const float d = __ldg(depth + pix);
-                        if (d >= min_d && d <= max_d) {
-                            const float sdf = fs(d, c.z);
-                            if (!(sdf < -trunc)) out = sdf;
-                        }
+                        czk = c.z;
                     }
                 }
                 c = add3(c, step);
             }
-            s_sdf[warp][lane][k] = out;
-            if (kColor) s_pix[warp][lane][k] = pix;
+            s_pix[warp][lane][k] = pix;
+            s_cz[warp][lane][k] = czk;
         }
         __syncwarp();
-        // phase 2: lane = x
+        // phase 2 (lane = x): adjacent lanes are adjacent voxels of one row and
+        // project to adjacent pixels, so the depth gathers coalesce; rows go in
+        // batches of 8 so their loads are in flight together.
         const int x = xc + lane;
-        for (int r = 0; r < 32; ++r) {
-            const float sdf = s_sdf[warp][r][lane];
-            if (sdf != sdf) continue;  // NaN: no update
-            const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + r)) * rr + x;
-            const float tsdf_new = fminf(1.0f, fd(sdf, trunc));
-            const float2 old = Vox<kHalf>::load_rw(vox, vi);
-            const float w_old = old.y;
-            n_new += (w_old == 0.0f);
-            ++n_upd;
-            const float wp1 = fa(w_old, 1.0f);
-            const float t = fd(fa(fm(old.x, w_old), tsdf_new), wp1);
-            const float w = fminf(wp1, max_w);
-            Vox<kHalf>::store(vox, vi, t, w);
-            if (kColor) {
-                if (rgb != nullptr && fabsf(sdf) < color_band) {
-                    const int pix = s_pix[warp][r][lane];
-                    const float inv = fd(1.0f, wp1);
-                    float* cv = color + 3 * vi;
+        for (int r0 = 0; r0 < 32; r0 += 8) {
+            float sdf[8];
+            int pixr[8];
 #pragma unroll
-                    for (int k = 0; k < 3; ++k)
-                        cv[k] = fm(fa(fm(cv[k], w_old), fd(static_cast<float>(rgb[3 * pix + k]), 255.0f)), inv);
-                    ++n_col;
+            for (int j = 0; j < 8; ++j) {
+                pixr[j] = s_pix[warp][r0 + j][lane];
+                sdf[j] = (pixr[j] >= 0) ? __ldg(depth + pixr[j]) : qnan;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float d = sdf[j];
+                sdf[j] = qnan;
+                if (d >= min_d && d <= max_d) {
+                    const float s = fs(d, s_cz[warp][r0 + j][lane]);
+                    if (!(s < -trunc)) sdf[j] = s;
+                }
+            }
+            float2 old[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + r0 + j)) * rr + x;
+                if (sdf[j] == sdf[j]) old[j] = Vox<kHalf>::load_rw(vox, vi);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (sdf[j] != sdf[j]) continue;  // NaN: no update
+                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + r0 + j)) * rr + x;
+                const float tsdf_new = fminf(1.0f, fd(sdf[j], trunc));
+                const float w_old = old[j].y;
+                n_new += (w_old == 0.0f);
+                ++n_upd;
+                const float wp1 = fa(w_old, 1.0f);
+                const float t = fd(fa(fm(old[j].x, w_old), tsdf_new), wp1);
+                const float w = fminf(wp1, max_w);
+                Vox<kHalf>::store(vox, vi, t, w);
+                if (bricks && !(Vox<kHalf>::rounded(t) >= kFreeTsdf)) clear_bricks(bricks, nb, x, ybase + r0 + j, z);
+                if (kColor) {
+                    if (rgb != nullptr && fabsf(sdf[j]) < color_band) {
+                        const int pix = pixr[j];
+                        const float inv = fd(1.0f, wp1);
+                        float* cv = color + 3 * vi;
+#pragma unroll
+                        for (int k = 0; k < 3; ++k)
+                            cv[k] = fm(fa(fm(cv[k], w_old), fd(static_cast<float>(rgb[3 * pix + k]), 255.0f)), inv);
+                        ++n_col;
+                    }
                 }
             }
         }
@@ -328,6 +371,36 @@ __device__ __forceinline__ bool sample_tsdf(const VolView& v, F3 p, float& f) {
     return true;
 }
 
+// True when the sample at p lies in a free brick, or outside the samplable box
+// (then it is invalid). Same base-voxel arithmetic as sample_tsdf, so the 8
+// corners of the sample are inside the brick's apron.
+__device__ __forceinline__ bool in_free_brick(const VolView& v, const uint8_t* __restrict__ bricks, int nb, F3 p) {
+    const F3 q = div3(sub3(p, v.origin), v.vs);
+    const float fx0 = floorf(q.x), fy0 = floorf(q.y), fz0 = floorf(q.z);
+    const float lim = static_cast<float>(v.res - 1);
+    if (!(fx0 >= 0.0f && fy0 >= 0.0f && fz0 >= 0.0f && fx0 < lim && fy0 < lim && fz0 < lim)) return true;
+    const int bx = static_cast<int>(fx0) >> kBrickShift, by = static_cast<int>(fy0) >> kBrickShift,
+              bz = static_cast<int>(fz0) >> kBrickShift;
+    return __ldg(bricks + (static_cast<size_t>(bz) * nb + by) * nb + bx) != 0;
+}
+
+// Exact free flags from the volume (after an upload).
+template <bool kHalf>
+__global__ void rebuild_bricks_kernel(const void* vox, int res, uint8_t* bricks, int nb) {
+    const size_t nbr = static_cast<size_t>(nb) * nb * nb;
+    const size_t b = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= nbr) return;
+    const int bx = static_cast<int>(b % nb), by = static_cast<int>((b / nb) % nb), bz = static_cast<int>(b / nb / nb);
+    bool free = true;
+    for (int z = bz * 8; free && z <= min(bz * 8 + 8, res - 1); ++z)
+        for (int y = by * 8; free && y <= min(by * 8 + 8, res - 1); ++y)
+            for (int x = bx * 8; free && x <= min(bx * 8 + 8, res - 1); ++x) {
+                const float2 r = Vox<kHalf>::load_rw(vox, (static_cast<size_t>(z) * res + y) * res + x);
+                if ((r.y > 0.0f) && !(r.x >= kFreeTsdf)) free = false;
+            }
+    bricks[b] = free ? 1 : 0;
+}
+
 // computeNormal (TSDFVolume.cpp:478-490).
 template <bool kHalf>
 __device__ __forceinline__ bool compute_normal(const VolView& v, F3 p, F3& n_out) {
@@ -354,7 +427,8 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
                                                      float fy, float cx, float cy, int W, int H, float trunc,
                                                      float min_depth, float max_depth, float* __restrict__ vout,
                                                      float* __restrict__ nout, uint8_t* __restrict__ cout,
-                                                     const int* __restrict__ gate) {
+                                                     const int* __restrict__ gate, const uint8_t* __restrict__ bricks,
+                                                     int nb) {
     if (gate && __ldg(gate) == 0) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -404,9 +478,14 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
         if (prev_valid && f_prev < 0.0f) break;
         bool found = false;
         float t_hit = 0.0f;
+        // A sample in a free brick is invalid or has f >= 0.999: its step is the
+        // far step and, unless the previous sample was negative, no test can fire.
+        // Such samples are not evaluated; the march keeps the same t sequence, and
+        // the last skipped sample is evaluated when the state is needed again.
+        bool skipped = false;
         while (t_prev < t_far) {
             float step;
-            if (!prev_valid || f_prev >= 0.999f) {
+            if (skipped || !prev_valid || f_prev >= 0.999f) {
                 step = far_step;
             } else {
                 const float s = fm(fm(0.8f, f_prev), trunc);
@@ -415,8 +494,20 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
             const float tn = fa(t_prev, step);
             const float t = (t_far < tn) ? t_far : tn;  // std::min(t_prev + step, t_far)
             if (!(t > t_prev)) break;  // no progress (degenerate parameters): stop without a hit
+            const F3 p = add3(co, mul3(dir, t));
+            if (bricks && (skipped || !prev_valid || f_prev >= 0.0f) && in_free_brick(v, bricks, nb, p)) {
+                t_prev = t;
+                skipped = true;
+                if (t >= t_far) break;
+                continue;
+            }
+            if (skipped) {
+                f_prev = 1.0f;
+                prev_valid = sample_tsdf<kHalf>(v, add3(co, mul3(dir, t_prev)), f_prev);
+                skipped = false;
+            }
             float f = 1.0f;
-            const bool valid = sample_tsdf<kHalf>(v, add3(co, mul3(dir, t)), f);
+            const bool valid = sample_tsdf<kHalf>(v, p, f);
             if (valid && !isfinite(f)) break;
             if (valid && prev_valid) {
                 if (f_prev > 0.0f && f <= 0.0f) {
@@ -502,7 +593,8 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
     const bool col = v->color != nullptr;
 #define AZU_INT_ARGS                                                                                             \
     v->vox, v->color, v->d_iconsts, d_depth_m, d_rgb, p.resolution, p.voxel_size, p.origin[0], p.origin[1],     \
-        p.origin[2], p.truncation, p.max_weight, fx, fy, cx, cy, W, H, min_d, max_d, d_gate, v->d_counters
+        p.origin[2], p.truncation, p.max_weight, fx, fy, cx, cy, W, H, min_d, max_d, d_gate, v->d_counters,   \
+        v->bricks, v->nb
     if (!half && !col) integrate_kernel<false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (!half && col) integrate_kernel<false, true><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (half && !col) integrate_kernel<true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
@@ -517,12 +609,15 @@ int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, f
     const azu_volume_params& p = v->p;
     VolView view{v->vox, v->color, p.resolution, p.voxel_size, mk3(p.origin[0], p.origin[1], p.origin[2])};
     const dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
+    const uint8_t* bricks = v->skip_free ? v->bricks : nullptr;
     if (p.format == AZU_TSDF_FP16)
         raycast_kernel<true><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
-                                                  p.max_depth, d_vertices, d_normals, d_colors, d_gate);
+                                                  p.max_depth, d_vertices, d_normals, d_colors, d_gate, bricks,
+                                                  v->nb);
     else
         raycast_kernel<false><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
-                                                   p.max_depth, d_vertices, d_normals, d_colors, d_gate);
+                                                   p.max_depth, d_vertices, d_normals, d_colors, d_gate, bricks,
+                                                   v->nb);
     AZU_LAUNCH_CHECK();
     return AZU_OK;
 }
@@ -531,13 +626,25 @@ static int volume_alloc(azu_volume* v) {
     const size_t n = static_cast<size_t>(v->p.resolution) * v->p.resolution * v->p.resolution;
     AZU_TRY_CUDA(cudaMalloc(&v->vox, n * voxel_bytes(v->p.format)));
     if (v->p.color) AZU_TRY_CUDA(cudaMalloc(&v->color, n * 3 * sizeof(float)));
+    v->nb = (v->p.resolution + 7) >> kBrickShift;
+    AZU_TRY_CUDA(cudaMalloc(&v->bricks, static_cast<size_t>(v->nb) * v->nb * v->nb));
     return AZU_OK;
 }
 static void volume_free_storage(azu_volume* v) {
     if (v->vox) cudaFree(v->vox);
     if (v->color) cudaFree(v->color);
+    if (v->bricks) cudaFree(v->bricks);
     v->vox = nullptr;
     v->color = nullptr;
+    v->bricks = nullptr;
+}
+int rebuild_bricks(azu_volume* v, cudaStream_t s) {
+    const size_t nbr = static_cast<size_t>(v->nb) * v->nb * v->nb;
+    const unsigned g = static_cast<unsigned>((nbr + 127) / 128);
+    if (v->p.format == AZU_TSDF_FP16) rebuild_bricks_kernel<true><<<g, 128, 0, s>>>(v->vox, v->p.resolution, v->bricks, v->nb);
+    else rebuild_bricks_kernel<false><<<g, 128, 0, s>>>(v->vox, v->p.resolution, v->bricks, v->nb);
+    AZU_LAUNCH_CHECK();
+    return AZU_OK;
 }
 static int check_params(const azu_volume_params* p) {
     AZU_CHECK_ARG(p != nullptr, "params is null");
@@ -562,6 +669,7 @@ extern "C" int azu_volume_reset(azu_volume* v) {
     else reset_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
     AZU_LAUNCH_CHECK();
     AZU_TRY_CUDA(cudaMemsetAsync(v->d_counters, 0, 4 * sizeof(unsigned long long), v->stream.s));
+    AZU_TRY_CUDA(cudaMemsetAsync(v->bricks, 1, static_cast<size_t>(v->nb) * v->nb * v->nb, v->stream.s));
     v->integrated_frames = 0;
     return AZU_OK;
 }
@@ -741,7 +849,16 @@ extern "C" int azu_volume_download(azu_volume* v, float* h_tsdf, float* h_weight
 
 extern "C" int azu_volume_upload(azu_volume* v, const float* h_tsdf, const float* h_weight, const float* h_color) {
     AZU_CHECK_ARG(v != nullptr && h_tsdf != nullptr && h_weight != nullptr, "null argument");
-    return transfer(v, nullptr, nullptr, nullptr, h_tsdf, h_weight, h_color, false);
+    if (int rc = transfer(v, nullptr, nullptr, nullptr, h_tsdf, h_weight, h_color, false)) return rc;
+    if (int rc = rebuild_bricks(v, v->stream.s)) return rc;
+    AZU_TRY_CUDA(cudaStreamSynchronize(v->stream.s));
+    return AZU_OK;
+}
+
+extern "C" int azu_volume_set_free_space_skipping(azu_volume* v, int on) {
+    AZU_CHECK_ARG(v != nullptr, "volume is null");
+    v->skip_free = on != 0;
+    return AZU_OK;
 }
 
 extern "C" void* azu_volume_device_voxels(azu_volume* v) { return v ? v->vox : nullptr; }

@@ -118,6 +118,10 @@ int azu_volume_get_stats(azu_volume* v, azu_volume_stats* s);
  * FP16 volumes convert on the device. Synchronous. */
 int azu_volume_download(azu_volume* v, float* h_tsdf, float* h_weight, float* h_color);
 int azu_volume_upload(azu_volume* v, const float* h_tsdf, const float* h_weight, const float* h_color);
+/* Free-space skipping in the raycast (on by default): samples whose 8 corners
+ * are all unobserved or at tsdf >= 0.9995 are not loaded, only stepped over;
+ * results are identical either way. For A/B timing. */
+int azu_volume_set_free_space_skipping(azu_volume* v, int on);
 /* TSDFVolume::getGPUVoxels (TSDFVolume.h:163): device voxel array (float2
  * {tsdf, weight} for FP32, uint32 {half, u16} for FP16). */
 void* azu_volume_device_voxels(azu_volume* v);
