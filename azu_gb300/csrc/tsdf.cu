@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     for (int xc = xfirst; xc <= wxe; xc += 32) {
         // phase 1 (lane = row): the sequential camera coordinate and the
         // projection only; the pixel and the camera z are parked for phase 2.
+        bool any_pix = false;
 #pragma unroll 4
         for (int k = 0; k < 32; ++k) {
             const int x = xc + k;
@@ -247,12 +248,13 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
             float czk = 0.0f;
             if (row_on && x >= x0 && x <= x1) {
                 if (x >= xs && x <= xe && c.z > 0.0f) {
-                    const float inv_z = fd(1.0f, c.z);
+                    const float inv_z = __frcp_rn(c.z);  // == 1.0f / c.z, correctly rounded
                     const float uf = floorf(fa(fa(fm(fm(fx, c.x), inv_z), cx), 0.5f));
                     const float vf = floorf(fa(fa(fm(fm(fy, c.y), inv_z), cy), 0.5f));
                     if (uf >= 0.0f && uf < fW && vf >= 0.0f && vf < fH) {
                         pix = static_cast<int>(vf) * W + static_cast<int>(uf);
                         czk = c.z;
+                        any_pix = true;
                     }
                 }
                 c = add3(c, step);
@@ -260,17 +262,29 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
             s_pix[warp][lane][k] = pix;
             s_cz[warp][lane][k] = czk;
         }
+        // rows of this chunk with at least one voxel inside the image
+        unsigned rows = __ballot_sync(0xffffffffu, any_pix);
         __syncwarp();
         // phase 2 (lane = x): adjacent lanes are adjacent voxels of one row and
         // project to adjacent pixels, so the depth gathers coalesce; rows go in
         // batches of 8 so their loads are in flight together.
         const int x = xc + lane;
-        for (int r0 = 0; r0 < 32; r0 += 8) {
+        while (rows) {
+            int rsel[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (rows) {
+                    rsel[j] = __ffs(rows) - 1;
+                    rows &= rows - 1;
+                } else {
+                    rsel[j] = -1;
+                }
+            }
             float sdf[8];
             int pixr[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                pixr[j] = s_pix[warp][r0 + j][lane];
+                pixr[j] = rsel[j] >= 0 ? s_pix[warp][rsel[j]][lane] : -1;
                 sdf[j] = (pixr[j] >= 0) ? __ldg(depth + pixr[j]) : qnan;
             }
 #pragma unroll
@@ -278,20 +292,20 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
                 const float d = sdf[j];
                 sdf[j] = qnan;
                 if (d >= min_d && d <= max_d) {
-                    const float s = fs(d, s_cz[warp][r0 + j][lane]);
+                    const float s = fs(d, s_cz[warp][rsel[j]][lane]);
                     if (!(s < -trunc)) sdf[j] = s;
                 }
             }
             float2 old[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + r0 + j)) * rr + x;
+                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
                 if (sdf[j] == sdf[j]) old[j] = Vox<kHalf>::load_rw(vox, vi);
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 if (sdf[j] != sdf[j]) continue;  // NaN: no update
-                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + r0 + j)) * rr + x;
+                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
                 const float tsdf_new = fminf(1.0f, fd(sdf[j], trunc));
                 const float w_old = old[j].y;
                 n_new += (w_old == 0.0f);
@@ -300,7 +314,7 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
                 const float t = fd(fa(fm(old[j].x, w_old), tsdf_new), wp1);
                 const float w = fminf(wp1, max_w);
                 Vox<kHalf>::store(vox, vi, t, w);
-                if (bricks && !(Vox<kHalf>::rounded(t) >= kFreeTsdf)) clear_bricks(bricks, nb, x, ybase + r0 + j, z);
+                if (bricks && !(Vox<kHalf>::rounded(t) >= kFreeTsdf)) clear_bricks(bricks, nb, x, ybase + rsel[j], z);
                 if (kColor) {
                     if (rgb != nullptr && fabsf(sdf[j]) < color_band) {
                         const int pix = pixr[j];
@@ -374,14 +388,34 @@ __device__ __forceinline__ bool sample_tsdf(const VolView& v, F3 p, float& f) {
 // True when the sample at p lies in a free brick, or outside the samplable box
 // (then it is invalid). Same base-voxel arithmetic as sample_tsdf, so the 8
 // corners of the sample are inside the brick's apron.
-__device__ __forceinline__ bool in_free_brick(const VolView& v, const uint8_t* __restrict__ bricks, int nb, F3 p) {
+// Returns 0 (not free), 1 (inside free brick (bx, by, bz)) or 2 (outside the box).
+__device__ __forceinline__ int in_free_brick(const VolView& v, const uint8_t* __restrict__ bricks, int nb, F3 p,
+                                             int& bx, int& by, int& bz) {
     const F3 q = div3(sub3(p, v.origin), v.vs);
     const float fx0 = floorf(q.x), fy0 = floorf(q.y), fz0 = floorf(q.z);
     const float lim = static_cast<float>(v.res - 1);
-    if (!(fx0 >= 0.0f && fy0 >= 0.0f && fz0 >= 0.0f && fx0 < lim && fy0 < lim && fz0 < lim)) return true;
-    const int bx = static_cast<int>(fx0) >> kBrickShift, by = static_cast<int>(fy0) >> kBrickShift,
-              bz = static_cast<int>(fz0) >> kBrickShift;
-    return __ldg(bricks + (static_cast<size_t>(bz) * nb + by) * nb + bx) != 0;
+    if (!(fx0 >= 0.0f && fy0 >= 0.0f && fz0 >= 0.0f && fx0 < lim && fy0 < lim && fz0 < lim)) return 2;
+    bx = static_cast<int>(fx0) >> kBrickShift;
+    by = static_cast<int>(fy0) >> kBrickShift;
+    bz = static_cast<int>(fz0) >> kBrickShift;
+    return __ldg(bricks + (static_cast<size_t>(bz) * nb + by) * nb + bx) != 0 ? 1 : 0;
+}
+
+// Ray parameter below which every sample position stays inside brick b: the
+// exit of its world box [o + 8 b vs, o + (8 b + 8) vs) shrunk by 1e-3 voxel,
+// a margin far above the rounding of the position and of this bound.
+__device__ __forceinline__ float brick_exit(const VolView& v, F3 co, F3 dir, int bx, int by, int bz) {
+    const float span = 8.0f * v.vs, d = 1e-3f * v.vs;
+    const int b[3] = {bx, by, bz};
+    float te = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float da = comp(dir, a);
+        const float lo = comp(v.origin, a) + span * static_cast<float>(b[a]);
+        if (da > 0.0f) te = fminf(te, (lo + span - d - comp(co, a)) / da);
+        else if (da < 0.0f) te = fminf(te, (lo + d - comp(co, a)) / da);
+    }
+    return te;
 }
 
 // Exact free flags from the volume (after an upload).
@@ -495,10 +529,26 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
             const float t = (t_far < tn) ? t_far : tn;  // std::min(t_prev + step, t_far)
             if (!(t > t_prev)) break;  // no progress (degenerate parameters): stop without a hit
             const F3 p = add3(co, mul3(dir, t));
-            if (bricks && (skipped || !prev_valid || f_prev >= 0.0f) && in_free_brick(v, bricks, nb, p)) {
+            int bx = 0, by = 0, bz = 0;
+            const int fb = (bricks && (skipped || !prev_valid || f_prev >= 0.0f)) ? in_free_brick(v, bricks, nb, p, bx, by, bz) : 0;
+            if (fb) {
                 t_prev = t;
                 skipped = true;
                 if (t >= t_far) break;
+                if (fb == 1) {
+                    // The following far steps inside this brick are skipped too:
+                    // advance t by the same float additions without positions.
+                    const float t_exit = brick_exit(v, co, dir, bx, by, bz);
+                    bool done = false;
+                    while (true) {
+                        const float tn2 = fa(t_prev, far_step);
+                        const float t2 = (t_far < tn2) ? t_far : tn2;
+                        if (!(t2 > t_prev) || !(t2 < t_exit)) break;
+                        t_prev = t2;
+                        if (t2 >= t_far) { done = true; break; }
+                    }
+                    if (done) break;
+                }
                 continue;
             }
             if (skipped) {
