@@ -13,6 +13,7 @@ kernels are ordered on one stream. Poses are (4, 4) row-major float32.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 
 import numpy as np
 
@@ -67,7 +68,6 @@ def _finalize(obj):
     """Garbage-collected handles are destroyed, except during interpreter
     shutdown, when the CUDA runtime may already be torn down (the process exit
     releases the device memory)."""
-    import sys
     if sys.is_finalizing():
         return
     try:

@@ -262,24 +262,18 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
             s_pix[warp][lane][k] = pix;
             s_cz[warp][lane][k] = czk;
         }
-        // rows of this chunk with at least one voxel inside the image
-        unsigned rows = __ballot_sync(0xffffffffu, any_pix);
+        // no row of this chunk reaches the image: nothing to update
+        if (!__any_sync(0xffffffffu, any_pix)) continue;
         __syncwarp();
         // phase 2 (lane = x): adjacent lanes are adjacent voxels of one row and
         // project to adjacent pixels, so the depth gathers coalesce; rows go in
         // batches of 8 so their loads are in flight together.
         const int x = xc + lane;
-        while (rows) {
+#pragma unroll 1
+        for (int r0 = 0; r0 < 32; r0 += 8) {
             int rsel[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                if (rows) {
-                    rsel[j] = __ffs(rows) - 1;
-                    rows &= rows - 1;
-                } else {
-                    rsel[j] = -1;
-                }
-            }
+            for (int j = 0; j < 8; ++j) rsel[j] = r0 + j;
             float sdf[8];
             int pixr[8];
 #pragma unroll
@@ -353,13 +347,22 @@ struct VolView {
     int res;
     float vs;
     F3 origin;
+    float inv_vs;  // 1 / vs when vs is a power of two (then exact), else 0
 };
+
+// (p - origin) / vs. When vs is a power of two the quotient equals the product
+// with its exact reciprocal bit for bit, and the multiplication is far cheaper.
+__device__ __forceinline__ F3 to_voxel(const VolView& v, F3 p) {
+    const F3 d = sub3(p, v.origin);
+    if (v.inv_vs != 0.0f) return mul3(d, v.inv_vs);
+    return div3(d, v.vs);
+}
 
 // sampleTSDF (TSDFVolume.cpp:492-525): trilinear, valid only if all 8 corners
 // are observed.
 template <bool kHalf>
 __device__ __forceinline__ bool sample_tsdf(const VolView& v, F3 p, float& f) {
-    const F3 q = div3(sub3(p, v.origin), v.vs);
+    const F3 q = to_voxel(v, p);
     const float fx0 = floorf(q.x), fy0 = floorf(q.y), fz0 = floorf(q.z);
     const float lim = static_cast<float>(v.res - 1);
     if (!(fx0 >= 0.0f && fy0 >= 0.0f && fz0 >= 0.0f && fx0 < lim && fy0 < lim && fz0 < lim)) return false;
@@ -391,7 +394,7 @@ __device__ __forceinline__ bool sample_tsdf(const VolView& v, F3 p, float& f) {
 // Returns 0 (not free), 1 (inside free brick (bx, by, bz)) or 2 (outside the box).
 __device__ __forceinline__ int in_free_brick(const VolView& v, const uint8_t* __restrict__ bricks, int nb, F3 p,
                                              int& bx, int& by, int& bz) {
-    const F3 q = div3(sub3(p, v.origin), v.vs);
+    const F3 q = to_voxel(v, p);
     const float fx0 = floorf(q.x), fy0 = floorf(q.y), fz0 = floorf(q.z);
     const float lim = static_cast<float>(v.res - 1);
     if (!(fx0 >= 0.0f && fy0 >= 0.0f && fz0 >= 0.0f && fx0 < lim && fy0 < lim && fz0 < lim)) return 2;
@@ -399,23 +402,6 @@ __device__ __forceinline__ int in_free_brick(const VolView& v, const uint8_t* __
     by = static_cast<int>(fy0) >> kBrickShift;
     bz = static_cast<int>(fz0) >> kBrickShift;
     return __ldg(bricks + (static_cast<size_t>(bz) * nb + by) * nb + bx) != 0 ? 1 : 0;
-}
-
-// Ray parameter below which every sample position stays inside brick b: the
-// exit of its world box [o + 8 b vs, o + (8 b + 8) vs) shrunk by 1e-3 voxel,
-// a margin far above the rounding of the position and of this bound.
-__device__ __forceinline__ float brick_exit(const VolView& v, F3 co, F3 dir, int bx, int by, int bz) {
-    const float span = 8.0f * v.vs, d = 1e-3f * v.vs;
-    const int b[3] = {bx, by, bz};
-    float te = __int_as_float(0x7f800000);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float da = comp(dir, a);
-        const float lo = comp(v.origin, a) + span * static_cast<float>(b[a]);
-        if (da > 0.0f) te = fminf(te, (lo + span - d - comp(co, a)) / da);
-        else if (da < 0.0f) te = fminf(te, (lo + d - comp(co, a)) / da);
-    }
-    return te;
 }
 
 // Exact free flags from the volume (after an upload).
@@ -535,20 +521,6 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
                 t_prev = t;
                 skipped = true;
                 if (t >= t_far) break;
-                if (fb == 1) {
-                    // The following far steps inside this brick are skipped too:
-                    // advance t by the same float additions without positions.
-                    const float t_exit = brick_exit(v, co, dir, bx, by, bz);
-                    bool done = false;
-                    while (true) {
-                        const float tn2 = fa(t_prev, far_step);
-                        const float t2 = (t_far < tn2) ? t_far : tn2;
-                        if (!(t2 > t_prev) || !(t2 < t_exit)) break;
-                        t_prev = t2;
-                        if (t2 >= t_far) { done = true; break; }
-                    }
-                    if (done) break;
-                }
                 continue;
             }
             if (skipped) {
@@ -580,7 +552,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
         if (!compute_normal<kHalf>(v, hit, nrm)) break;
         if (!finite3(hit)) break;
         if (cout) {
-            const F3 q = div3(sub3(hit, v.origin), vs);
+            const F3 q = to_voxel(v, hit);
             int vx, vy, vz;
             if (floor_to_int(q.x, &vx) && floor_to_int(q.y, &vy) && floor_to_int(q.z, &vz) && vx >= 0 &&
                 vx < v.res && vy >= 0 && vy < v.res && vz >= 0 && vz < v.res) {
@@ -657,7 +629,11 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
 int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, float cx, float cy, int W, int H,
                        float* d_vertices, float* d_normals, uint8_t* d_colors, const int* d_gate, cudaStream_t s) {
     const azu_volume_params& p = v->p;
-    VolView view{v->vox, v->color, p.resolution, p.voxel_size, mk3(p.origin[0], p.origin[1], p.origin[2])};
+    int e2 = 0;
+    const float mant = std::frexp(p.voxel_size, &e2);
+    // 2^(e2-1) with an exact, normal reciprocal 2^(1-e2)
+    const float inv_vs = (mant == 0.5f && e2 > -120 && e2 < 120) ? std::ldexp(1.0f, 1 - e2) : 0.0f;
+    VolView view{v->vox, v->color, p.resolution, p.voxel_size, mk3(p.origin[0], p.origin[1], p.origin[2]), inv_vs};
     const dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
     const uint8_t* bricks = v->skip_free ? v->bricks : nullptr;
     if (p.format == AZU_TSDF_FP16)
