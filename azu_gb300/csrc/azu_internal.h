@@ -63,6 +63,19 @@ struct IntegrateConsts {
     float step_x[3];
     int x0, x1, y0, y1, z0, z1;
     int valid;
+    // chunk culling: a stepped coordinate lies within cull_eps of its chunk's
+    // line; cull_off = trunc + cull_eps + slack; voxels nearer than z_safe are
+    // never culled
+    float cull_eps, cull_off, z_safe;
+};
+
+// Tile-max pyramid over the depth image: level l tiles are 8 * 2^l pixels
+// square, stored level after level from offset off[l].
+constexpr int kMaxTileLevels = 12;
+constexpr int kMaxTilePixels = 8 << (kMaxTileLevels - 1);
+struct TileMip {
+    int levels, total;
+    int w[kMaxTileLevels], h[kMaxTileLevels], off[kMaxTileLevels];
 };
 
 struct RaycastConsts {
@@ -92,6 +105,9 @@ struct azu_volume {
     uint8_t* bricks = nullptr;
     int nb = 0;
     bool skip_free = true;
+    // Deepest in-band depth per 8x8 pixel tile of the frame being integrated.
+    float* d_tiles = nullptr;
+    size_t tile_cap = 0;
 };
 
 namespace azu {

@@ -6,12 +6,12 @@
 //   1. each block accumulates the 21 + 6 normal-equation terms, the Huber loss
 //      and 6 counters over a slice of the level's interior pixels (projective
 //      association into the model image, one thread per pixel);
-//   2. warp shuffles, then shared memory, reduce them to one block partial,
-//      written to global memory;
-//   3. one grid barrier (bounded spin; a timeout sets an error word);
-//   4. every block reduces all block partials itself, in the same fixed order,
-//      and solves the damped 6x6 system itself — identical inputs and code give
-//      identical results in every block, so no second barrier is needed.
+//   2. warp shuffles (recursive halving), then shared memory, reduce them to
+//      one block partial, written to global memory value-major;
+//   3. the block that arrives last at the split barrier reduces all block
+//      partials in one fixed order, solves the damped 6x6 system and publishes
+//      the outcome; the others wait (bounded spin; a timeout sets an error
+//      word) and read it.
 // Partials are double-buffered by iteration parity.
 #include <cuda_fp16.h>
 
@@ -63,10 +63,11 @@ struct IcpArgs {
     azu_icp_result* d_result;
     int* d_quality;
     int* d_gate;          // set to 1 when the frame grades Good
-    double* partials;     // [2][nblocks][kNF]
-    int* ipartials;       // [2][nblocks][kNI]
+    double* partials;     // [2][kNF][nblocks], double or float (precision form or not)
+    int* ipartials;       // [2][kNI][nblocks]
     unsigned* bar;        // [0] arrivals, [1] generation
     unsigned* err;
+    unsigned* state;      // iteration outcome published by the last-arriving block
     float* build_out;     // build mode: A[36], b[6], residual, counts[6] (as int bits)
 };
 
@@ -107,6 +108,55 @@ __device__ void grid_sync(unsigned* bar, unsigned* err, unsigned nblocks, unsign
     __syncthreads();
 }
 
+// Split barrier: every block arrives; the one that arrives last reduces and
+// solves, publishes the outcome and releases the others (one reduction and
+// one solve per iteration instead of one per block). Waits are bounded like
+// grid_sync; with the error word set nobody waits and every block proceeds
+// on its own (the result is then reported as a timeout).
+__device__ bool arrive_last(unsigned* bar, unsigned* err, unsigned nblocks, int* s_flag) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int last = 1;
+        if (ld_acquire(err) == 0) {
+            __threadfence();
+            last = (atomicAdd(&bar[0], 1u) == nblocks - 1) ? 1 : 0;
+            __threadfence();
+        }
+        *s_flag = last;
+    }
+    __syncthreads();
+    return *s_flag != 0;
+}
+
+__device__ void release_all(unsigned* bar, unsigned* err, unsigned& gen) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (ld_acquire(err) == 0) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        }
+        gen += 1;
+    }
+    __syncthreads();
+}
+
+__device__ void wait_release(unsigned* bar, unsigned* err, unsigned& gen) {
+    if (threadIdx.x == 0) {
+        unsigned spins = 0;
+        while (ld_acquire(err) == 0 && ld_acquire(&bar[1]) == gen) {
+            if (++spins > kSpinLimit) {
+                atomicExch(err, kDevErrBarrierTimeout);
+                break;
+            }
+            __nanosleep(32);
+        }
+        gen += 1;
+        __threadfence();
+    }
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Per-pixel association (ICPTracker.cpp:236-328).
 struct Rel {
@@ -121,29 +171,34 @@ struct Acc {
 
 __device__ __forceinline__ bool normal_valid(F3 n) { return finite3(n) && sqnorm3(n) > 0.9f; }
 
-__device__ __forceinline__ void associate(const IcpArgs& a, const Rel& r, const IcpLevel& L, int x, int y, Acc& acc) {
-    const int idx = y * L.W + x;
-    const F3 lv = mk3(__ldg(L.v + 3 * idx), __ldg(L.v + 3 * idx + 1), __ldg(L.v + 3 * idx + 2));
-    if (lv.z <= 0.001f || !finite3(lv)) return;
+__device__ __forceinline__ F3 ld3(const float* p, int i) {
+    return mk3(__ldg(p + 3 * i), __ldg(p + 3 * i + 1), __ldg(p + 3 * i + 2));
+}
+
+// First half: live point into the model image. Returns the model pixel or -1.
+__device__ __forceinline__ int associate_project(const IcpArgs& a, const Rel& r, F3 lv, Acc& acc) {
+    if (lv.z <= 0.001f || !finite3(lv)) return -1;
     const F3 vr = add3(mv3(r.Rrel, lv), r.trel);
-    if (vr.z <= 0.001f) return;
+    if (vr.z <= 0.001f) return -1;
     acc.i[1]++;
     const float inv_z = fd(1.0f, vr.z);
     const float mxf = fa(fm(fm(a.fx, vr.x), inv_z), a.cx);
     const float myf = fa(fm(fm(a.fy, vr.y), inv_z), a.cy);
     int mx, my;
-    if (!floor_to_int(fa(mxf, 0.5f), &mx) || !floor_to_int(fa(myf, 0.5f), &my)) return;
-    if (mx < 0 || mx >= a.MW || my < 0 || my >= a.MH) return;
+    if (!floor_to_int(fa(mxf, 0.5f), &mx) || !floor_to_int(fa(myf, 0.5f), &my)) return -1;
+    if (mx < 0 || mx >= a.MW || my < 0 || my >= a.MH) return -1;
     acc.i[3]++;
-    const int m = my * a.MW + mx;
-    const F3 mv = mk3(__ldg(a.mv + 3 * m), __ldg(a.mv + 3 * m + 1), __ldg(a.mv + 3 * m + 2));
-    const F3 mn = mk3(__ldg(a.mn + 3 * m), __ldg(a.mn + 3 * m + 1), __ldg(a.mn + 3 * m + 2));
+    return my * a.MW + mx;
+}
+
+// Second half: filters and the normal-equation terms of one association.
+__device__ __forceinline__ void associate_finish(const IcpArgs& a, const Rel& r, F3 lv, F3 ln, F3 mv, F3 mn,
+                                                 Acc& acc) {
     if (!(finite3(mv) && sqnorm3(mv) > 1e-12f) || !normal_valid(mn)) return;
     acc.i[2]++;
     const F3 vw = add3(mv3(r.Rcw, lv), r.tcw);
     const F3 dvm = sub3(vw, mv);
     if (sqnorm3(dvm) > a.dist2) { acc.i[4]++; return; }
-    const F3 ln = mk3(__ldg(L.n + 3 * idx), __ldg(L.n + 3 * idx + 1), __ldg(L.n + 3 * idx + 2));
     if (!normal_valid(ln)) return;
     const F3 nw = mv3(r.Rcw, ln);
     if (fabsf(dot3(nw, mn)) < a.angle_cos) { acc.i[5]++; return; }
@@ -172,80 +227,154 @@ __device__ __forceinline__ void associate(const IcpArgs& a, const Rel& r, const 
     acc.i[0]++;
 }
 
-// Block reduction of one pass into global partial slot `slot`.
-__device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, double* s_red, int* s_ired) {
+// The interior pixels p = first, first + stride, ... of a level, two at a
+// time so that the loads of both are in flight together. Accumulation order
+// is the pixel order.
+__device__ __forceinline__ void associate_range(const IcpArgs& a, const Rel& r, const IcpLevel& L, int first,
+                                                int stride, int n, Acc& acc) {
+    const int iw = L.W - 2;
+    const F3 zero = mk3(0.0f, 0.0f, 0.0f);
+    for (int p0 = first; p0 < n; p0 += 2 * stride) {
+        const int p1 = p0 + stride;
+        const bool has1 = p1 < n;
+        const int i0 = (1 + p0 / iw) * L.W + 1 + p0 % iw;
+        const int i1 = has1 ? (1 + p1 / iw) * L.W + 1 + p1 % iw : i0;
+        const F3 lv0 = ld3(L.v, i0), ln0 = ld3(L.n, i0);
+        const F3 lv1 = has1 ? ld3(L.v, i1) : zero, ln1 = has1 ? ld3(L.n, i1) : zero;
+        const int m0 = associate_project(a, r, lv0, acc);
+        const int m1 = has1 ? associate_project(a, r, lv1, acc) : -1;
+        const F3 mv0 = m0 >= 0 ? ld3(a.mv, m0) : zero, mn0 = m0 >= 0 ? ld3(a.mn, m0) : zero;
+        const F3 mv1 = m1 >= 0 ? ld3(a.mv, m1) : zero, mn1 = m1 >= 0 ? ld3(a.mn, m1) : zero;
+        if (m0 >= 0) associate_finish(a, r, lv0, ln0, mv0, mn0, acc);
+        if (m1 >= 0) associate_finish(a, r, lv1, ln1, mv1, mn1, acc);
+    }
+}
+
+// Warp sum of 32 values per lane by recursive halving: at offset o each lane
+// keeps half of its values, adds the partner's copy of that half and hands it
+// the other half. After five steps lane l holds the warp sum of value l
+// (31 shuffles instead of 32 x 5). Fixed pattern, so deterministic.
+template <typename T>
+__device__ __forceinline__ T warp_sum_transpose32(T (&v)[32], int lane) {
+#pragma unroll
+    for (int lvl = 0; lvl < 5; ++lvl) {
+        const int o = 16 >> lvl, n = 16 >> lvl;
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < n; ++i) {
+            const T send = upper ? v[i] : v[i + n];
+            const T keep = upper ? v[i + n] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0];
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block reduction of one pass into global partial slot `slot`, in the
+// accumulation type T: float, or double for the precision form (the float
+// path issues no FP64 instruction; GB300's FP64 rate is a small fraction of
+// its FP32 rate). The six counters travel as T: every per-block count is
+// below 2^24, so exact. Partials are stored value-major, [slot][value][block],
+// so the grid reduction reads them coalesced; the partial buffers and the
+// shared staging are sized for double and reinterpreted for float.
+template <typename T>
+__device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc, int slot, double* s_red_raw) {
+    constexpr int kNV = kNF + kNI;  // 34
+    T* s_red = reinterpret_cast<T*>(s_red_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
-    if (a.precision) {
+    T v[32];
 #pragma unroll
-        for (int k = 0; k < kNF; ++k) {
-            double v = acc.f[k];
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) s_red[warp * kNF + k] = v;
-        }
-    } else {
+    for (int k = 0; k < kNF; ++k) v[k] = static_cast<T>(acc.f[k]);
 #pragma unroll
-        for (int k = 0; k < kNF; ++k) {
-            float v = acc.f[k];
-            for (int o = 16; o > 0; o >>= 1) v = fa(v, __shfl_down_sync(0xffffffffu, v, o));
-            if (lane == 0) s_red[warp * kNF + k] = v;
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < kNI; ++k) {
-        int v = acc.i[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) s_ired[warp * kNI + k] = v;
+    for (int k = kNF; k < 32; ++k) v[k] = static_cast<T>(acc.i[k - kNF]);
+    const T e0 = warp_sum(static_cast<T>(acc.i[32 - kNF]));
+    const T e1 = warp_sum(static_cast<T>(acc.i[33 - kNF]));
+    const T mine = warp_sum_transpose32(v, lane);
+    s_red[warp * kNV + lane] = mine;
+    if (lane == 0) {
+        s_red[warp * kNV + 32] = e0;
+        s_red[warp * kNV + 33] = e1;
     }
     __syncthreads();
-    const size_t base = (static_cast<size_t>(slot) * gridDim.x + blockIdx.x);
-    if (threadIdx.x < kNF) {
-        if (a.precision) {
-            double s = 0.0;
-            for (int w = 0; w < nw; ++w) s += s_red[w * kNF + threadIdx.x];
-            a.partials[base * kNF + threadIdx.x] = s;
-        } else {
-            float s = 0.0f;
-            for (int w = 0; w < nw; ++w) s = fa(s, static_cast<float>(s_red[w * kNF + threadIdx.x]));
-            a.partials[base * kNF + threadIdx.x] = static_cast<double>(s);
-        }
-    } else if (threadIdx.x < kNF + kNI) {
-        const int k = threadIdx.x - kNF;
-        int s = 0;
-        for (int w = 0; w < nw; ++w) s += s_ired[w * kNI + k];
-        a.ipartials[base * kNI + k] = s;
+    const int k = threadIdx.x, nb = gridDim.x;
+    if (k < kNF) {
+        T sum = T(0);
+        for (int w = 0; w < nw; ++w) sum += s_red[w * kNV + k];
+        reinterpret_cast<T*>(a.partials)[(static_cast<size_t>(slot) * kNF + k) * nb + blockIdx.x] = sum;
+    } else if (k < kNV) {
+        T sum = T(0);
+        for (int w = 0; w < nw; ++w) sum += s_red[w * kNV + k];
+        a.ipartials[(static_cast<size_t>(slot) * kNI + (k - kNF)) * nb + blockIdx.x] = static_cast<int>(sum);
     }
     __syncthreads();
 }
 
-// Every block: sum all block partials of `slot` in a fixed order.
-__device__ void reduce_grid(const IcpArgs& a, int slot, double* s_sum, int* s_isum) {
+__device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, double* s_red, int* /*unused*/) {
+    if (a.precision) reduce_block_t<double>(a, acc, slot, s_red);
+    else reduce_block_t<float>(a, acc, slot, s_red);
+}
+
+// Sum of all block partials of `slot` in one fixed order (lane l takes blocks
+// l, l + 32, ...; then a fixed shuffle tree), so the result does not depend
+// on which block computes it. All loads of a lane are issued before the adds.
+// The sums land in s_sum as T (float sums in the first half of the storage).
+constexpr int kMaxGridBlocks = 512;
+constexpr int kPerLane = kMaxGridBlocks / 32;
+
+template <typename T>
+__device__ __forceinline__ void reduce_grid_t(const IcpArgs& a, int slot, double* s_sum_raw, int* s_isum) {
+    T* s_sum = reinterpret_cast<T*>(s_sum_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
     const int nb = gridDim.x;
-    const size_t base = static_cast<size_t>(slot) * nb;
     for (int k = warp; k < kNF + kNI; k += nw) {
         if (k < kNF) {
-            if (a.precision) {
-                double s = 0.0;
-                for (int b = lane; b < nb; b += 32) s += __ldcg(a.partials + (base + b) * kNF + k);
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-                if (lane == 0) s_sum[k] = s;
-            } else {
-                float s = 0.0f;
-                for (int b = lane; b < nb; b += 32) s = fa(s, static_cast<float>(__ldcg(a.partials + (base + b) * kNF + k)));
-                for (int o = 16; o > 0; o >>= 1) s = fa(s, __shfl_down_sync(0xffffffffu, s, o));
-                if (lane == 0) s_sum[k] = static_cast<double>(s);
+            const T* src = reinterpret_cast<const T*>(a.partials) + (static_cast<size_t>(slot) * kNF + k) * nb;
+            T v[kPerLane];
+#pragma unroll
+            for (int j = 0; j < kPerLane; ++j) {
+                const int b = lane + 32 * j;
+                v[j] = b < nb ? __ldcg(src + b) : T(0);
             }
+            T sum = T(0);
+#pragma unroll
+            for (int j = 0; j < kPerLane; ++j) sum += v[j];
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+            if (lane == 0) s_sum[k] = sum;
         } else {
             const int kk = k - kNF;
-            int s = 0;
-            for (int b = lane; b < nb; b += 32) s += __ldcg(a.ipartials + (base + b) * kNI + kk);
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0) s_isum[kk] = s;
+            const int* src = a.ipartials + (static_cast<size_t>(slot) * kNI + kk) * nb;
+            int v[kPerLane];
+#pragma unroll
+            for (int j = 0; j < kPerLane; ++j) {
+                const int b = lane + 32 * j;
+                v[j] = b < nb ? __ldcg(src + b) : 0;
+            }
+            int sum = 0;
+#pragma unroll
+            for (int j = 0; j < kPerLane; ++j) sum += v[j];
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+            if (lane == 0) s_isum[kk] = sum;
         }
     }
     __syncthreads();
+}
+
+__device__ void reduce_grid(const IcpArgs& a, int slot, double* s_sum, int* s_isum) {
+    if (a.precision) reduce_grid_t<double>(a, slot, s_sum, s_isum);
+    else reduce_grid_t<float>(a, slot, s_sum, s_isum);
+}
+
+// Reduced sum k as float (the storage holds floats unless in precision form).
+__device__ __forceinline__ float sum_f(const IcpArgs& a, const double* sum, int k) {
+    return a.precision ? static_cast<float>(sum[k]) : reinterpret_cast<const float*>(sum)[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -316,44 +445,6 @@ __device__ void warp_eig6(float* m /* smem 36, destroyed */, float* cs /* smem 1
     mx = hi;
 }
 
-// A x = b by LDL^T with symmetric diagonal pivoting (float, one thread).
-__device__ void ldlt_solve_f(const float* Ain, const float* b, float* x) {
-    float A[36], L[36], D[6], y[6], z[6];
-    int perm[6] = {0, 1, 2, 3, 4, 5};
-    for (int i = 0; i < 36; ++i) { A[i] = Ain[i]; L[i] = 0.0f; }
-    for (int k = 0; k < 6; ++k) {
-        int p = k;
-        for (int i = k + 1; i < 6; ++i) if (fabsf(A[i * 6 + i]) > fabsf(A[p * 6 + p])) p = i;
-        if (p != k) {
-            for (int j = 0; j < 6; ++j) { const float t = A[k * 6 + j]; A[k * 6 + j] = A[p * 6 + j]; A[p * 6 + j] = t; }
-            for (int i = 0; i < 6; ++i) { const float t = A[i * 6 + k]; A[i * 6 + k] = A[i * 6 + p]; A[i * 6 + p] = t; }
-            for (int j = 0; j < k; ++j) { const float t = L[k * 6 + j]; L[k * 6 + j] = L[p * 6 + j]; L[p * 6 + j] = t; }
-            const int t = perm[k]; perm[k] = perm[p]; perm[p] = t;
-        }
-        D[k] = A[k * 6 + k];
-        L[k * 6 + k] = 1.0f;
-        for (int i = k + 1; i < 6; ++i) L[i * 6 + k] = fd(A[i * 6 + k], D[k]);
-        for (int i = k + 1; i < 6; ++i)
-            for (int j = k + 1; j <= i; ++j) {
-                A[i * 6 + j] = fs(A[i * 6 + j], fm(L[i * 6 + k], A[j * 6 + k]));
-                A[j * 6 + i] = A[i * 6 + j];
-            }
-        for (int i = k + 1; i < 6; ++i) A[i * 6 + k] = A[k * 6 + i] = 0.0f;
-    }
-    for (int i = 0; i < 6; ++i) {
-        float s = b[perm[i]];
-        for (int j = 0; j < i; ++j) s = fs(s, fm(L[i * 6 + j], y[j]));
-        y[i] = s;
-    }
-    for (int i = 0; i < 6; ++i) y[i] = fd(y[i], D[i]);
-    for (int i = 5; i >= 0; --i) {
-        float s = y[i];
-        for (int j = i + 1; j < 6; ++j) s = fs(s, fm(L[j * 6 + i], z[j]));
-        z[i] = s;
-    }
-    for (int i = 0; i < 6; ++i) x[perm[i]] = z[i];
-}
-
 // A x = b by Cholesky in double (precision form).
 __device__ bool chol_solve_d(const double* Ain, const double* b, double* x) {
     double L[36];
@@ -403,22 +494,33 @@ __device__ void project_so3(float* P /* row-major 4x4, rotation block replaced *
     for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) P[4 * i + j] = static_cast<float>(R[3 * i + j]);
 }
 
-// The same projection in float: the polar iteration converges quadratically
-// from a near-rotation, three steps reach float precision.
+// The same projection in float by the Newton-Schulz iteration
+// X <- X (3 I - X^T X) / 2, which converges quadratically to the orthogonal
+// polar factor from a near-rotation (no division); two steps reach float
+// precision from the composed pose.
 __device__ void project_so3_f(float* P) {
-    float R[9];
-    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) R[3 * i + j] = P[4 * i + j];
-    for (int it = 0; it < 3; ++it) {
-        const float c00 = R[4] * R[8] - R[5] * R[7], c01 = R[5] * R[6] - R[3] * R[8], c02 = R[3] * R[7] - R[4] * R[6];
-        const float c10 = R[2] * R[7] - R[1] * R[8], c11 = R[0] * R[8] - R[2] * R[6], c12 = R[1] * R[6] - R[0] * R[7];
-        const float c20 = R[1] * R[5] - R[2] * R[4], c21 = R[2] * R[3] - R[0] * R[5], c22 = R[0] * R[4] - R[1] * R[3];
-        const float id = 1.0f / (R[0] * c00 + R[1] * c01 + R[2] * c02);
-        const float N[9] = {0.5f * (R[0] + c00 * id), 0.5f * (R[1] + c01 * id), 0.5f * (R[2] + c02 * id),
-                            0.5f * (R[3] + c10 * id), 0.5f * (R[4] + c11 * id), 0.5f * (R[5] + c12 * id),
-                            0.5f * (R[6] + c20 * id), 0.5f * (R[7] + c21 * id), 0.5f * (R[8] + c22 * id)};
-        for (int k = 0; k < 9; ++k) R[k] = N[k];
+    float X[9];
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) X[3 * i + j] = P[4 * i + j];
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        float G[9];  // 3 I - X^T X
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float g = X[i] * X[j] + X[3 + i] * X[3 + j] + X[6 + i] * X[6 + j];
+                G[3 * i + j] = (i == j ? 3.0f : 0.0f) - g;
+            }
+        float N[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                N[3 * i + j] = 0.5f * (X[3 * i] * G[j] + X[3 * i + 1] * G[3 + j] + X[3 * i + 2] * G[6 + j]);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) X[k] = N[k];
     }
-    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) P[4 * i + j] = R[3 * i + j];
+    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) P[4 * i + j] = X[3 * i + j];
 }
 
 // Rodrigues rotation (Eigen::AngleAxisf::toRotationMatrix) into a row-major 3x3.
@@ -446,36 +548,106 @@ struct LevelState {
 
 // Shared-memory scratch of the solve.
 struct SolveSmem {
-    double sum[kNF];
+    double sum[kNF];  // reduced sums: double (precision form) or float in the first half
     int isum[kNI];
     float m[36];
     float cs[12];
     int action;    // 0 continue, 1 stop level
     int need_eig;  // the shifted-Cholesky test could not settle the damping
+    float xdef[6]; // solution with the level's default damping
+    int xdef_ok;
 };
 
-// True when A - shift I is positive definite (float Cholesky, one thread).
-__device__ bool pd_after_shift(const float* A, float shift) {
-    float L[36];
+// Cholesky factor of A + shift I (6x6, float), fully unrolled so that the
+// factor stays in registers. False when a pivot is not positive.
+__device__ __forceinline__ bool chol6_f(const float* A, float shift, float (&L)[36], float (&inv)[6]) {
+#pragma unroll
     for (int j = 0; j < 6; ++j) {
-        float s = A[j * 6 + j] - shift;
-        for (int k = 0; k < j; ++k) s -= L[j * 6 + k] * L[j * 6 + k];
-        if (!(s > 0.0f)) return false;
-        const float d = sqrtf(s);
+        float sj = A[j * 6 + j] + shift;
+#pragma unroll
+        for (int k = 0; k < j; ++k) sj -= L[j * 6 + k] * L[j * 6 + k];
+        if (!(sj > 0.0f)) return false;
+        const float d = sqrtf(sj);
+        inv[j] = 1.0f / d;
         L[j * 6 + j] = d;
+#pragma unroll
         for (int i = j + 1; i < 6; ++i) {
             float t = A[i * 6 + j];
+#pragma unroll
             for (int k = 0; k < j; ++k) t -= L[i * 6 + k] * L[j * 6 + k];
-            L[i * 6 + j] = t / d;
+            L[i * 6 + j] = t * inv[j];
         }
     }
     return true;
 }
 
+// True when A - shift I is positive definite.
+__device__ bool pd_after_shift(const float* A, float shift) {
+    float L[36], inv[6];
+    return chol6_f(A, -shift, L, inv);
+}
+
+// (A + damp I) x = b by Cholesky (A + damp I is positive definite for a
+// normal-equation matrix); NaN when the factorisation breaks down, which the
+// caller's finiteness check turns into a stop.
+__device__ void chol6_solve_f(const float* A, float damp, const float* b, float* x) {
+    float L[36], inv[6];
+    if (!chol6_f(A, damp, L, inv)) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) x[i] = __int_as_float(0x7fffffff);
+        return;
+    }
+    float y[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        float t = b[i];
+#pragma unroll
+        for (int k = 0; k < i; ++k) t -= L[i * 6 + k] * y[k];
+        y[i] = t * inv[i];
+    }
+#pragma unroll
+    for (int i = 5; i >= 0; --i) {
+        float t = y[i];
+#pragma unroll
+        for (int k = i + 1; k < 6; ++k) t -= L[k * 6 + i] * x[k];
+        x[i] = t * inv[i];
+    }
+}
+
+// Damped solve of (A + damp I) x = b from the reduced sums: Cholesky in float,
+// or in double for the precision form (the reference's LDL^T of the same
+// positive definite matrix agrees to rounding). False when the
+// double factorisation breaks down.
+__device__ bool damped_solve(const IcpArgs& a, const SolveSmem& sm, float damp, float* x) {
+    if (a.precision) {
+        double A[36], b[6], xd[6];
+        int k = 0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j) { A[i * 6 + j] = A[j * 6 + i] = sm.sum[k++]; }
+        for (int i = 0; i < 6; ++i) { A[i * 6 + i] += damp; b[i] = sm.sum[21 + i]; }
+        if (!chol_solve_d(A, b, xd)) return false;
+        for (int i = 0; i < 6; ++i) x[i] = static_cast<float>(xd[i]);
+    } else {
+        float A[36], b[6];
+        int k = 0;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int j = i; j < 6; ++j) { A[i * 6 + j] = A[j * 6 + i] = sum_f(a, sm.sum, k++); }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) b[i] = sum_f(a, sm.sum, 21 + i);
+        chol6_solve_f(A, damp, b, x);
+    }
+    return true;
+}
+
 // One solve from the reduced sums (ICPTracker.cpp:78-131), executed by warp 0.
+// Lane 1 solves with the level's default damping while lane 0 runs the
+// damping test; only an escalated damping needs a second solve.
 __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelState& st) {
     const int lane = threadIdx.x & 31;
     const int inl = sm.isum[0];
+    const float base_damp = (level == 0) ? kDampingLevel0 : kDampingDefault;
     if (lane == 0) {
         for (int k = 1; k < 6; ++k) st.counts[k] = sm.isum[k];
         sm.action = (inl <= 0 || inl < kMinInliersForIteration) ? 1 : 0;
@@ -483,7 +655,7 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
             int k = 0;
             for (int i = 0; i < 6; ++i)
                 for (int j = i; j < 6; ++j) {
-                    const float v = static_cast<float>(sm.sum[k++]);
+                    const float v = sum_f(a, sm.sum, k++);
                     st.information[i * 6 + j] = v;
                     st.information[j * 6 + i] = v;
                 }
@@ -500,31 +672,26 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
             const float shift = 2.0f * sigma + 32.0f * 1.1920929e-7f * tr;
             sm.need_eig = (isfinite(tr) && pd_after_shift(st.information, shift)) ? 0 : 1;
         }
+    } else if (lane == 1 && !(inl <= 0 || inl < kMinInliersForIteration)) {
+        sm.xdef_ok = damped_solve(a, sm, base_damp, sm.xdef) ? 1 : 0;
     }
     __syncwarp();
     if (sm.action != 0) return;
     float mn = 1.0f, mx = 1.0f;
     if (sm.need_eig) warp_eig6(sm.m, sm.cs, mn, mx);
     if (lane != 0) return;
-    float damp = (level == 0) ? kDampingLevel0 : kDampingDefault;
+    float damp = base_damp;
     if (sm.need_eig) {
         if (!isfinite(mn) || !isfinite(mx) || mn < kMinEigEscalate) damp = kDampingEscalated;
         else if (mx > kCondEscalate * mn) damp = kDampingEscalated;
     }
     float x[6];
-    if (a.precision) {
-        double A[36], b[6], xd[6];
-        int k = 0;
-        for (int i = 0; i < 6; ++i)
-            for (int j = i; j < 6; ++j) { A[i * 6 + j] = A[j * 6 + i] = sm.sum[k++]; }
-        for (int i = 0; i < 6; ++i) { A[i * 6 + i] += damp; b[i] = sm.sum[21 + i]; }
-        if (!chol_solve_d(A, b, xd)) { sm.action = 1; return; }
-        for (int i = 0; i < 6; ++i) x[i] = static_cast<float>(xd[i]);
-    } else {
-        float A[36], b[6];
-        for (int i = 0; i < 36; ++i) A[i] = st.information[i];
-        for (int i = 0; i < 6; ++i) { A[i * 6 + i] = fa(A[i * 6 + i], damp); b[i] = static_cast<float>(sm.sum[21 + i]); }
-        ldlt_solve_f(A, b, x);
+    if (damp == base_damp) {
+        if (!sm.xdef_ok) { sm.action = 1; return; }
+        for (int i = 0; i < 6; ++i) x[i] = sm.xdef[i];
+    } else if (!damped_solve(a, sm, damp, x)) {
+        sm.action = 1;
+        return;
     }
     bool fin = true;
     for (int i = 0; i < 6; ++i) fin = fin && isfinite(x[i]);
@@ -562,7 +729,7 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
     else project_so3_f(P);
     for (int i = 0; i < 16; ++i) st.pose[i] = P[i];
     st.final_step = step_norm;
-    st.error = fd(static_cast<float>(sm.sum[27]), static_cast<float>(inl > 1 ? inl : 1));
+    st.error = fd(sum_f(a, sm.sum, 27), static_cast<float>(inl > 1 ? inl : 1));
     st.inliers = inl;
     st.iters++;
     if (step_norm < kConvergenceStep) {
@@ -601,8 +768,8 @@ __device__ int classify(const azu_icp_result& r, const float* prev) {
 }
 
 __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
-    __shared__ double s_red[(kIcpThreads / 32) * kNF];
-    __shared__ int s_ired[(kIcpThreads / 32) * kNI];
+    __shared__ double s_red[(kIcpThreads / 32) * (kNF + kNI)];
+    int* s_ired = nullptr;
     __shared__ SolveSmem sm;
     __shared__ LevelState st;
     __shared__ Rel s_rel;
@@ -611,6 +778,7 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
     __shared__ float s_start[16];
     __shared__ azu_icp_result s_res;
     __shared__ int s_retry;
+    __shared__ int s_last;
 
     if (threadIdx.x == 0) {
         s_gen = ld_acquire(&a.bar[1]);
@@ -633,8 +801,7 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
         for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
         const int iw = L.W - 2, ih = L.H - 2;
         const int n = iw > 0 && ih > 0 ? iw * ih : 0;
-        for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
-            associate(a, rel, L, 1 + p % iw, 1 + p / iw, acc);
+        associate_range(a, rel, L, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, acc);
         reduce_block(a, acc, 0, s_red, s_ired);
         grid_sync(a.bar, a.err, gridDim.x, gen);
         reduce_grid(a, 0, sm.sum, sm.isum);
@@ -642,12 +809,12 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
             int k = 0;
             for (int i = 0; i < 6; ++i)
                 for (int j = i; j < 6; ++j) {
-                    const float v = static_cast<float>(sm.sum[k++]);
+                    const float v = sum_f(a, sm.sum, k++);
                     a.build_out[i * 6 + j] = v;
                     a.build_out[j * 6 + i] = v;
                 }
-            for (int i = 0; i < 6; ++i) a.build_out[36 + i] = static_cast<float>(sm.sum[21 + i]);
-            a.build_out[42] = static_cast<float>(sm.sum[27]);
+            for (int i = 0; i < 6; ++i) a.build_out[36 + i] = sum_f(a, sm.sum, 21 + i);
+            a.build_out[42] = sum_f(a, sm.sum, 27);
             for (int i = 0; i < 6; ++i) reinterpret_cast<int*>(a.build_out)[43 + i] = sm.isum[i];
         }
         return;
@@ -691,14 +858,28 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
                 for (int k = 0; k < kNF; ++k) acc.f[k] = 0.0f;
 #pragma unroll
                 for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
-                for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
-                    associate(a, rel, L, 1 + p % iw, 1 + p / iw, acc);
+                associate_range(a, rel, L, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, acc);
                 reduce_block(a, acc, slot, s_red, s_ired);
-                grid_sync(a.bar, a.err, gridDim.x, gen);
-                reduce_grid(a, slot, sm.sum, sm.isum);
+                constexpr int kWords = static_cast<int>(sizeof(LevelState) / 4);
+                unsigned* st_words = reinterpret_cast<unsigned*>(&st);
+                if (arrive_last(a.bar, a.err, gridDim.x, &s_last)) {
+                    reduce_grid(a, slot, sm.sum, sm.isum);
+                    if (threadIdx.x < 32) solve_step(a, level, sm, st);
+                    __syncthreads();
+                    for (int i = threadIdx.x; i <= kWords; i += blockDim.x)
+                        __stcg(a.state + i, i < kWords ? st_words[i] : static_cast<unsigned>(sm.action));
+                    __threadfence();
+                    release_all(a.bar, a.err, gen);
+                } else {
+                    wait_release(a.bar, a.err, gen);
+                    for (int i = threadIdx.x; i <= kWords; i += blockDim.x) {
+                        const unsigned w = __ldcg(a.state + i);
+                        if (i < kWords) st_words[i] = w;
+                        else sm.action = static_cast<int>(w);
+                    }
+                    __syncthreads();
+                }
                 slot ^= 1;
-                if (threadIdx.x < 32) solve_step(a, level, sm, st);
-                __syncthreads();
                 if (sm.action != 0) break;
             }
             // track(): the level result replaces the running one; final_step
@@ -765,7 +946,7 @@ struct azu_tracker {
     int nblocks = 0;
     double* partials = nullptr;
     int* ipartials = nullptr;
-    unsigned* bar = nullptr;  // [0] arrivals [1] generation [2] error
+    unsigned* bar = nullptr;  // [0] arrivals [1] generation [2] error [4..] published state
     float* d_est = nullptr;   // 16 estimate, 16 ref, 16 prev
     azu_icp_result* d_result = nullptr;
     float* d_build = nullptr;
@@ -824,6 +1005,7 @@ static void fill_args(azu_tracker* t, IcpArgs& a, const float* mv, const float* 
     a.ipartials = t->ipartials;
     a.bar = t->bar;
     a.err = t->bar + 2;
+    a.state = t->bar + 4;
 }
 
 int icp_launch(azu_tracker* t, const IcpArgs& a, cudaStream_t s) {
@@ -880,10 +1062,10 @@ extern "C" int azu_tracker_create(int device, const azu_tracker_params* p, void*
         if (e != cudaSuccess || occ < 1) { set_error("ICP occupancy query failed"); rc = AZU_E_CUDA; }
     }
     if (!rc) {
-        t->nblocks = sms * std::min(occ, 2);
+        t->nblocks = std::min(sms * std::min(occ, 2), kMaxGridBlocks);
         cudaError_t e = cudaMalloc(&t->partials, sizeof(double) * 2 * t->nblocks * kNF);
         if (e == cudaSuccess) e = cudaMalloc(&t->ipartials, sizeof(int) * 2 * t->nblocks * kNI);
-        if (e == cudaSuccess) e = cudaMalloc(&t->bar, sizeof(unsigned) * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&t->bar, sizeof(unsigned) * (4 + sizeof(LevelState) / 4 + 1));
         if (e == cudaSuccess) e = cudaMemset(t->bar, 0, sizeof(unsigned) * 4);
         if (e == cudaSuccess) e = cudaMalloc(&t->d_est, sizeof(float) * 48);
         if (e == cudaSuccess) e = cudaMalloc(&t->d_result, sizeof(azu_icp_result));
@@ -1095,7 +1277,7 @@ static int static_slot_for_current_device(StaticSlot& out) {
         AZU_TRY_CUDA(cudaGetSymbolAddress(&p, g_icp_static_scratch));
         int occ = 0;
         AZU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, icp_kernel, kIcpThreads, 0));
-        s.nblocks = prop.multiProcessorCount * std::min(occ, 2);
+        s.nblocks = std::min(prop.multiProcessorCount * std::min(occ, 2), azu::kMaxGridBlocks);
         s.base = static_cast<unsigned char*>(p);
     }
     out = s;
@@ -1153,6 +1335,7 @@ extern "C" int azu_icp_build_system_noalloc(const float* d_live_vertices, const 
     a.ipartials = reinterpret_cast<int*>(slot.base + kOffIPartials);
     a.bar = d_bar;
     a.err = d_bar + 2;
+    a.state = nullptr;  // build mode publishes no iteration state
     a.build_out = d_out;
 
     cudaLaunchConfig_t cfg = {};

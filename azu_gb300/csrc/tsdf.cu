@@ -102,76 +102,173 @@ __global__ void reset_kernel(void* vox, float* color, size_t n) {
     }
 }
 
+// ---- integration -----------------------------------------------------------
+constexpr int kIntWarps = 4;
+constexpr int kTileShift = 3;  // level-0 depth tiles are 8x8 pixels
+
+// Deepest in-band depth of every 8x8 pixel tile (-inf when the tile has none),
+// level 0 of the tile pyramid. Eight lanes share a tile, one pixel row each.
+__global__ void depth_tiles_kernel(const float* __restrict__ depth, int W, int H, float min_d, float max_d, int tw,
+                                   int ntiles, float* __restrict__ tiles, const int* __restrict__ gate) {
+    if (gate && __ldg(gate) == 0) return;
+    const int t = blockIdx.x * (blockDim.x >> 3) + (threadIdx.x >> 3);
+    const int r = threadIdx.x & 7;
+    float m = -__int_as_float(0x7f800000);
+    if (t < ntiles) {
+        const int ty = t / tw, tx = t - ty * tw;
+        const int y = (ty << kTileShift) + r;
+        if (y < H) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int x = (tx << kTileShift) + i;
+                if (x < W) {
+                    const float d = __ldg(depth + static_cast<size_t>(y) * W + x);
+                    if (d >= min_d && d <= max_d) m = fmaxf(m, d);
+                }
+            }
+        }
+    }
+    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 4));
+    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+    if (t < ntiles && r == 0) tiles[t] = m;
+}
+
+TileMip make_tile_mip(int W, int H) {
+    TileMip m{};
+    int w = (W + 7) >> kTileShift, h = (H + 7) >> kTileShift, off = 0;
+    for (m.levels = 0; m.levels < kMaxTileLevels; ++m.levels) {
+        m.w[m.levels] = w;
+        m.h[m.levels] = h;
+        m.off[m.levels] = off;
+        off += w * h;
+        if (w == 1 && h == 1) {
+            ++m.levels;
+            break;
+        }
+        w = (w + 1) >> 1;
+        h = (h + 1) >> 1;
+    }
+    m.total = off;
+    return m;
+}
+
 // Frustum AABB and camera transform for one integration (TSDFVolume.cpp:238-264),
 // computed on the device so the pose may come from the tracker without a host
-// round trip. Same float expression trees as the CPU path.
+// round trip. Same float expression trees as the CPU path. Thread 0 writes the
+// constants; the block then builds levels 1.. of the tile pyramid.
 __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res, float vs, float ox, float oy,
                                        float oz, float trunc, float fx, float fy, float cx, float cy, int W, int H,
-                                       float max_d, IntegrateConsts* out, unsigned long long* counters) {
-    if (threadIdx.x != 0) return;
-    float P[16], inv[16], Rcw[9];
-    for (int i = 0; i < 16; ++i) P[i] = d_pose[i];
-    inverse4(P, inv);
-    IntegrateConsts ic;
-    rot_of(inv, ic.R_wc);
-    const F3 t_wc = trans_of(inv);
-    ic.t_wc[0] = t_wc.x; ic.t_wc[1] = t_wc.y; ic.t_wc[2] = t_wc.z;
-    rot_of(P, Rcw);
-    const F3 t_cw = trans_of(P);
-    const F3 origin = mk3(ox, oy, oz);
-    F3 lo = div3(sub3(t_cw, origin), vs);
-    F3 hi = lo;
-    const float z_far = fa(max_d, trunc);
-    const float cpx[4][2] = {{0.0f, 0.0f}, {float(W), 0.0f}, {0.0f, float(H)}, {float(W), float(H)}};
-    for (int k = 0; k < 4; ++k) {
-        const F3 ray = mk3(fm(fd(fs(cpx[k][0], cx), fx), z_far), fm(fd(fs(cpx[k][1], cy), fy), z_far), z_far);
-        const F3 v = div3(sub3(add3(mv3(Rcw, ray), t_cw), origin), vs);
-        lo = mk3(v.x < lo.x ? v.x : lo.x, v.y < lo.y ? v.y : lo.y, v.z < lo.z ? v.z : lo.z);
-        hi = mk3(hi.x < v.x ? v.x : hi.x, hi.y < v.y ? v.y : hi.y, hi.z < v.z ? v.z : hi.z);
+                                       float max_d, IntegrateConsts* out, unsigned long long* counters,
+                                       float* __restrict__ tiles, TileMip mip) {
+    if (threadIdx.x == 0) {
+        float P[16], inv[16], Rcw[9];
+        for (int i = 0; i < 16; ++i) P[i] = d_pose[i];
+        inverse4(P, inv);
+        IntegrateConsts ic;
+        rot_of(inv, ic.R_wc);
+        const F3 t_wc = trans_of(inv);
+        ic.t_wc[0] = t_wc.x; ic.t_wc[1] = t_wc.y; ic.t_wc[2] = t_wc.z;
+        rot_of(P, Rcw);
+        const F3 t_cw = trans_of(P);
+        const F3 origin = mk3(ox, oy, oz);
+        F3 lo = div3(sub3(t_cw, origin), vs);
+        F3 hi = lo;
+        const float z_far = fa(max_d, trunc);
+        const float cpx[4][2] = {{0.0f, 0.0f}, {float(W), 0.0f}, {0.0f, float(H)}, {float(W), float(H)}};
+        for (int k = 0; k < 4; ++k) {
+            const F3 ray = mk3(fm(fd(fs(cpx[k][0], cx), fx), z_far), fm(fd(fs(cpx[k][1], cy), fy), z_far), z_far);
+            const F3 v = div3(sub3(add3(mv3(Rcw, ray), t_cw), origin), vs);
+            lo = mk3(v.x < lo.x ? v.x : lo.x, v.y < lo.y ? v.y : lo.y, v.z < lo.z ? v.z : lo.z);
+            hi = mk3(hi.x < v.x ? v.x : hi.x, hi.y < v.y ? v.y : hi.y, hi.z < v.z ? v.z : hi.z);
+        }
+        ic.valid = finite3(lo) && finite3(hi);
+        auto clampIdx = [res](float f) {
+            const float top = static_cast<float>(res - 1);
+            const float a = f < top ? f : top;
+            return static_cast<int>(a > 0.0f ? a : 0.0f);
+        };
+        ic.x0 = ic.valid ? clampIdx(floorf(lo.x)) : 0;
+        ic.x1 = ic.valid ? clampIdx(ceilf(hi.x)) : -1;
+        ic.y0 = ic.valid ? clampIdx(floorf(lo.y)) : 0;
+        ic.y1 = ic.valid ? clampIdx(ceilf(hi.y)) : -1;
+        ic.z0 = ic.valid ? clampIdx(floorf(lo.z)) : 0;
+        ic.z1 = ic.valid ? clampIdx(ceilf(hi.z)) : -1;
+        ic.step_x[0] = fm(ic.R_wc[0], vs);
+        ic.step_x[1] = fm(ic.R_wc[3], vs);
+        ic.step_x[2] = fm(ic.R_wc[6], vs);
+        // Bounds for the chunk culling. cmax bounds |c_i| over the AABB (c is
+        // affine in the voxel index, so a corner attains it), with slack for
+        // the stepped sums. A stepped coordinate then stays within
+        // 31 * ulp(cmax) / 2 of the line through its chunk start, and cull_eps
+        // is twice that and more. A voxel nearer than z_safe may project more
+        // than one pixel away from that line.
+        float cmax = 0.0f;
+        for (int k = 0; k < 8; ++k) {
+            const float px = ox + vs * static_cast<float>((k & 1) ? ic.x1 + 1 : ic.x0);
+            const float py = oy + vs * static_cast<float>((k & 2) ? ic.y1 + 1 : ic.y0);
+            const float pz = oz + vs * static_cast<float>((k & 4) ? ic.z1 + 1 : ic.z0);
+            const F3 c = add3(mv3(ic.R_wc, mk3(px, py, pz)), t_wc);
+            cmax = fmaxf(cmax, fmaxf(fabsf(c.x), fmaxf(fabsf(c.y), fabsf(c.z))));
+        }
+        cmax = cmax * 1.01f + 1e-3f;
+        const float eps = 40.0f * cmax * 1.1920929e-7f;  // 40 * 2^-23 * cmax
+        const float unx = (fmaxf(fabsf(cx), fabsf(float(W) - cx)) + 3.0f) / fx;
+        const float uny = (fmaxf(fabsf(cy), fabsf(float(H) - cy)) + 3.0f) / fy;
+        ic.cull_eps = eps;
+        ic.cull_off = trunc + eps + 1e-5f;
+        ic.z_safe = fmaxf(1e-3f, 2.0f * eps * (fmaxf(fx * (1.0f + unx), fy * (1.0f + uny)) + 2.0f));
+        if (!(isfinite(ic.cull_off) && isfinite(ic.z_safe))) ic.z_safe = __int_as_float(0x7f800000);
+        *out = ic;
+        counters[1] = 0;
+        counters[2] = 0;
     }
-    ic.valid = finite3(lo) && finite3(hi);
-    auto clampIdx = [res](float f) {
-        const float top = static_cast<float>(res - 1);
-        const float a = f < top ? f : top;
-        return static_cast<int>(a > 0.0f ? a : 0.0f);
-    };
-    ic.x0 = ic.valid ? clampIdx(floorf(lo.x)) : 0;
-    ic.x1 = ic.valid ? clampIdx(ceilf(hi.x)) : -1;
-    ic.y0 = ic.valid ? clampIdx(floorf(lo.y)) : 0;
-    ic.y1 = ic.valid ? clampIdx(ceilf(hi.y)) : -1;
-    ic.z0 = ic.valid ? clampIdx(floorf(lo.z)) : 0;
-    ic.z1 = ic.valid ? clampIdx(ceilf(hi.z)) : -1;
-    ic.step_x[0] = fm(ic.R_wc[0], vs);
-    ic.step_x[1] = fm(ic.R_wc[3], vs);
-    ic.step_x[2] = fm(ic.R_wc[6], vs);
-    *out = ic;
-    counters[1] = 0;
-    counters[2] = 0;
+    // tile pyramid: level l from level l-1, 2x2 children
+    for (int l = 1; l < mip.levels; ++l) {
+        __syncthreads();
+        const float* src = tiles + mip.off[l - 1];
+        float* dst = tiles + mip.off[l];
+        const int sw = mip.w[l - 1], sh = mip.h[l - 1], w = mip.w[l], n = w * mip.h[l];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int ty = i / w, tx = i - ty * w;
+            const int x0 = 2 * tx, y0 = 2 * ty;
+            float m = src[y0 * sw + x0];
+            if (x0 + 1 < sw) m = fmaxf(m, src[y0 * sw + x0 + 1]);
+            if (y0 + 1 < sh) {
+                m = fmaxf(m, src[(y0 + 1) * sw + x0]);
+                if (x0 + 1 < sw) m = fmaxf(m, src[(y0 + 1) * sw + x0 + 1]);
+            }
+            dst[i] = m;
+        }
+    }
 }
 
 // Voxel-projective integration (TSDFVolume.cpp:282-329).
 //
 // The CPU steps the camera coordinate of a voxel row incrementally along x
 // (c += R_wc.col(0) * vs from the AABB start x0), so the pixel a voxel lands in
-// depends on that rounded running sum. To reproduce it exactly and still touch
-// memory coalesced, a warp owns 32 voxel rows (32 consecutive y at one z) and
-// walks them in chunks of 32 x:
-//   phase 1 (lane = row): replay the sequential c-steps for the chunk, project,
-//            test, and park the signed distance (NaN = no update) in shared memory;
-//   phase 2 (lane = x):   for each of the 32 rows, update the voxels that have a
-//            parked distance with one coalesced read-modify-write.
-// Voxels that take no update are never read, so HBM traffic is 2 x record size
-// per updated voxel.
-constexpr int kIntWarps = 4;
-
+// depends on that rounded running sum. A warp owns 32 voxel rows (32
+// consecutive y at one z) and walks them in chunks of 32 x:
+//   cull  (lane = row): the chunk's voxels lie within cull_eps of a segment;
+//          project its ends, take the deepest depth over the pixels the segment
+//          can reach (two tiles a side at the pyramid level that fits) and drop
+//          the chunk if its nearest voxel is beyond it by more than trunc;
+//   chain (lane = row): replay the sequential c-steps, parking c of live rows
+//          in shared memory;
+//   update (lane = x): for each live row, project every voxel exactly, test its
+//          8x8 tile, then gather depth and read-modify-write the voxel, all
+//          coalesced.
+// Every test is exact or conservative, so the updated set and the values are
+// the CPU's. Voxels that take no update are never read: HBM traffic is
+// 2 x record size per updated voxel.
 template <bool kHalf, bool kColor>
 __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     void* __restrict__ vox, float* __restrict__ color, const IntegrateConsts* __restrict__ icp,
     const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
     float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
-    float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb) {
-    __shared__ float s_cz[kIntWarps][32][33];
-    __shared__ int s_pix[kIntWarps][32][33];
+    float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb,
+    const float* __restrict__ tiles, TileMip mip) {
+    __shared__ float s_c[kIntWarps][3][32][33];
     if (gate && __ldg(gate) == 0) return;
     if (!__ldg(&icp->valid)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -188,43 +285,51 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     for (int i = 0; i < 9; ++i) R[i] = __ldg(&icp->R_wc[i]);
     const F3 t_wc = mk3(__ldg(&icp->t_wc[0]), __ldg(&icp->t_wc[1]), __ldg(&icp->t_wc[2]));
     const F3 step = mk3(__ldg(&icp->step_x[0]), __ldg(&icp->step_x[1]), __ldg(&icp->step_x[2]));
+    const float cull_eps = __ldg(&icp->cull_eps), cull_off = __ldg(&icp->cull_off), z_safe = __ldg(&icp->z_safe);
 
     const int y = ybase + lane;
     const bool row_on = (y >= y0 && y <= y1);
     F3 c = add3(mv3(R, add3(mk3(ox, oy, oz), mul3(mk3(float(x0), float(y), float(z)), vs))), t_wc);
     const float fW = static_cast<float>(W), fH = static_cast<float>(H);
     const float color_band = fm(0.5f, trunc);
-    const float qnan = __int_as_float(0x7fffffff);
     unsigned long long n_new = 0, n_upd = 0, n_col = 0;
     const size_t rr = static_cast<size_t>(res);
 
     // Conservative x-interval of this row that can land in front of the camera
     // and inside the image: c(t) = c(x0) + t step is linear, so each of
     // c.z > 0, 0 <= u, u < W, 0 <= v, v < H is a half-line in t (u, v times c.z
-    // are linear). Solved in double and widened by 2 voxels, far more than the
-    // rounding of the stepped coordinate can move a projection. Outside it a
-    // voxel only advances the coordinate, exactly as the sequential sweep does.
+    // are linear). Solved in float, every bound widened by the rounding of its
+    // coefficients (2^-21 relative, four times the worst case) and by 2
+    // voxels, far more than the rounding of the stepped coordinate can move a
+    // projection; a constraint whose direction rounding cannot settle is
+    // dropped. Outside the interval a voxel only advances the coordinate,
+    // exactly as the sequential sweep does.
     int xs = x1 + 1, xe = x0 - 1;
     if (row_on) {
-        double lo = 0.0, hi = static_cast<double>(x1 - x0);
-        auto keep = [&](double a, double b) {  // keep t with a + b t >= 0
-            if (b == 0.0) {
-                if (a < 0.0) { lo = 1.0; hi = 0.0; }
-            } else if (b > 0.0) {
-                lo = fmax(lo, -a / b);
-            } else {
-                hi = fmin(hi, -a / b);
+        const float tmax = static_cast<float>(x1 - x0);
+        float lo = 0.0f, hi = tmax;
+        constexpr float kRel = 4.76837158e-7f;  // 2^-21
+        auto keep = [&](float p1, float p2, float q1, float q2) {  // keep t with (p1 + p2) + (q1 + q2) t >= 0
+            const float a = p1 + p2, b = q1 + q2;
+            const float ea = kRel * (fabsf(p1) + fabsf(p2)), eb = kRel * (fabsf(q1) + fabsf(q2));
+            if (!(fabsf(b) > eb)) {
+                if (a + ea + (fabsf(b) + eb) * tmax < 0.0f) { lo = 1.0f; hi = 0.0f; }
+                return;
             }
+            const float t = -a / b;
+            const float err = (ea + fabsf(t) * eb) / fabsf(b) + fabsf(t) * kRel;
+            if (b > 0.0f) lo = fmaxf(lo, t - err);
+            else hi = fminf(hi, t + err);
         };
-        const double cxs = c.x, cys = c.y, czs = c.z, sx = step.x, sy = step.y, sz = step.z;
-        keep(czs, sz);
-        keep(fx * cxs + (cx + 0.5) * czs, fx * sx + (cx + 0.5) * sz);
-        keep(-(fx * cxs + (cx + 0.5 - W) * czs), -(fx * sx + (cx + 0.5 - W) * sz));
-        keep(fy * cys + (cy + 0.5) * czs, fy * sy + (cy + 0.5) * sz);
-        keep(-(fy * cys + (cy + 0.5 - H) * czs), -(fy * sy + (cy + 0.5 - H) * sz));
-        if (lo <= hi + 4.0) {
-            xs = max(x0, x0 + static_cast<int>(floor(lo)) - 2);
-            xe = min(x1, x0 + static_cast<int>(ceil(hi)) + 2);
+        const float cu = cx + 0.5f, cv = cy + 0.5f;
+        keep(c.z, 0.0f, step.z, 0.0f);
+        keep(fx * c.x, cu * c.z, fx * step.x, cu * step.z);
+        keep(-(fx * c.x), -((cu - fW) * c.z), -(fx * step.x), -((cu - fW) * step.z));
+        keep(fy * c.y, cv * c.z, fy * step.y, cv * step.z);
+        keep(-(fy * c.y), -((cv - fH) * c.z), -(fy * step.y), -((cv - fH) * step.z));
+        if (lo <= hi + 4.0f) {
+            xs = max(x0, x0 + static_cast<int>(floorf(lo)) - 2);
+            xe = min(x1, x0 + static_cast<int>(ceilf(hi)) + 2);
         }
     }
     int wxs = xs, wxe = xe;
@@ -238,67 +343,134 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
         for (int x = x0; x < xfirst; ++x) c = add3(c, step);
 
     for (int xc = xfirst; xc <= wxe; xc += 32) {
-        // phase 1 (lane = row): the sequential camera coordinate and the
-        // projection only; the pixel and the camera z are parked for phase 2.
-        bool any_pix = false;
-#pragma unroll 4
-        for (int k = 0; k < 32; ++k) {
-            const int x = xc + k;
-            int pix = -1;
-            float czk = 0.0f;
-            if (row_on && x >= x0 && x <= x1) {
-                if (x >= xs && x <= xe && c.z > 0.0f) {
-                    const float inv_z = __frcp_rn(c.z);  // == 1.0f / c.z, correctly rounded
-                    const float uf = floorf(fa(fa(fm(fm(fx, c.x), inv_z), cx), 0.5f));
-                    const float vf = floorf(fa(fa(fm(fm(fy, c.y), inv_z), cy), 0.5f));
-                    if (uf >= 0.0f && uf < fW && vf >= 0.0f && vf < fH) {
-                        pix = static_cast<int>(vf) * W + static_cast<int>(uf);
-                        czk = c.z;
-                        any_pix = true;
+        // cull (lane = row). The lane's c belongs to x = max(xc, x0).
+        bool live = false;
+        if (row_on) {
+            const int xcur = max(xc, x0);
+            const int xa = max(xcur, xs), xb = min(min(xc + 31, x1), xe);
+            if (xa <= xb) {
+                const float ka = static_cast<float>(xa - xcur), kb = static_cast<float>(xb - xcur);
+                const F3 ca = mk3(fmaf(ka, step.x, c.x), fmaf(ka, step.y, c.y), fmaf(ka, step.z, c.z));
+                const F3 cb = mk3(fmaf(kb, step.x, c.x), fmaf(kb, step.y, c.y), fmaf(kb, step.z, c.z));
+                if (!(ca.z >= z_safe && cb.z >= z_safe)) {
+                    live = true;  // near or behind the camera plane: no bound
+                } else {
+                    const float ua = fx * __fdividef(ca.x, ca.z) + cx, ub = fx * __fdividef(cb.x, cb.z) + cx;
+                    const float va = fy * __fdividef(ca.y, ca.z) + cy, vb = fy * __fdividef(cb.y, cb.z) + cy;
+                    const float ulo = fminf(ua, ub) - 2.0f, uhi = fmaxf(ua, ub) + 3.0f;
+                    const float vlo = fminf(va, vb) - 2.0f, vhi = fmaxf(va, vb) + 3.0f;
+                    if (uhi >= 0.0f && ulo < fW && vhi >= 0.0f && vlo < fH) {
+                        const int iu0 = static_cast<int>(fmaxf(ulo, 0.0f));
+                        const int iu1 = static_cast<int>(fminf(uhi, fW - 1.0f));
+                        const int iv0 = static_cast<int>(fmaxf(vlo, 0.0f));
+                        const int iv1 = static_cast<int>(fminf(vhi, fH - 1.0f));
+                        const int ext = max(iu1 - iu0, iv1 - iv0) >> kTileShift;
+                        const int l = min(ext ? 32 - __clz(ext) : 0, mip.levels - 1);
+                        const int sh = kTileShift + l, w = mip.w[l];
+                        const float* tl = tiles + mip.off[l];
+                        const int a0 = (iv0 >> sh) * w, a1 = (iv1 >> sh) * w, b0 = iu0 >> sh, b1 = iu1 >> sh;
+                        const float tm = fmaxf(fmaxf(__ldg(tl + a0 + b0), __ldg(tl + a0 + b1)),
+                                               fmaxf(__ldg(tl + a1 + b0), __ldg(tl + a1 + b1)));
+                        live = !(fminf(ca.z, cb.z) > tm + cull_off);
                     }
                 }
-                c = add3(c, step);
             }
-            s_pix[warp][lane][k] = pix;
-            s_cz[warp][lane][k] = czk;
         }
-        // no row of this chunk reaches the image: nothing to update
-        if (!__any_sync(0xffffffffu, any_pix)) continue;
+        const unsigned live_rows = __ballot_sync(0xffffffffu, live);
+        // chain (lane = row): the sequential c-steps of the chunk
+        if (row_on) {
+            if (xc >= x0 && xc + 31 <= x1) {
+                if (live) {
+#pragma unroll 8
+                    for (int k = 0; k < 32; ++k) {
+                        s_c[warp][0][lane][k] = c.x;
+                        s_c[warp][1][lane][k] = c.y;
+                        s_c[warp][2][lane][k] = c.z;
+                        c = add3(c, step);
+                    }
+                } else {
+#pragma unroll 8
+                    for (int k = 0; k < 32; ++k) c = add3(c, step);
+                }
+            } else {
+                for (int k = 0; k < 32; ++k) {
+                    const int x = xc + k;
+                    if (x >= x0 && x <= x1) {
+                        if (live) {
+                            s_c[warp][0][lane][k] = c.x;
+                            s_c[warp][1][lane][k] = c.y;
+                            s_c[warp][2][lane][k] = c.z;
+                        }
+                        c = add3(c, step);
+                    }
+                }
+            }
+        }
+        if (!live_rows) continue;
         __syncwarp();
-        // phase 2 (lane = x): adjacent lanes are adjacent voxels of one row and
-        // project to adjacent pixels, so the depth gathers coalesce; rows go in
-        // batches of 8 so their loads are in flight together.
+        // update (lane = x), live rows in batches of 8 so their loads overlap
         const int x = xc + lane;
+        const bool x_on = x >= x0 && x <= x1;
+        const int tw0 = mip.w[0];
+        unsigned rem = live_rows;
 #pragma unroll 1
-        for (int r0 = 0; r0 < 32; r0 += 8) {
+        while (rem) {
             int rsel[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) rsel[j] = r0 + j;
-            float sdf[8];
-            int pixr[8];
+            for (int j = 0; j < 8; ++j) {
+                rsel[j] = rem ? __ffs(rem) - 1 : -1;
+                rem &= rem - 1;
+            }
+            int pix[8];
+            float cz[8], tm[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                pixr[j] = rsel[j] >= 0 ? s_pix[warp][rsel[j]][lane] : -1;
-                sdf[j] = (pixr[j] >= 0) ? __ldg(depth + pixr[j]) : qnan;
+                pix[j] = -1;
+                cz[j] = 0.0f;
+                tm[j] = 0.0f;
+                if (rsel[j] >= 0 && x_on) {
+                    const F3 cv = mk3(s_c[warp][0][rsel[j]][lane], s_c[warp][1][rsel[j]][lane],
+                                      s_c[warp][2][rsel[j]][lane]);
+                    if (cv.z > 0.0f) {
+                        const float inv_z = __frcp_rn(cv.z);  // == 1.0f / c.z, correctly rounded
+                        const float uf = floorf(fa(fa(fm(fm(fx, cv.x), inv_z), cx), 0.5f));
+                        const float vf = floorf(fa(fa(fm(fm(fy, cv.y), inv_z), cy), 0.5f));
+                        if (uf >= 0.0f && uf < fW && vf >= 0.0f && vf < fH) {
+                            const int ui = static_cast<int>(uf), vi = static_cast<int>(vf);
+                            pix[j] = vi * W + ui;
+                            cz[j] = cv.z;
+                            tm[j] = __ldg(tiles + (vi >> kTileShift) * tw0 + (ui >> kTileShift));
+                        }
+                    }
+                }
+            }
+            float sdf[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                // fs is monotone in the depth: below -trunc for the tile's
+                // deepest in-band depth means no pixel of the tile updates it
+                if (pix[j] >= 0 && fs(tm[j], cz[j]) < -trunc) pix[j] = -1;
+                sdf[j] = pix[j] >= 0 ? __ldg(depth + pix[j]) : 0.0f;
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const float d = sdf[j];
-                sdf[j] = qnan;
-                if (d >= min_d && d <= max_d) {
-                    const float s = fs(d, s_cz[warp][rsel[j]][lane]);
-                    if (!(s < -trunc)) sdf[j] = s;
+                bool ok = false;
+                if (pix[j] >= 0 && d >= min_d && d <= max_d) {
+                    sdf[j] = fs(d, cz[j]);
+                    ok = !(sdf[j] < -trunc);
                 }
+                if (!ok) pix[j] = -1;
             }
             float2 old[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
-                if (sdf[j] == sdf[j]) old[j] = Vox<kHalf>::load_rw(vox, vi);
+                const size_t v = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
+                if (pix[j] >= 0) old[j] = Vox<kHalf>::load_rw(vox, v);
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                if (sdf[j] != sdf[j]) continue;  // NaN: no update
+                if (pix[j] < 0) continue;
                 const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
                 const float tsdf_new = fminf(1.0f, fd(sdf[j], trunc));
                 const float w_old = old[j].y;
@@ -311,12 +483,12 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
                 if (bricks && !(Vox<kHalf>::rounded(t) >= kFreeTsdf)) clear_bricks(bricks, nb, x, ybase + rsel[j], z);
                 if (kColor) {
                     if (rgb != nullptr && fabsf(sdf[j]) < color_band) {
-                        const int pix = pixr[j];
+                        const int p = pix[j];
                         const float inv = fd(1.0f, wp1);
-                        float* cv = color + 3 * vi;
+                        float* cvp = color + 3 * vi;
 #pragma unroll
                         for (int k = 0; k < 3; ++k)
-                            cv[k] = fm(fa(fm(cv[k], w_old), fd(static_cast<float>(rgb[3 * pix + k]), 255.0f)), inv);
+                            cvp[k] = fm(fa(fm(cvp[k], w_old), fd(static_cast<float>(rgb[3 * p + k]), 255.0f)), inv);
                         ++n_col;
                     }
                 }
@@ -600,13 +772,39 @@ int set_pose_async(float* d_pose, const float* pose, cudaStream_t s) {
     return AZU_OK;
 }
 
+// Depth-tile buffer with room for n tiles. Grows outside stream capture only;
+// volumes are created with room for a 640x480 image.
+static int ensure_tiles(azu_volume* v, size_t n, cudaStream_t s) {
+    if (n <= v->tile_cap) return AZU_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    AZU_TRY_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) {
+        set_error("integrate: image larger than the depth-tile buffer during stream capture");
+        return AZU_E_STATE;
+    }
+    AZU_TRY_CUDA(cudaStreamSynchronize(s));
+    if (v->d_tiles) cudaFree(v->d_tiles);
+    v->d_tiles = nullptr;
+    v->tile_cap = 0;
+    AZU_TRY_CUDA(cudaMalloc(&v->d_tiles, n * sizeof(float)));
+    v->tile_cap = n;
+    return AZU_OK;
+}
+
 int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d_rgb, const float* d_pose, float fx,
                          float fy, float cx, float cy, int W, int H, float min_d, float max_d, const int* d_gate,
                          cudaStream_t s) {
     const azu_volume_params& p = v->p;
-    integrate_setup_kernel<<<1, 32, 0, s>>>(d_pose, p.resolution, p.voxel_size, p.origin[0], p.origin[1],
-                                            p.origin[2], p.truncation, fx, fy, cx, cy, W, H, max_d, v->d_iconsts,
-                                            v->d_counters);
+    AZU_CHECK_ARG(W <= kMaxTilePixels && H <= kMaxTilePixels, "image larger than 16384 pixels a side");
+    const TileMip mip = make_tile_mip(W, H);
+    if (int rc = ensure_tiles(v, static_cast<size_t>(mip.total), s)) return rc;
+    const int nt0 = mip.w[0] * mip.h[0];
+    depth_tiles_kernel<<<(nt0 + 31) / 32, 256, 0, s>>>(d_depth_m, W, H, min_d, max_d, mip.w[0], nt0, v->d_tiles,
+                                                        d_gate);
+    AZU_LAUNCH_CHECK();
+    integrate_setup_kernel<<<1, 256, 0, s>>>(d_pose, p.resolution, p.voxel_size, p.origin[0], p.origin[1],
+                                             p.origin[2], p.truncation, fx, fy, cx, cy, W, H, max_d, v->d_iconsts,
+                                             v->d_counters, v->d_tiles, mip);
     AZU_LAUNCH_CHECK();
     const int ngroups = (p.resolution + 31) / 32;
     const long items = static_cast<long>(p.resolution) * ngroups;
@@ -616,7 +814,7 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
 #define AZU_INT_ARGS                                                                                             \
     v->vox, v->color, v->d_iconsts, d_depth_m, d_rgb, p.resolution, p.voxel_size, p.origin[0], p.origin[1],     \
         p.origin[2], p.truncation, p.max_weight, fx, fy, cx, cy, W, H, min_d, max_d, d_gate, v->d_counters,   \
-        v->bricks, v->nb
+        v->bricks, v->nb, v->d_tiles, mip
     if (!half && !col) integrate_kernel<false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (!half && col) integrate_kernel<false, true><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (half && !col) integrate_kernel<true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
@@ -654,6 +852,11 @@ static int volume_alloc(azu_volume* v) {
     if (v->p.color) AZU_TRY_CUDA(cudaMalloc(&v->color, n * 3 * sizeof(float)));
     v->nb = (v->p.resolution + 7) >> kBrickShift;
     AZU_TRY_CUDA(cudaMalloc(&v->bricks, static_cast<size_t>(v->nb) * v->nb * v->nb));
+    if (!v->d_tiles) {
+        const size_t n = static_cast<size_t>(make_tile_mip(640, 480).total);
+        AZU_TRY_CUDA(cudaMalloc(&v->d_tiles, n * sizeof(float)));
+        v->tile_cap = n;
+    }
     return AZU_OK;
 }
 static void volume_free_storage(azu_volume* v) {
@@ -732,6 +935,7 @@ extern "C" int azu_volume_destroy(azu_volume* v) {
     if (v->d_counters) cudaFree(v->d_counters);
     if (v->d_depth_stage) cudaFree(v->d_depth_stage);
     if (v->d_rgb_stage) cudaFree(v->d_rgb_stage);
+    if (v->d_tiles) cudaFree(v->d_tiles);
     v->stream.release();
     delete v;
     return AZU_OK;
