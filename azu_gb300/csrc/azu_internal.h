@@ -103,6 +103,10 @@ struct azu_volume {
     // on reset and rebuilt from the volume after an upload; integration only
     // clears flags.
     uint8_t* bricks = nullptr;
+    // Capped Chebyshev distance of every brick to the nearest brick that is
+    // not free, recomputed from the flags before each raycast.
+    uint8_t* brick_dist = nullptr;
+    uint8_t* brick_tmp = nullptr;
     int nb = 0;
     bool skip_free = true;
     // Deepest in-band depth per 8x8 pixel tile of the frame being integrated.

@@ -560,20 +560,80 @@ __device__ __forceinline__ bool sample_tsdf(const VolView& v, F3 p, float& f) {
     return true;
 }
 
-// True when the sample at p lies in a free brick, or outside the samplable box
-// (then it is invalid). Same base-voxel arithmetic as sample_tsdf, so the 8
-// corners of the sample are inside the brick's apron.
-// Returns 0 (not free), 1 (inside free brick (bx, by, bz)) or 2 (outside the box).
-__device__ __forceinline__ int in_free_brick(const VolView& v, const uint8_t* __restrict__ bricks, int nb, F3 p,
-                                             int& bx, int& by, int& bz) {
+// State of the brick holding the sample at p: -1 outside the samplable box
+// (the sample is invalid), else the brick's free distance: 0 for a brick that
+// is not free, d >= 1 when every brick within Chebyshev distance d - 1 is free.
+// Same base-voxel arithmetic as sample_tsdf, so the 8 corners of the sample
+// are inside the brick's apron.
+__device__ __forceinline__ int brick_state(const VolView& v, const uint8_t* __restrict__ dist, int nb, F3 p, int& bx,
+                                           int& by, int& bz) {
     const F3 q = to_voxel(v, p);
     const float fx0 = floorf(q.x), fy0 = floorf(q.y), fz0 = floorf(q.z);
     const float lim = static_cast<float>(v.res - 1);
-    if (!(fx0 >= 0.0f && fy0 >= 0.0f && fz0 >= 0.0f && fx0 < lim && fy0 < lim && fz0 < lim)) return 2;
+    if (!(fx0 >= 0.0f && fy0 >= 0.0f && fz0 >= 0.0f && fx0 < lim && fy0 < lim && fz0 < lim)) return -1;
     bx = static_cast<int>(fx0) >> kBrickShift;
     by = static_cast<int>(fy0) >> kBrickShift;
     bz = static_cast<int>(fz0) >> kBrickShift;
-    return __ldg(bricks + (static_cast<size_t>(bz) * nb + by) * nb + bx) != 0 ? 1 : 0;
+    return __ldg(dist + (static_cast<size_t>(bz) * nb + by) * nb + bx);
+}
+
+// One pass of the capped Chebyshev distance transform of the free flags:
+// out(b) = min over |k| <= kDistCap of max(|k|, in(b + k e_axis)), with
+// in = 0 for a brick that is not free and kDistCap for a free one (the first
+// pass reads the flags) and kDistCap outside the grid. Three passes (x, y, z)
+// give the distance to the nearest non-free brick, capped.
+constexpr int kDistCap = 12;
+__global__ void brick_dist_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, int nb, int axis,
+                                  int from_flags, const int* __restrict__ gate) {
+    if (gate && __ldg(gate) == 0) return;
+    const size_t n = static_cast<size_t>(nb) * nb * nb;
+    const size_t b = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const int c[3] = {static_cast<int>(b % nb), static_cast<int>((b / nb) % nb), static_cast<int>(b / nb / nb)};
+    const size_t stride = axis == 0 ? 1 : (axis == 1 ? static_cast<size_t>(nb) : static_cast<size_t>(nb) * nb);
+    const int pos = c[axis];
+    int d = kDistCap;
+    for (int k = -kDistCap + 1; k < kDistCap; ++k) {
+        const int q = pos + k;
+        if (q < 0 || q >= nb) continue;
+        const uint8_t raw = __ldg(in + b + static_cast<ptrdiff_t>(k) * static_cast<ptrdiff_t>(stride));
+        const int val = from_flags ? (raw ? kDistCap : 0) : raw;
+        d = min(d, max(abs(k), val));
+    }
+    out[b] = static_cast<uint8_t>(d);
+}
+
+// Fast-forward through free space. From a sample t whose brick b has free
+// distance r + 1, every brick of the cube b +- r is free, and the march takes
+// far steps t_k = t + k step (each sum rounded) whose samples in the cube are
+// all skipped anyway. While the sums stay in t's binade [2^e, 2^(e+1)) and
+// step is not a rounding tie there, each one adds the same delta =
+// RN(t + step) - t exactly, so t_m = t + m delta in one exact fma. m stops one
+// step short of the cube's exit (its box shrunk by 4e-3 voxel, far above the
+// rounding of positions), of t_far and of the binade's end. Returns t when no
+// step can be taken this way.
+__device__ __forceinline__ float free_space_jump(const VolView& v, F3 co, F3 inv_dir, float t, float step,
+                                                 float t_far, int bx, int by, int bz, int r) {
+    const float span = 8.0f * v.vs, mg = 4e-3f * v.vs;
+    const int b[3] = {bx, by, bz};
+    float t_exit = t_far;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float ia = comp(inv_dir, a);
+        if (!(fabsf(ia) < __int_as_float(0x7f800000))) continue;  // ray parallel to this axis
+        const float face = ia > 0.0f ? comp(v.origin, a) + span * static_cast<float>(b[a] + r + 1) - mg
+                                     : comp(v.origin, a) + span * static_cast<float>(b[a] - r) + mg;
+        t_exit = fminf(t_exit, (face - comp(co, a)) * ia);
+    }
+    const float top = __int_as_float((__float_as_int(t) & 0x7f800000) + 0x00800000);  // 2^(e+1)
+    const float u = top * 5.9604645e-8f;                                              // ulp of the binade
+    const float t1 = fa(t, step);
+    const float delta = fs(t1, t);
+    if (!(t1 < top) || fabsf(fs(step, delta)) == 0.5f * u) return t;
+    const float lim = fminf(fminf(t_exit, t_far) - t, fs(fs(top, u), t));
+    const float m = floorf(lim / delta) - 1.0f;
+    if (!(m >= 1.0f)) return t;
+    return fmaf(m, delta, t);
 }
 
 // Exact free flags from the volume (after an upload).
@@ -619,7 +679,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
                                                      float fy, float cx, float cy, int W, int H, float trunc,
                                                      float min_depth, float max_depth, float* __restrict__ vout,
                                                      float* __restrict__ nout, uint8_t* __restrict__ cout,
-                                                     const int* __restrict__ gate, const uint8_t* __restrict__ bricks,
+                                                     const int* __restrict__ gate, const uint8_t* __restrict__ bdist,
                                                      int nb) {
     if (gate && __ldg(gate) == 0) return;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -648,10 +708,12 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
         const F3 dir = div3(mv3(R, ray), ray_norm);
         float t_near = fm(min_depth, ray_norm);
         float t_far = fm(max_depth, ray_norm);
+        float inv_dir[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const float da = comp(dir, a), oa = comp(co, a), la = comp(box_lo, a), ha = comp(box_hi, a);
             const float inv = fd(1.0f, da);
+            inv_dir[a] = inv;
             float t0 = fm(fs(la, oa), inv);
             float t1 = fm(fs(ha, oa), inv);
             if (t0 > t1) { const float tmp = t0; t0 = t1; t1 = tmp; }
@@ -688,11 +750,14 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
             if (!(t > t_prev)) break;  // no progress (degenerate parameters): stop without a hit
             const F3 p = add3(co, mul3(dir, t));
             int bx = 0, by = 0, bz = 0;
-            const int fb = (bricks && (skipped || !prev_valid || f_prev >= 0.0f)) ? in_free_brick(v, bricks, nb, p, bx, by, bz) : 0;
+            const int fb = (bdist && (skipped || !prev_valid || f_prev >= 0.0f)) ? brick_state(v, bdist, nb, p, bx, by, bz) : 0;
             if (fb) {
                 t_prev = t;
                 skipped = true;
                 if (t >= t_far) break;
+                if (fb >= 2)
+                    t_prev = free_space_jump(v, co, mk3(inv_dir[0], inv_dir[1], inv_dir[2]), t, far_step, t_far, bx,
+                                             by, bz, fb - 1);
                 continue;
             }
             if (skipped) {
@@ -833,7 +898,16 @@ int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, f
     const float inv_vs = (mant == 0.5f && e2 > -120 && e2 < 120) ? std::ldexp(1.0f, 1 - e2) : 0.0f;
     VolView view{v->vox, v->color, p.resolution, p.voxel_size, mk3(p.origin[0], p.origin[1], p.origin[2]), inv_vs};
     const dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
-    const uint8_t* bricks = v->skip_free ? v->bricks : nullptr;
+    const uint8_t* bricks = nullptr;
+    if (v->skip_free) {
+        const size_t nbr = static_cast<size_t>(v->nb) * v->nb * v->nb;
+        const unsigned g = static_cast<unsigned>((nbr + 255) / 256);
+        brick_dist_kernel<<<g, 256, 0, s>>>(v->bricks, v->brick_dist, v->nb, 0, 1, d_gate);
+        brick_dist_kernel<<<g, 256, 0, s>>>(v->brick_dist, v->brick_tmp, v->nb, 1, 0, d_gate);
+        brick_dist_kernel<<<g, 256, 0, s>>>(v->brick_tmp, v->brick_dist, v->nb, 2, 0, d_gate);
+        AZU_LAUNCH_CHECK();
+        bricks = v->brick_dist;
+    }
     if (p.format == AZU_TSDF_FP16)
         raycast_kernel<true><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
                                                   p.max_depth, d_vertices, d_normals, d_colors, d_gate, bricks,
@@ -852,6 +926,8 @@ static int volume_alloc(azu_volume* v) {
     if (v->p.color) AZU_TRY_CUDA(cudaMalloc(&v->color, n * 3 * sizeof(float)));
     v->nb = (v->p.resolution + 7) >> kBrickShift;
     AZU_TRY_CUDA(cudaMalloc(&v->bricks, static_cast<size_t>(v->nb) * v->nb * v->nb));
+    AZU_TRY_CUDA(cudaMalloc(&v->brick_dist, static_cast<size_t>(v->nb) * v->nb * v->nb));
+    AZU_TRY_CUDA(cudaMalloc(&v->brick_tmp, static_cast<size_t>(v->nb) * v->nb * v->nb));
     if (!v->d_tiles) {
         const size_t n = static_cast<size_t>(make_tile_mip(640, 480).total);
         AZU_TRY_CUDA(cudaMalloc(&v->d_tiles, n * sizeof(float)));
@@ -863,6 +939,10 @@ static void volume_free_storage(azu_volume* v) {
     if (v->vox) cudaFree(v->vox);
     if (v->color) cudaFree(v->color);
     if (v->bricks) cudaFree(v->bricks);
+    if (v->brick_dist) cudaFree(v->brick_dist);
+    if (v->brick_tmp) cudaFree(v->brick_tmp);
+    v->brick_dist = nullptr;
+    v->brick_tmp = nullptr;
     v->vox = nullptr;
     v->color = nullptr;
     v->bricks = nullptr;

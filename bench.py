@@ -39,7 +39,7 @@ METRIC = "frames/s @512³ TSDF, 640×480 (FP32 vs FP16-TSDF form, CPU ref); inte
 SEQ_FRAMES = 300
 MESH_EVERY = 30
 W, H = 640, 480
-KERNELS_PER_FRAME_RAW = 16  # 7 preprocess + 2 frame + predict + ICP + 3 integrate + raycast + commit
+KERNELS_PER_FRAME_RAW = 19  # 7 preprocess + 2 frame + predict + ICP + 3 integrate + 3 brick distance + raycast + commit
 D2H_RESULT_BYTES = 336 + 264  # device pose state + azu_icp_result read back per frame
 
 
