@@ -18,6 +18,7 @@ AZU_E_STATE = -6
 
 AZU_TSDF_FP32 = 0
 AZU_TSDF_FP16 = 1
+AZU_TSDF_FP16R = 2
 AZU_PRE_FULL = 0
 AZU_PRE_MINIMAL = 1
 

@@ -21,6 +21,8 @@
 #include <algorithm>
 #include <cstring>
 
+#include <cuda_fp16.h>
+
 #include "azu_internal.h"
 #include "kf_math.cuh"
 #include "mc_tables.h"
@@ -38,7 +40,8 @@ __constant__ int c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}
                                   {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
 
 struct MeshVol {
-    const float2* vox;
+    const void* vox;
+    int half;  // FP16 formats: half tsdf in the low 16 bits, weight word (> 0 iff observed) above
     const float* color;
     int res;
     float vs;
@@ -49,7 +52,14 @@ struct MeshVol {
     }
     // sampleCorner (:81-85)
     __device__ __forceinline__ bool corner(int x, int y, int z, float& v) const {
-        const float2 r = __ldg(vox + idx(x, y, z));
+        float2 r;
+        if (half) {
+            const uint32_t u = __ldg(static_cast<const uint32_t*>(vox) + idx(x, y, z));
+            r = make_float2(__half2float(__ushort_as_half(static_cast<unsigned short>(u & 0xFFFFu))),
+                            static_cast<float>(u >> 16));
+        } else {
+            r = __ldg(static_cast<const float2*>(vox) + idx(x, y, z));
+        }
         if (!isfinite(r.x) || r.y <= kWeightEps) { v = kEmptyTsdf; return false; }
         v = r.x;
         return true;
@@ -508,10 +518,6 @@ extern "C" int azu_mesher_set_max_triangles(azu_mesher* m, int64_t n) {
 
 extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* info) {
     AZU_CHECK_ARG(m != nullptr && v != nullptr && info != nullptr, "null argument");
-    if (v->p.format != AZU_TSDF_FP32) {
-        set_error("marching cubes reads FP32 volumes (the FP16 form meshes after conversion)");
-        return AZU_E_UNSUPPORTED;
-    }
     AZU_TRY_CUDA(cudaSetDevice(m->device));
     cudaStream_t s = m->stream.s;
     // The volume may be written on its own stream: order after it.
@@ -521,7 +527,7 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     const int res = v->p.resolution;
     const long long cr = res - 1;
     const long long ncubes = cr * cr * cr;
-    MeshVol mv{static_cast<const float2*>(v->vox), v->color, res, v->p.voxel_size,
+    MeshVol mv{v->vox, v->p.format != AZU_TSDF_FP32 ? 1 : 0, v->color, res, v->p.voxel_size,
                mk3(v->p.origin[0], v->p.origin[1], v->p.origin[2])};
     const size_t nblocks = static_cast<size_t>((ncubes + kCubeBlock - 1) / kCubeBlock);
     if (int rc = grow(m->counts, m->counts_cap, static_cast<size_t>(ncubes))) return rc;

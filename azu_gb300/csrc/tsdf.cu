@@ -29,7 +29,7 @@ constexpr float kEmptyColor = 128.0f / 255.0f;
 constexpr float kFreeTsdf = 0.9995f;
 constexpr int kBrickShift = 3;  // 8^3-voxel bricks
 
-size_t voxel_bytes(int format) { return format == AZU_TSDF_FP16 ? 4 : 8; }
+size_t voxel_bytes(int format) { return format == AZU_TSDF_FP32 ? 8 : 4; }
 
 // Clears the free flag of every brick whose apron [8b, 8b+8] holds voxel (x, y, z).
 __device__ __forceinline__ void clear_bricks(uint8_t* bricks, int nb, int x, int y, int z) {
@@ -79,6 +79,36 @@ struct Vox<true> {
         static_cast<uint32_t*>(v)[i] = h | (static_cast<uint32_t>(w) << 16);
     }
     __device__ static __forceinline__ float rounded(float t) { return __half2float(__float2half_rn(t)); }
+};
+
+// FP16 tsdf with a sub-half residual (AZU_TSDF_FP16R). Word: bits 0-15 the
+// half h = RN(t); bits 16-31 the weight (7 bits) << 9 | q, q a 9-bit two's
+// complement in units s = ulp(h) / 512, |q| <= 255. The fold reads
+// t' = h + q s (exact in float: at most 21 significant bits), so repeated
+// updates do not stall at half precision; readers use h.
+struct VoxR {
+    // s = ulp(h) / 512 from the half's exponent field (subnormals: 2^-24 / 512)
+    __device__ static __forceinline__ float unit(uint32_t hbits) {
+        const int e = static_cast<int>((hbits >> 10) & 0x1fu);
+        return __int_as_float((e == 0 ? 94 : e + 93) << 23);
+    }
+    __device__ static __forceinline__ float2 load_fold(const void* v, size_t i) {
+        const uint32_t u = static_cast<const uint32_t*>(v)[i];
+        const uint32_t hi = u >> 16;
+        const int q = static_cast<int>((hi & 0x1ffu) ^ 0x100u) - 0x100;
+        const float h = __half2float(__ushort_as_half(static_cast<unsigned short>(u & 0xFFFFu)));
+        return make_float2(fmaf(static_cast<float>(q), unit(u & 0xFFFFu), h), static_cast<float>(hi >> 9));
+    }
+    __device__ static __forceinline__ void store(void* v, size_t i, float t, float w) {
+        const unsigned short hb = __half_as_ushort(__float2half_rn(t));
+        const float h = __half2float(__ushort_as_half(hb));
+        const float s = unit(hb);
+        // t - h is exact; dividing by the power of two s is exact
+        int q = __float2int_rn(fs(t, h) / s);
+        q = max(-255, min(255, q));
+        const uint32_t hi = (static_cast<uint32_t>(w) << 9) | (static_cast<uint32_t>(q) & 0x1ffu);
+        static_cast<uint32_t*>(v)[i] = static_cast<uint32_t>(hb) | (hi << 16);
+    }
 };
 
 // ---- small kernels -------------------------------------------------------
@@ -261,7 +291,7 @@ __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res
 // Every test is exact or conservative, so the updated set and the values are
 // the CPU's. Voxels that take no update are never read: HBM traffic is
 // 2 x record size per updated voxel.
-template <bool kHalf, bool kColor>
+template <bool kHalf, bool kColor, bool kResid>
 __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     void* __restrict__ vox, float* __restrict__ color, const IntegrateConsts* __restrict__ icp,
     const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
@@ -466,7 +496,7 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const size_t v = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
-                if (pix[j] >= 0) old[j] = Vox<kHalf>::load_rw(vox, v);
+                if (pix[j] >= 0) old[j] = kResid ? VoxR::load_fold(vox, v) : Vox<kHalf>::load_rw(vox, v);
             }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -479,7 +509,8 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
                 const float wp1 = fa(w_old, 1.0f);
                 const float t = fd(fa(fm(old[j].x, w_old), tsdf_new), wp1);
                 const float w = fminf(wp1, max_w);
-                Vox<kHalf>::store(vox, vi, t, w);
+                if (kResid) VoxR::store(vox, vi, t, w);
+                else Vox<kHalf>::store(vox, vi, t, w);
                 if (bricks && !(Vox<kHalf>::rounded(t) >= kFreeTsdf)) clear_bricks(bricks, nb, x, ybase + rsel[j], z);
                 if (kColor) {
                     if (rgb != nullptr && fabsf(sdf[j]) < color_band) {
@@ -814,19 +845,20 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
 }
 
 // ---- whole-volume transfers -------------------------------------------------
-template <bool kHalf>
+template <bool kHalf, bool kResid>
 __global__ void unpack_kernel(const void* vox, size_t base, size_t n, float* t, float* w) {
     const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float2 r = Vox<kHalf>::load_rw(vox, base + i);
+    const float2 r = kResid ? VoxR::load_fold(vox, base + i) : Vox<kHalf>::load_rw(vox, base + i);
     t[i] = r.x;
     w[i] = r.y;
 }
-template <bool kHalf>
+template <bool kHalf, bool kResid>
 __global__ void pack_kernel(void* vox, size_t base, size_t n, const float* t, const float* w) {
     const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    Vox<kHalf>::store(vox, base + i, t[i], w[i]);
+    if (kResid) VoxR::store(vox, base + i, t[i], w[i]);
+    else Vox<kHalf>::store(vox, base + i, t[i], w[i]);
 }
 
 int set_pose_async(float* d_pose, const float* pose, cudaStream_t s) {
@@ -874,16 +906,19 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
     const int ngroups = (p.resolution + 31) / 32;
     const long items = static_cast<long>(p.resolution) * ngroups;
     const int blocks = static_cast<int>((items + kIntWarps - 1) / kIntWarps);
-    const bool half = p.format == AZU_TSDF_FP16;
+    const bool half = p.format != AZU_TSDF_FP32;
+    const bool resid = p.format == AZU_TSDF_FP16R;
     const bool col = v->color != nullptr;
 #define AZU_INT_ARGS                                                                                             \
     v->vox, v->color, v->d_iconsts, d_depth_m, d_rgb, p.resolution, p.voxel_size, p.origin[0], p.origin[1],     \
         p.origin[2], p.truncation, p.max_weight, fx, fy, cx, cy, W, H, min_d, max_d, d_gate, v->d_counters,   \
         v->bricks, v->nb, v->d_tiles, mip
-    if (!half && !col) integrate_kernel<false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
-    else if (!half && col) integrate_kernel<false, true><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
-    else if (half && !col) integrate_kernel<true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
-    else integrate_kernel<true, true><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    if (!half && !col) integrate_kernel<false, false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    else if (!half && col) integrate_kernel<false, true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    else if (!resid && !col) integrate_kernel<true, false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    else if (!resid && col) integrate_kernel<true, true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    else if (!col) integrate_kernel<true, false, true><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
+    else integrate_kernel<true, true, true><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
 #undef AZU_INT_ARGS
     AZU_LAUNCH_CHECK();
     return AZU_OK;
@@ -908,7 +943,7 @@ int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, f
         AZU_LAUNCH_CHECK();
         bricks = v->brick_dist;
     }
-    if (p.format == AZU_TSDF_FP16)
+    if (p.format != AZU_TSDF_FP32)
         raycast_kernel<true><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
                                                   p.max_depth, d_vertices, d_normals, d_colors, d_gate, bricks,
                                                   v->nb);
@@ -950,7 +985,7 @@ static void volume_free_storage(azu_volume* v) {
 int rebuild_bricks(azu_volume* v, cudaStream_t s) {
     const size_t nbr = static_cast<size_t>(v->nb) * v->nb * v->nb;
     const unsigned g = static_cast<unsigned>((nbr + 127) / 128);
-    if (v->p.format == AZU_TSDF_FP16) rebuild_bricks_kernel<true><<<g, 128, 0, s>>>(v->vox, v->p.resolution, v->bricks, v->nb);
+    if (v->p.format != AZU_TSDF_FP32) rebuild_bricks_kernel<true><<<g, 128, 0, s>>>(v->vox, v->p.resolution, v->bricks, v->nb);
     else rebuild_bricks_kernel<false><<<g, 128, 0, s>>>(v->vox, v->p.resolution, v->bricks, v->nb);
     AZU_LAUNCH_CHECK();
     return AZU_OK;
@@ -961,7 +996,8 @@ static int check_params(const azu_volume_params* p) {
     AZU_CHECK_ARG(p->voxel_size > 0.0f && std::isfinite(p->voxel_size), "voxel_size must be > 0");
     AZU_CHECK_ARG(p->truncation > 0.0f && std::isfinite(p->truncation), "truncation must be > 0");
     AZU_CHECK_ARG(p->max_weight >= 1.0f && p->max_weight <= 65535.0f, "max_weight must be in [1, 65535]");
-    AZU_CHECK_ARG(p->format == AZU_TSDF_FP32 || p->format == AZU_TSDF_FP16, "format");
+    AZU_CHECK_ARG(p->format == AZU_TSDF_FP32 || p->format == AZU_TSDF_FP16 || p->format == AZU_TSDF_FP16R, "format");
+    AZU_CHECK_ARG(p->format != AZU_TSDF_FP16R || p->max_weight <= 127.0f, "AZU_TSDF_FP16R needs max_weight <= 127");
     return AZU_OK;
 }
 
@@ -974,7 +1010,7 @@ extern "C" int azu_volume_reset(azu_volume* v) {
     AZU_TRY_CUDA(cudaSetDevice(v->device));
     const size_t n = static_cast<size_t>(v->p.resolution) * v->p.resolution * v->p.resolution;
     const int blocks = static_cast<int>(std::min<size_t>((n + 255) / 256, 152 * 32));
-    if (v->p.format == AZU_TSDF_FP16) reset_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
+    if (v->p.format != AZU_TSDF_FP32) reset_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
     else reset_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
     AZU_LAUNCH_CHECK();
     AZU_TRY_CUDA(cudaMemsetAsync(v->d_counters, 0, 4 * sizeof(unsigned long long), v->stream.s));
@@ -1118,13 +1154,14 @@ static int transfer(azu_volume* v, float* ht, float* hw, float* hc, const float*
     AZU_TRY_CUDA(cudaStreamSynchronize(v->stream.s));
     cudaError_t e = cudaMalloc(&dt, chunk * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&dw, chunk * sizeof(float));
-    const bool half = v->p.format == AZU_TSDF_FP16;
+    const int fmt = v->p.format;
     for (size_t base = 0; e == cudaSuccess && base < n; base += chunk) {
         const size_t m = std::min(chunk, n - base);
         const int blocks = static_cast<int>((m + 255) / 256);
         if (download) {
-            if (half) unpack_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
-            else unpack_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+            if (fmt == AZU_TSDF_FP16R) unpack_kernel<true, true><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+            else if (fmt == AZU_TSDF_FP16) unpack_kernel<true, false><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+            else unpack_kernel<false, false><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
             e = cudaGetLastError();
             if (e == cudaSuccess && ht) e = cudaMemcpyAsync(ht + base, dt, m * sizeof(float), cudaMemcpyDeviceToHost, v->stream.s);
             if (e == cudaSuccess && hw) e = cudaMemcpyAsync(hw + base, dw, m * sizeof(float), cudaMemcpyDeviceToHost, v->stream.s);
@@ -1132,8 +1169,9 @@ static int transfer(azu_volume* v, float* ht, float* hw, float* hc, const float*
             e = cudaMemcpyAsync(dt, ut + base, m * sizeof(float), cudaMemcpyHostToDevice, v->stream.s);
             if (e == cudaSuccess) e = cudaMemcpyAsync(dw, uw + base, m * sizeof(float), cudaMemcpyHostToDevice, v->stream.s);
             if (e == cudaSuccess) {
-                if (half) pack_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
-                else pack_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+                if (fmt == AZU_TSDF_FP16R) pack_kernel<true, true><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+                else if (fmt == AZU_TSDF_FP16) pack_kernel<true, false><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
+                else pack_kernel<false, false><<<blocks, 256, 0, v->stream.s>>>(v->vox, base, m, dt, dw);
                 e = cudaGetLastError();
             }
         }

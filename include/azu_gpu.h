@@ -58,7 +58,7 @@ int azu_select_device(size_t min_free_bytes, int* device);
 
 typedef struct azu_volume azu_volume;
 
-enum { AZU_TSDF_FP32 = 0, AZU_TSDF_FP16 = 1 };
+enum { AZU_TSDF_FP32 = 0, AZU_TSDF_FP16 = 1, AZU_TSDF_FP16R = 2 };
 
 typedef struct {
     int   resolution;   /* voxels per axis (TSDFParams::resolution) */
@@ -69,7 +69,13 @@ typedef struct {
     float min_depth;    /* raycast band, camera Z-depth (TSDFParams::min_depth) */
     float max_depth;    /* TSDFParams::max_depth */
     int   format;       /* AZU_TSDF_FP32: float tsdf + float weight (8 B/voxel);
-                           AZU_TSDF_FP16: half tsdf + uint16 weight (4 B/voxel) */
+                           AZU_TSDF_FP16: half tsdf + uint16 weight (4 B/voxel);
+                           AZU_TSDF_FP16R: half tsdf + a 16-bit word holding the
+                             weight (7 bits, max_weight <= 127) and a 9-bit residual
+                             of the tsdf below half precision, which only the
+                             integration fold reads (4 B/voxel). Readers (raycast,
+                             marching cubes) see the half tsdf in both FP16 formats;
+                             download returns the half tsdf plus residual. */
     int   color;        /* nonzero: keep float sRGB colour per voxel (12 B/voxel) */
 } azu_volume_params;
 

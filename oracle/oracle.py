@@ -388,12 +388,13 @@ class Lockstep:
 
 
 class PrecisionVolume(Volume):
-    """FP16-storage emulation (half_storage=True) or FP32, plus the FP64 running
-    average of the same updates in `tsdf64`."""
+    """FP16-storage emulation (half_storage 1: half RN; 2: half plus the 9-bit
+    residual of the FP16R format; 0/False: FP32), plus the FP64 running average
+    of the same updates in `tsdf64`."""
 
-    def __init__(self, p: TsdfParams, half_storage: bool, fp64: bool = True):
+    def __init__(self, p: TsdfParams, half_storage, fp64: bool = True):
         super().__init__(p)
-        self.half = bool(half_storage)
+        self.half = int(half_storage)
         self.tsdf64 = np.ones(p.res ** 3, np.float64) if fp64 else None
 
     def integrate(self, depth_m, pose, K, W, H, min_depth, max_depth, rgb=None):

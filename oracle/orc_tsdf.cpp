@@ -300,10 +300,26 @@ extern "C" int orc_get_threads(void) {
 #endif
 }
 
+// FP16 tsdf plus a 9-bit residual below half precision (the FP16R volume
+// format; no reference counterpart): h = RN_half(t), q = RN((t - h) / s) with
+// s = ulp(h) / 512, |q| <= 255; the stored value is h + q s (exact in float).
+static float fp16r_roundtrip(float t) {
+    const _Float16 hh = static_cast<_Float16>(t);
+    const float h = static_cast<float>(hh);
+    uint16_t hb;
+    std::memcpy(&hb, &hh, sizeof(hb));
+    const int e = (hb >> 10) & 0x1f;
+    const float s = std::ldexp(1.0f, (e == 0 ? 94 : e + 93) - 127);
+    int q = static_cast<int>(std::nearbyint((t - h) / s));
+    q = std::max(-255, std::min(255, q));
+    return std::fma(static_cast<float>(q), s, h);
+}
+
 // Precision form of the same integration: identical projections and decisions
 // (float camera stepping), with
-//   half_storage != 0: the tsdf stored rounded to IEEE half (round to nearest
+//   half_storage == 1: the tsdf stored rounded to IEEE half (round to nearest
 //                      even) after every update, i.e. the FP16 + u16 volume;
+//   half_storage == 2: the tsdf stored as half plus residual (fp16r_roundtrip);
 //   tsdf64 != NULL:    the running average of the same float tsdf_new values
 //                      carried in double (the FP64 reference).
 extern "C" void orc_tsdf_integrate_prec(const orc_tsdf_params* p, float* tsdf, float* weight, double* tsdf64,
@@ -356,7 +372,8 @@ extern "C" void orc_tsdf_integrate_prec(const orc_tsdf_params* p, float* tsdf, f
                 const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(y)) * rr + static_cast<size_t>(x);
                 const float w_old = weight[vi];
                 const float t = (tsdf[vi] * w_old + tsdf_new) / (w_old + 1.0f);
-                tsdf[vi] = half_storage ? static_cast<float>(static_cast<_Float16>(t)) : t;
+                tsdf[vi] = half_storage == 2 ? fp16r_roundtrip(t)
+                           : half_storage ? static_cast<float>(static_cast<_Float16>(t)) : t;
                 if (tsdf64)
                     tsdf64[vi] = (tsdf64[vi] * static_cast<double>(w_old) + static_cast<double>(tsdf_new)) /
                                  (static_cast<double>(w_old) + 1.0);
