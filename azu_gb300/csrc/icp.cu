@@ -12,7 +12,10 @@
 //      partials in one fixed order, solves the damped 6x6 system and publishes
 //      the outcome; the others wait (bounded spin; a timeout sets an error
 //      word) and read it.
-// Partials are double-buffered by iteration parity.
+// Partials are double-buffered by iteration parity. The precision form
+// (precision = 1) keeps the per-pixel terms in FP32 with compensated block
+// sums and uses FP64 only for the cross-block sum, the Cholesky solve, the
+// SE(3) exponential, the pose composition and the rotation projection.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -63,7 +66,7 @@ struct IcpArgs {
     azu_icp_result* d_result;
     int* d_quality;
     int* d_gate;          // set to 1 when the frame grades Good
-    double* partials;     // [2][kNF][nblocks], double or float (precision form or not)
+    double* partials;     // [2][kNF][nblocks]: double in the precision form, else float
     int* ipartials;       // [2][kNI][nblocks]
     unsigned* bar;        // [0] arrivals, [1] generation
     unsigned* err;
@@ -276,13 +279,12 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// Block reduction of one pass into global partial slot `slot`, in the
-// accumulation type T: float, or double for the precision form (the float
-// path issues no FP64 instruction; GB300's FP64 rate is a small fraction of
-// its FP32 rate). The six counters travel as T: every per-block count is
-// below 2^24, so exact. Partials are stored value-major, [slot][value][block],
-// so the grid reduction reads them coalesced; the partial buffers and the
-// shared staging are sized for double and reinterpreted for float.
+// Block reduction of one pass into global partial slot `slot` (FP32 path; no
+// FP64 instruction — GB300's FP64 rate is a small fraction of its FP32 rate).
+// The six counters travel as T: every per-block count is below 2^24, so exact.
+// Partials are stored value-major, [slot][value][block], so the grid reduction
+// reads them coalesced; the partial buffers and the shared staging are sized
+// for double and reinterpreted for float.
 template <typename T>
 __device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc, int slot, double* s_red_raw) {
     constexpr int kNV = kNF + kNI;  // 34
@@ -316,8 +318,56 @@ __device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc,
     __syncthreads();
 }
 
+// Error-free sum: s + e == a + b exactly (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Precision form: the per-pixel terms and the warp sums stay FP32 (the same
+// recursive halving as the plain path); the sum over the block's warps is
+// compensated (each value carries the exact error of its additions), and the
+// block partial enters the FP64 cross-block sum as (double) s + (double) c.
+__device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, double* s_red_raw) {
+    constexpr int kNV = kNF + kNI;
+    float* s_red = reinterpret_cast<float*>(s_red_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    float v[32];
+#pragma unroll
+    for (int k = 0; k < kNF; ++k) v[k] = acc.f[k];
+#pragma unroll
+    for (int k = kNF; k < 32; ++k) v[k] = static_cast<float>(acc.i[k - kNF]);
+    const float e0 = warp_sum(static_cast<float>(acc.i[32 - kNF]));
+    const float e1 = warp_sum(static_cast<float>(acc.i[33 - kNF]));
+    const float mine = warp_sum_transpose32(v, lane);
+    s_red[warp * kNV + lane] = mine;
+    if (lane == 0) {
+        s_red[warp * kNV + 32] = e0;
+        s_red[warp * kNV + 33] = e1;
+    }
+    __syncthreads();
+    const int k = threadIdx.x, nb = gridDim.x;
+    if (k < kNV) {
+        float sum = 0.0f, c = 0.0f;
+        for (int w = 0; w < nw; ++w) {
+            float sn, err;
+            two_sum(sum, s_red[w * kNV + k], sn, err);
+            sum = sn;
+            c = __fadd_rn(c, err);
+        }
+        if (k < kNF)
+            a.partials[(static_cast<size_t>(slot) * kNF + k) * nb + blockIdx.x] =
+                static_cast<double>(sum) + static_cast<double>(c);
+        else
+            a.ipartials[(static_cast<size_t>(slot) * kNI + (k - kNF)) * nb + blockIdx.x] = static_cast<int>(sum);
+    }
+    __syncthreads();
+}
+
 __device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, double* s_red, int* /*unused*/) {
-    if (a.precision) reduce_block_t<double>(a, acc, slot, s_red);
+    if (a.precision) reduce_block_comp(a, acc, slot, s_red);
     else reduce_block_t<float>(a, acc, slot, s_red);
 }
 
@@ -475,23 +525,55 @@ __device__ bool chol_solve_d(const double* Ain, const double* b, double* x) {
     return true;
 }
 
-// Nearest rotation (orthogonal polar factor, = U V^T of the SVD for det > 0)
-// by Newton's iteration R <- (R + R^-T) / 2 in double.
-__device__ void project_so3(float* P /* row-major 4x4, rotation block replaced */) {
+// Precision form: SE(3) exponential of the step and pose composition in FP64,
+// then the nearest rotation (orthogonal polar factor, = U V^T of the SVD for
+// det > 0) by two Newton-Schulz steps X <- X (3 I - X^T X) / 2 in FP64.
+__device__ void compose_precise(float* pose, const double* x) {
+    const double rx = x[3], ry = x[4], rz = x[5];
+    const double angle = sqrt(rx * rx + ry * ry + rz * rz);
     double R[9];
-    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) R[3 * i + j] = P[4 * i + j];
-    for (int it = 0; it < 6; ++it) {
-        const double c00 = R[4] * R[8] - R[5] * R[7], c01 = R[5] * R[6] - R[3] * R[8], c02 = R[3] * R[7] - R[4] * R[6];
-        const double c10 = R[2] * R[7] - R[1] * R[8], c11 = R[0] * R[8] - R[2] * R[6], c12 = R[1] * R[6] - R[0] * R[7];
-        const double c20 = R[1] * R[5] - R[2] * R[4], c21 = R[2] * R[3] - R[0] * R[5], c22 = R[0] * R[4] - R[1] * R[3];
-        const double det = R[0] * c00 + R[1] * c01 + R[2] * c02;
-        const double id = 1.0 / det;  // R^-T = cofactor / det
-        const double N[9] = {0.5 * (R[0] + c00 * id), 0.5 * (R[1] + c01 * id), 0.5 * (R[2] + c02 * id),
-                             0.5 * (R[3] + c10 * id), 0.5 * (R[4] + c11 * id), 0.5 * (R[5] + c12 * id),
-                             0.5 * (R[6] + c20 * id), 0.5 * (R[7] + c21 * id), 0.5 * (R[8] + c22 * id)};
-        for (int k = 0; k < 9; ++k) R[k] = N[k];
+    if (angle > 1e-4) {
+        const double ax = rx / angle, ay = ry / angle, az = rz / angle;
+        const double sn = sin(angle), cs = cos(angle), cc = 1.0 - cs;
+        R[0] = cs + cc * ax * ax;      R[1] = cc * ax * ay - sn * az; R[2] = cc * ax * az + sn * ay;
+        R[3] = cc * ax * ay + sn * az; R[4] = cs + cc * ay * ay;      R[5] = cc * ay * az - sn * ax;
+        R[6] = cc * ax * az - sn * ay; R[7] = cc * ay * az + sn * ax; R[8] = cs + cc * az * az;
+    } else {
+        R[0] = 1.0; R[1] = -rz; R[2] = ry; R[3] = rz; R[4] = 1.0; R[5] = -rx; R[6] = -ry; R[7] = rx; R[8] = 1.0;
     }
-    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) P[4 * i + j] = static_cast<float>(R[3 * i + j]);
+    const double D[12] = {R[0], R[1], R[2], x[0], R[3], R[4], R[5], x[1], R[6], R[7], R[8], x[2]};
+    double P[12];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            double sum = (j == 3) ? static_cast<double>(pose[4 * i + 3]) : 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) sum += static_cast<double>(pose[4 * i + k]) * D[4 * k + j];
+            P[4 * i + j] = sum;
+        }
+    double X[9] = {P[0], P[1], P[2], P[4], P[5], P[6], P[8], P[9], P[10]};
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        double G[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                G[3 * i + j] = (i == j ? 3.0 : 0.0) - (X[i] * X[j] + X[3 + i] * X[3 + j] + X[6 + i] * X[6 + j]);
+        double N[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                N[3 * i + j] = 0.5 * (X[3 * i] * G[j] + X[3 * i + 1] * G[3 + j] + X[3 * i + 2] * G[6 + j]);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) X[k] = N[k];
+    }
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) pose[4 * i + j] = static_cast<float>(X[3 * i + j]);
+        pose[4 * i + 3] = static_cast<float>(P[4 * i + 3]);
+    }
 }
 
 // The same projection in float by the Newton-Schulz iteration
@@ -555,6 +637,7 @@ struct SolveSmem {
     int action;    // 0 continue, 1 stop level
     int need_eig;  // the shifted-Cholesky test could not settle the damping
     float xdef[6]; // solution with the level's default damping
+    double xdef_d[6];  // the same in FP64 (precision form)
     int xdef_ok;
 };
 
@@ -618,9 +701,9 @@ __device__ void chol6_solve_f(const float* A, float damp, const float* b, float*
 // or in double for the precision form (the reference's LDL^T of the same
 // positive definite matrix agrees to rounding). False when the
 // double factorisation breaks down.
-__device__ bool damped_solve(const IcpArgs& a, const SolveSmem& sm, float damp, float* x) {
+__device__ bool damped_solve(const IcpArgs& a, const SolveSmem& sm, float damp, float* x, double* xd) {
     if (a.precision) {
-        double A[36], b[6], xd[6];
+        double A[36], b[6];
         int k = 0;
         for (int i = 0; i < 6; ++i)
             for (int j = i; j < 6; ++j) { A[i * 6 + j] = A[j * 6 + i] = sm.sum[k++]; }
@@ -673,7 +756,7 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
             sm.need_eig = (isfinite(tr) && pd_after_shift(st.information, shift)) ? 0 : 1;
         }
     } else if (lane == 1 && !(inl <= 0 || inl < kMinInliersForIteration)) {
-        sm.xdef_ok = damped_solve(a, sm, base_damp, sm.xdef) ? 1 : 0;
+        sm.xdef_ok = damped_solve(a, sm, base_damp, sm.xdef, sm.xdef_d) ? 1 : 0;
     }
     __syncwarp();
     if (sm.action != 0) return;
@@ -686,10 +769,11 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
         else if (mx > kCondEscalate * mn) damp = kDampingEscalated;
     }
     float x[6];
+    double xd[6];
     if (damp == base_damp) {
         if (!sm.xdef_ok) { sm.action = 1; return; }
-        for (int i = 0; i < 6; ++i) x[i] = sm.xdef[i];
-    } else if (!damped_solve(a, sm, damp, x)) {
+        for (int i = 0; i < 6; ++i) { x[i] = sm.xdef[i]; xd[i] = sm.xdef_d[i]; }
+    } else if (!damped_solve(a, sm, damp, x, xd)) {
         sm.action = 1;
         return;
     }
@@ -700,34 +784,27 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
     float ss = 0.0f;
     for (int i = 0; i < 6; ++i) ss = fa(ss, fm(x[i], x[i]));
     const float step_norm = fsq(ss);
-    const float rx = x[3], ry = x[4], rz = x[5];
-    float delta[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
-    const float angle = fsq(fa(fa(fm(rx, rx), fm(ry, ry)), fm(rz, rz)));
-    float R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    if (angle > 1e-4f) {
-        F3 axis = mk3(rx, ry, rz);
-        axis = div3(axis, norm3(axis));
-        angle_axis(angle, axis, R);
-    } else {
-        R[1] = -rz; R[2] = ry; R[3] = rz; R[5] = -rx; R[6] = -ry; R[7] = rx;
-    }
-    for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) delta[4 * i + j] = R[3 * i + j];
-    delta[3] = x[0]; delta[7] = x[1]; delta[11] = x[2];
-    float P[16];
     if (a.precision) {
-        // SE(3) composition in double.
-        for (int i = 0; i < 4; ++i)
-            for (int j = 0; j < 4; ++j) {
-                double s = 0.0;
-                for (int k = 0; k < 4; ++k) s += static_cast<double>(st.pose[4 * i + k]) * delta[4 * k + j];
-                P[4 * i + j] = static_cast<float>(s);
-            }
+        compose_precise(st.pose, xd);
     } else {
+        const float rx = x[3], ry = x[4], rz = x[5];
+        float delta[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        const float angle = fsq(fa(fa(fm(rx, rx), fm(ry, ry)), fm(rz, rz)));
+        float R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        if (angle > 1e-4f) {
+            F3 axis = mk3(rx, ry, rz);
+            axis = div3(axis, norm3(axis));
+            angle_axis(angle, axis, R);
+        } else {
+            R[1] = -rz; R[2] = ry; R[3] = rz; R[5] = -rx; R[6] = -ry; R[7] = rx;
+        }
+        for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) delta[4 * i + j] = R[3 * i + j];
+        delta[3] = x[0]; delta[7] = x[1]; delta[11] = x[2];
+        float P[16];
         mm4(st.pose, delta, P);
+        project_so3_f(P);
+        for (int i = 0; i < 16; ++i) st.pose[i] = P[i];
     }
-    if (a.precision) project_so3(P);
-    else project_so3_f(P);
-    for (int i = 0; i < 16; ++i) st.pose[i] = P[i];
     st.final_step = step_norm;
     st.error = fd(sum_f(a, sm.sum, 27), static_cast<float>(inl > 1 ? inl : 1));
     st.inliers = inl;

@@ -40,7 +40,7 @@ __device__ __forceinline__ void clear_bricks(uint8_t* bricks, int nb, int x, int
         for (int dy = 0; dy <= ey; ++dy)
             for (int dx = 0; dx <= ex; ++dx) {
                 const size_t b = (static_cast<size_t>(bz - dz) * nb + (by - dy)) * nb + (bx - dx);
-                if (bricks[b]) bricks[b] = 0;
+                bricks[b] = 0;
             }
 }
 
@@ -102,9 +102,10 @@ struct VoxR {
     __device__ static __forceinline__ void store(void* v, size_t i, float t, float w) {
         const unsigned short hb = __half_as_ushort(__float2half_rn(t));
         const float h = __half2float(__ushort_as_half(hb));
-        const float s = unit(hb);
-        // t - h is exact; dividing by the power of two s is exact
-        int q = __float2int_rn(fs(t, h) / s);
+        // t - h is exact; scaling by 1 / s, a power of two, is exact
+        const int e = static_cast<int>((hb >> 10) & 0x1fu);
+        const float inv_s = __int_as_float((e == 0 ? 160 : 161 - e) << 23);
+        int q = __float2int_rn(fs(t, h) * inv_s);
         q = max(-255, min(255, q));
         const uint32_t hi = (static_cast<uint32_t>(w) << 9) | (static_cast<uint32_t>(q) & 0x1ffu);
         static_cast<uint32_t*>(v)[i] = static_cast<uint32_t>(hb) | (hi << 16);

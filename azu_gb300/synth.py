@@ -10,7 +10,8 @@ quantisation and 2 % zero dropout, all from a seed:
              scene centre S = (0, 0, 1.5); 256^3 fp32 over a 2 m cube; trunc 3 vox
   c2 full    300 frames, full 360 deg orbit (1.2 deg per frame), plus 40 seeded
              spheres r in [2, 10] cm inside a 1.6 m cube about S; 512^3 fp32, 2 m
-  c3 fp16    the c2 sequence, 1024^3 fp16 tsdf + u16 weight over a 4 m cube
+  c3 fp16    the c2 sequence, 1024^3 FP16R tsdf (half + 9-bit residual) + weight
+             over a 4 m cube
   c4 batch   16 independent scenes, volumes 128/192/256/384^3, 320x240 or
              640x480, 50-200 frames
   c5 diff    512^3 built from 100 c2 frames; a perturbed render-and-compare pose
@@ -156,7 +157,7 @@ def sequence(name: str, seed: int = 1234, frames: int | None = None) -> Sequence
         scene = base_scene()
         scene.spheres += random_spheres(seed + 1)
         n, step = 300, 360.0 / 300
-        vol = _volume(1024, 4.0, fmt=1) if name == "c3" else _volume(512, 2.0)
+        vol = _volume(1024, 4.0, fmt=2) if name == "c3" else _volume(512, 2.0)
         if name == "c5":
             n = 100
     else:

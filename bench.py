@@ -141,6 +141,90 @@ def cpu_baseline(seq, raw, rgb, frames: int):
             "stage_s_per_frame": {k: v / frames for k, v in L.times.items()}}
 
 
+def run_forms(seq, raw, rgb, dev, frames: int, err_frames: int):
+    """The precision form next to the plain path on the same GPU: the c3 volume
+    (1024^3 over a 4 m cube, FP16R tsdf, ICP with FP64 sums and solve) against an
+    FP32 volume of the same size on the same frames, plus the FP16R storage
+    error against the FP64 oracle on a bounded sample."""
+    import torch
+    from azu_gb300 import _abi, api, synth
+    out = {}
+    c3 = synth.sequence("c3", frames=1).volume
+    res = {}
+    for name, fmt, prec in (("fp32", _abi.AZU_TSDF_FP32, 0), ("fp16r", _abi.AZU_TSDF_FP16R, 1)):
+        vp = api.volume_params(c3["resolution"], c3["voxel_size"], c3["truncation"], c3["max_weight"], c3["origin"],
+                               seq.min_depth, seq.max_depth, fmt)
+        tp = api.tracker_params(min_depth=seq.min_depth, max_depth=seq.max_depth, precision=prec)
+        pl = api.Pipeline(api.pipeline_params(vp, tp, 0, seq.min_depth, seq.max_depth, False, True), device=dev)
+        d_raw = torch.from_numpy(raw.view(np.int16)).to(f"cuda:{dev}")
+        d_rgb = torch.from_numpy(rgb).to(f"cuda:{dev}")
+        fb = raw[0].nbytes
+        for k in range(3):
+            pl.process_frame_device(d_raw.data_ptr() + k * fb, d_rgb.data_ptr())
+        stream = torch.cuda.ExternalStream(pl.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for k in range(3, 3 + frames):
+            pl.process_frame_device(d_raw.data_ptr() + (k % SEQ_FRAMES) * fb, d_rgb.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        fps = frames / (e0.elapsed_time(e1) / 1000.0)
+        pl.set_profiling(True)
+        for k in range(3 + frames, 3 + 2 * frames):  # stage times: one synchronous frame at a time
+            pl.process_frame_device(d_raw.data_ptr() + (k % SEQ_FRAMES) * fb, d_rgb.data_ptr(), sync=True)
+        st, nf = pl.stage_times()
+        res[name] = {"frames_per_s": fps,
+                     "stage_ms_per_frame": {k: v / max(nf, 1) for k, v in st.items()},
+                     "pose": pl.last_result()["pose"]}
+        _release(torch, dev, pl)
+        del d_raw, d_rgb
+    dp = res["fp16r"]["pose"] @ np.linalg.inv(res["fp32"]["pose"])
+    ang = float(np.arccos(np.clip((np.trace(dp[:3, :3]) - 1) / 2, -1, 1)))
+    out["precision_fp16r"] = {
+        "workload": f"c3: 1024^3 over a 4 m cube, FP16R tsdf (half + 9-bit residual, 4 B/voxel) vs FP32 (8 B/voxel), "
+                    f"ICP with compensated FP32 block sums and FP64 cross-block sum, Cholesky, SE(3) exponential and composition; "
+                    f"frames 3..{2 + frames} of the c2 orbit (stage times: the next {frames}, one at a time)",
+        "frames_per_s": res["fp16r"]["frames_per_s"], "stage_ms_per_frame": res["fp16r"]["stage_ms_per_frame"],
+        "fp32_same_workload": {"frames_per_s": res["fp32"]["frames_per_s"],
+                               "stage_ms_per_frame": res["fp32"]["stage_ms_per_frame"]},
+        "integrate_speedup_vs_fp32": res["fp32"]["stage_ms_per_frame"]["integrate"] /
+                                     max(res["fp16r"]["stage_ms_per_frame"]["integrate"], 1e-9),
+        "final_pose_vs_fp32_form": {"rad": ang, "m": float(np.linalg.norm(dp[:3, 3]))},
+    }
+    if err_frames > 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        O.set_threads(os.cpu_count() or 1)
+        v = seq.volume
+        g = api.TSDFVolume(api.volume_params(v["resolution"], v["voxel_size"], v["truncation"], v["max_weight"],
+                                             v["origin"], seq.min_depth, seq.max_depth, _abi.AZU_TSDF_FP16R),
+                           device=dev)
+        o = O.PrecisionVolume(O.tsdf_params(resolution=v["resolution"], voxel_size=v["voxel_size"],
+                                            truncation=v["truncation"], max_weight=v["max_weight"],
+                                            origin=v["origin"]), half_storage=2)
+        K = (seq.fx, seq.fy, seq.cx, seq.cy)
+        for k in range(err_frames):
+            dm = synth.mm_to_meters(seq.depth_mm[k])
+            g.integrate(dm, seq.poses[k], K, seq.width, seq.height, seq.min_depth, seq.max_depth)
+            o.integrate(dm, seq.poses[k], O.intr(*K), seq.width, seq.height, seq.min_depth, seq.max_depth)
+        t, w = g.download()
+        g.close()
+        m = w > 0
+        e = np.abs(t[m].astype(np.float64) - o.tsdf64[m])
+        eh = np.abs(t[m].astype(np.float16).astype(np.float64) - o.tsdf64[m])
+        out["precision_fp16r"]["tsdf_error_vs_fp64"] = {
+            "fold_value_max": float(e.max()), "fold_value_rms": float(np.sqrt(np.mean(e ** 2))),
+            "half_max": float(eh.max()), "half_rms": float(np.sqrt(np.mean(eh ** 2))),
+            "unit": "fraction of truncation",
+            "bit_exact_vs_emulation": bool(np.array_equal(t.view(np.uint32), o.tsdf.view(np.uint32)) and
+                                           np.array_equal(w, o.weight)),
+            "sample": f"512^3 over 2 m, first {err_frames} c2 frames at ground-truth poses, "
+                      f"{int(m.sum())} observed voxels"}
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -325,8 +409,10 @@ def run_gpu(args):
     if cpu:
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         line["cpu_stage_s_per_frame"] = cpu["stage_s_per_frame"]
-    print(json.dumps(line), flush=True)
     _release(torch, dev, mc, pl)
+    if args.form_frames > 0:
+        line["forms"] = run_forms(seq, raw, rgb, dev, args.form_frames, args.form_err_frames)
+    print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -350,6 +436,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-frames", type=int, default=12)
+    ap.add_argument("--form-frames", type=int, default=60, help="frames per precision-form run (0: skip)")
+    ap.add_argument("--form-err-frames", type=int, default=20, help="frames of the FP64 error sample (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
