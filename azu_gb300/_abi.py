@@ -91,6 +91,12 @@ SIGNATURES = {
     "azu_volume_upload": (C.c_int, [vp, vp, vp, vp]),
     "azu_volume_device_voxels": (vp, [vp]),
     "azu_volume_set_free_space_skipping": (C.c_int, [vp, C.c_int]),
+    "azu_volume_render_depth": (C.c_int, [vp, fp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, vp]),
+    "azu_volume_depth_backward": (C.c_int, [vp, fp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
+                                            vp, C.c_float, vp, vp, vp, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_uint)]),
+    "azu_volume_refine_pose": (C.c_int, [vp, fp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, vp,
+                                         C.c_float, C.c_int, fp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     # tracker
     "azu_tracker_create": (C.c_int, [C.c_int, C.POINTER(TrackerParams), vp, C.POINTER(vp)]),
     "azu_tracker_destroy": (C.c_int, [vp]),

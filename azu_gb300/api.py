@@ -157,6 +157,53 @@ class TSDFVolume:
             out["colors"] = c.cpu().numpy()
         return out
 
+    # ---- differentiation form -------------------------------------------
+    def render_depth(self, pose, K, W, H) -> np.ndarray:
+        torch = _torch()
+        d = torch.empty((H, W), dtype=torch.float32, device="cuda")
+        _ready()
+        check(self.lib.azu_volume_render_depth(self.h, _pose(pose), *map(float, K), W, H, _ptr(d)), "render_depth")
+        _done()
+        return d.cpu().numpy()
+
+    def depth_backward(self, pose, K, W, H, depth_obs, huber_delta=0.01, grad_tsdf=False, jacobian=False):
+        """Huber depth loss, dL/dxi (right se(3) perturbation), Gauss-Newton
+        terms, and optionally dL/dtsdf and the per-pixel dD/dxi."""
+        torch = _torch()
+        obs = torch.from_numpy(np.ascontiguousarray(depth_obs, np.float32)).cuda()
+        depth = torch.empty((H, W), dtype=torch.float32, device="cuda")
+        jac = torch.empty((H, W, 6), dtype=torch.float32, device="cuda") if jacobian else None
+        n = self.params.resolution ** 3
+        g = torch.zeros(n, dtype=torch.float32, device="cuda") if grad_tsdf else None
+        sums = (C.c_double * 35)()
+        over = C.c_uint(0)
+        _ready()
+        check(self.lib.azu_volume_depth_backward(self.h, _pose(pose), *map(float, K), W, H, _ptr(obs),
+                                                 float(huber_delta), _ptr(depth), _ptr(jac), _ptr(g), sums,
+                                                 C.byref(over)), "depth_backward")
+        _done()
+        s = np.array(sums[:], np.float64)
+        out = dict(loss=s[0], grad_xi=s[1:7], jtj=s[7:28], jtr=s[28:34], n_valid=int(s[34]),
+                   depth=depth.cpu().numpy(), chain_overflow=over.value)
+        if jacobian:
+            out["jacobian"] = jac.cpu().numpy()
+        if grad_tsdf:
+            out["grad_tsdf"] = g.cpu().numpy()
+        return out
+
+    def refine_pose(self, pose, K, W, H, depth_obs, huber_delta=0.01, max_iterations=20):
+        torch = _torch()
+        obs = torch.from_numpy(np.ascontiguousarray(depth_obs, np.float32)).cuda()
+        out = (C.c_float * 16)()
+        trace = (C.c_double * (max_iterations + 1))()
+        its = C.c_int(0)
+        _ready()
+        check(self.lib.azu_volume_refine_pose(self.h, _pose(pose), *map(float, K), W, H, _ptr(obs),
+                                              float(huber_delta), int(max_iterations), out, trace, C.byref(its)),
+              "refine_pose")
+        _done()
+        return np.array(out[:], np.float32).reshape(4, 4), np.array(trace[:its.value + 1]), its.value
+
     def stats(self) -> dict:
         s = _abi.VolumeStats()
         check(self.lib.azu_volume_get_stats(self.h, C.byref(s)), "stats")

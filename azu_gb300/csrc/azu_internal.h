@@ -112,6 +112,9 @@ struct azu_volume {
     // Deepest in-band depth per 8x8 pixel tile of the frame being integrated.
     float* d_tiles = nullptr;
     size_t tile_cap = 0;
+    // Differentiable rendering: per-block partials + sums + overflow counter.
+    double* d_diff = nullptr;
+    size_t diff_cap = 0;
 };
 
 namespace azu {

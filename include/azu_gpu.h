@@ -132,6 +132,33 @@ int azu_volume_set_free_space_skipping(azu_volume* v, int on);
  * {tsdf, weight} for FP32, uint32 {half, u16} for FP16). */
 void* azu_volume_device_voxels(azu_volume* v);
 
+/* ---- differentiation form (no counterpart in the reference) ------------ */
+/* Depth image of the raycast at `pose` (camera z of the hit, metres; 0 where
+ * the raycast returns no vertex): d_depth is a device float[width*height]. */
+int azu_volume_render_depth(azu_volume* v, const float pose[16], float fx, float fy, float cx, float cy, int width,
+                            int height, float* d_depth);
+/* Huber loss sum_i rho(D_i - obs_i) over pixels whose raycast hits and whose
+ * observed depth (device d_depth_obs, metres) lies in the raycast band, and
+ * its adjoint: the pose gradient is with respect to xi of pose * Exp(xi), xi =
+ * (rho, omega). Marching positions are recomputed in the backward pass.
+ * sums (host, 35 doubles): [0] loss, [1..6] dL/dxi, [7..27] sum w J J^T
+ * (upper triangle, row major), [28..33] sum w J r, [34] pixel count, with J =
+ * dD/dxi and IRLS weights w = min(1, delta/|r|). Optional device outputs:
+ * d_depth (float[W*H]), d_jacobian (float[6*W*H], dD/dxi per pixel),
+ * d_grad_tsdf (float[res^3], dL/dtsdf ADDED to its contents). chain_overflow
+ * (host, optional) counts pixels whose chain of f-dependent steps exceeded the
+ * 24 kept for the reverse sweep (their oldest terms are dropped). */
+int azu_volume_depth_backward(azu_volume* v, const float pose[16], float fx, float fy, float cx, float cy,
+                              int width, int height, const float* d_depth_obs, float huber_delta, float* d_depth,
+                              float* d_jacobian, float* d_grad_tsdf, double sums[35], unsigned* chain_overflow);
+/* Render-and-compare pose refinement: Levenberg-Marquardt on the IRLS
+ * Gauss-Newton system of the Huber depth loss from pose_in, at most
+ * max_iterations accepted steps. loss_trace (host, optional, max_iterations+1
+ * doubles) receives the loss after each accepted step. */
+int azu_volume_refine_pose(azu_volume* v, const float pose_in[16], float fx, float fy, float cx, float cy, int width,
+                           int height, const float* d_depth_obs, float huber_delta, int max_iterations,
+                           float pose_out[16], double* loss_trace, int* iterations);
+
 /* ------------------------------------------------------------------------ */
 /* ICP tracker — tracking::ICPTracker (include/tracking/ICPTracker.h:80-126). */
 /* ------------------------------------------------------------------------ */

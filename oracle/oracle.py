@@ -402,3 +402,42 @@ class PrecisionVolume(Volume):
         lib().orc_tsdf_integrate_prec(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.tsdf64, C.c_double),
                                       _p(depth_m), _p(_pose(pose)), K, int(W), int(H), C.c_float(min_depth),
                                       C.c_float(max_depth), int(self.half))
+
+
+def depth_adjoint_f(prm, tsdf, weight, pose, K, W, H, depth_obs=None, huber_delta=0.01, grad_tsdf=False,
+                    jac=False):
+    """Depth render + Huber loss + adjoint on the reference's float march, the
+    adjoint evaluated in double (differentiation form; test infrastructure)."""
+    loss = C.c_double(0.0)
+    g = np.zeros(6, np.float64)
+    gv = np.zeros(tsdf.size, np.float64) if grad_tsdf else None
+    d = np.zeros(W * H, np.float64)
+    J = np.zeros(W * H * 6, np.float64) if jac else None
+    nv = C.c_int(0)
+    obs = None if depth_obs is None else np.ascontiguousarray(depth_obs, np.float32)
+    lib().orc_depth_adjoint_f(C.byref(prm), _p(np.ascontiguousarray(tsdf, np.float32)),
+                              _p(np.ascontiguousarray(weight, np.float32)), _p(_pose(pose)), K, int(W), int(H),
+                              _p(obs), C.c_double(huber_delta), C.byref(loss), _p(g, C.c_double),
+                              _p(gv, C.c_double), _p(d, C.c_double), _p(J, C.c_double), C.byref(nv))
+    return dict(loss=loss.value, grad_xi=g, grad_tsdf=gv, depth=d.reshape(H, W),
+                jac=None if J is None else J.reshape(H, W, 6), n_valid=nv.value)
+
+
+def depth_loss_d(prm, tsdf64, weight, pose, xi, K, W, H, depth_obs=None, huber_delta=0.01, grads=False,
+                 grad_tsdf=False, jac=False):
+    """The same in double at pose * Exp(xi): the finite-difference reference."""
+    loss = C.c_double(0.0)
+    g = np.zeros(6, np.float64) if grads else None
+    gv = np.zeros(tsdf64.size, np.float64) if grad_tsdf else None
+    d = np.zeros(W * H, np.float64)
+    J = np.zeros(W * H * 6, np.float64) if jac else None
+    nv = C.c_int(0)
+    obs = None if depth_obs is None else np.ascontiguousarray(depth_obs, np.float32)
+    P = np.ascontiguousarray(np.asarray(pose, np.float64).reshape(16))
+    x = np.ascontiguousarray(np.asarray(xi, np.float64).reshape(6))
+    lib().orc_depth_loss_d(C.byref(prm), _p(np.ascontiguousarray(tsdf64, np.float64), C.c_double),
+                           _p(np.ascontiguousarray(weight, np.float32)), _p(P, C.c_double), _p(x, C.c_double), K,
+                           int(W), int(H), _p(obs), C.c_double(huber_delta), C.byref(loss), _p(g, C.c_double),
+                           _p(gv, C.c_double), _p(d, C.c_double), _p(J, C.c_double), C.byref(nv))
+    return dict(loss=loss.value, grad_xi=g, grad_tsdf=gv, depth=d.reshape(H, W),
+                jac=None if J is None else J.reshape(H, W, 6), n_valid=nv.value)

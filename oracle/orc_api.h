@@ -156,6 +156,23 @@ uint16_t orc_meters_to_raw(float meters, float min_depth, float max_depth);
 void orc_set_threads(int n);
 int  orc_get_threads(void);
 
+/* Differentiation form (no reference counterpart): depth image of the
+ * reference's raycast (camera z of the hit, 0 on a miss), Huber loss on the
+ * residual to depth_obs (pixels whose observed depth is in the raycast band),
+ * and the adjoint with respect to xi of pose * Exp(xi) (xi = rho, omega) and to
+ * the tsdf values (accumulated into grad_tsdf, res^3 doubles, when non-null).
+ * jac_out (6 per pixel) receives dDepth/dxi. orc_depth_adjoint_f marches in
+ * float exactly as the reference and evaluates the adjoint in double;
+ * orc_depth_loss_d does everything in double at pose * Exp(xi). */
+void orc_depth_adjoint_f(const orc_tsdf_params* p, const float* tsdf, const float* weight, const float pose[16],
+                         orc_intrinsics K, int width, int height, const float* depth_obs, double huber_delta,
+                         double* loss, double grad_xi[6], double* grad_tsdf, double* depth_out, double* jac_out,
+                         int* n_valid);
+void orc_depth_loss_d(const orc_tsdf_params* p, const double* tsdf, const float* weight, const double pose[16],
+                      const double xi[6], orc_intrinsics K, int width, int height, const float* depth_obs,
+                      double huber_delta, double* loss, double grad_xi[6], double* grad_tsdf, double* depth_out,
+                      double* jac_out, int* n_valid);
+
 #ifdef __cplusplus
 }
 #endif
