@@ -61,12 +61,17 @@ class MeshInfo(C.Structure):
 class PipelineParams(C.Structure):
     _fields_ = [("volume", VolumeParams), ("tracker", TrackerParams), ("preprocess_mode", C.c_int),
                 ("min_depth", C.c_float), ("max_depth", C.c_float), ("input_is_mm", C.c_int),
-                ("use_graph", C.c_int)]
+                ("use_graph", C.c_int), ("width", C.c_int), ("height", C.c_int)]
 
 
 class FrameResult(C.Structure):
     _fields_ = [("pose", C.c_float * 16), ("icp", IcpResult), ("quality", C.c_int),
                 ("integrated", C.c_int), ("frame_index", C.c_int)]
+
+
+class BatchScene(C.Structure):
+    _fields_ = [("volume", VolumeParams), ("tracker", TrackerParams), ("width", C.c_int), ("height", C.c_int),
+                ("min_depth", C.c_float), ("max_depth", C.c_float)]
 
 
 # name -> (restype, argtypes)
@@ -145,6 +150,17 @@ SIGNATURES = {
     "azu_pipeline_set_profiling": (C.c_int, [vp, C.c_int]),
     "azu_pipeline_stage_times": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "azu_pipeline_uses_graph": (C.c_int, [vp]),
+    # batch
+    "azu_batch_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(BatchScene), C.POINTER(vp)]),
+    "azu_batch_destroy": (C.c_int, [vp]),
+    "azu_batch_process": (C.c_int, [vp, C.POINTER(vp), C.c_int, C.POINTER(FrameResult)]),
+    "azu_batch_autotune": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "azu_batch_set_shapes": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+    "azu_batch_get_shapes": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "azu_batch_volume": (vp, [vp, C.c_int]),
+    "azu_batch_stream": (vp, [vp]),
+    "azu_batch_uses_graph": (C.c_int, [vp]),
+    "azu_batch_synchronize": (C.c_int, [vp]),
 }
 
 

@@ -107,10 +107,21 @@ class TSDFVolume:
               "azu_volume_create")
         self.params = params
 
+    @classmethod
+    def borrowed(cls, handle, params: _abi.VolumeParams, device: int = 0):
+        """A view of a volume owned by another object (pipeline, batch)."""
+        v = cls.__new__(cls)
+        v.lib = _abi.load()
+        v.device = device
+        v.h = handle if isinstance(handle, C.c_void_p) else C.c_void_p(handle)
+        v.params = params
+        v._borrowed = True
+        return v
+
     def close(self):
-        if self.h:
+        if self.h and not getattr(self, "_borrowed", False):
             self.lib.azu_volume_destroy(self.h)
-            self.h = C.c_void_p()
+        self.h = C.c_void_p()
 
     def __del__(self):
         _finalize(self)
@@ -374,9 +385,10 @@ class MarchingCubes:
 
 
 def pipeline_params(volume: _abi.VolumeParams, tracker: _abi.TrackerParams, preprocess_mode=_abi.AZU_PRE_FULL,
-                    min_depth=0.3, max_depth=2.5, input_is_mm=False, use_graph=True) -> _abi.PipelineParams:
+                    min_depth=0.3, max_depth=2.5, input_is_mm=False, use_graph=True, width=0,
+                    height=0) -> _abi.PipelineParams:
     return _abi.PipelineParams(volume, tracker, int(preprocess_mode), float(min_depth), float(max_depth),
-                               int(bool(input_is_mm)), int(bool(use_graph)))
+                               int(bool(input_is_mm)), int(bool(use_graph)), int(width), int(height))
 
 
 class Pipeline:
@@ -442,3 +454,76 @@ class Pipeline:
 
     def volume_handle(self):
         return C.c_void_p(self.lib.azu_pipeline_volume(self.h))
+
+
+class Batch:
+    """Many independent scenes on millimetre depth (the batching form): one
+    frame per step for every scene given a depth image."""
+
+    def __init__(self, scenes, device: int = 0):
+        self.lib = _abi.load()
+        self.device = device
+        self.n = len(scenes)
+        arr = (_abi.BatchScene * self.n)()
+        self.params = []
+        for i, sc in enumerate(scenes):
+            v = sc.volume
+            vp = volume_params(v["resolution"], v["voxel_size"], v["truncation"], v["max_weight"], v["origin"],
+                               sc.min_depth, sc.max_depth, 0)
+            tp = tracker_params(min_depth=sc.min_depth, max_depth=sc.max_depth, fx=sc.fx, fy=sc.fy, cx=sc.cx,
+                                cy=sc.cy)
+            arr[i] = _abi.BatchScene(vp, tp, int(sc.width), int(sc.height), float(sc.min_depth),
+                                     float(sc.max_depth))
+            self.params.append(vp)
+        self.h = C.c_void_p()
+        check(self.lib.azu_batch_create(device, self.n, arr, C.byref(self.h)), "azu_batch_create")
+
+    def close(self):
+        if self.h:
+            self.lib.azu_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        _finalize(self)
+
+    def process(self, depth_mm, on_device=False, results=True):
+        """depth_mm: per scene a uint16 array (host) / device pointer, or None."""
+        ptrs = (C.c_void_p * self.n)()
+        keep = []
+        for i, d in enumerate(depth_mm):
+            if d is None:
+                ptrs[i] = None
+            elif on_device:
+                ptrs[i] = int(d)
+            else:
+                a = np.ascontiguousarray(d, np.uint16)
+                keep.append(a)
+                ptrs[i] = a.ctypes.data_as(C.c_void_p).value
+        res = (_abi.FrameResult * self.n)() if results else None
+        check(self.lib.azu_batch_process(self.h, ptrs, int(bool(on_device)), res), "azu_batch_process")
+        if not results:
+            return None
+        return [Pipeline._frame(res[i]) if depth_mm[i] is not None else None for i in range(self.n)]
+
+    def autotune(self):
+        a, b = C.c_float(0), C.c_float(0)
+        check(self.lib.azu_batch_autotune(self.h, C.byref(a), C.byref(b)), "azu_batch_autotune")
+        return a.value, b.value
+
+    def shapes(self):
+        w, rw, rh = C.c_int(), C.c_int(), C.c_int()
+        check(self.lib.azu_batch_get_shapes(self.h, C.byref(w), C.byref(rw), C.byref(rh)), "get_shapes")
+        return w.value, rw.value, rh.value
+
+    def set_shapes(self, int_warps, ray_w, ray_h):
+        check(self.lib.azu_batch_set_shapes(self.h, int(int_warps), int(ray_w), int(ray_h)), "set_shapes")
+
+    def volume(self, i) -> TSDFVolume:
+        return TSDFVolume.borrowed(self.lib.azu_batch_volume(self.h, i), self.params[i], self.device)
+
+    def synchronize(self):
+        check(self.lib.azu_batch_synchronize(self.h), "synchronize")
+
+    @property
+    def stream(self):
+        return self.lib.azu_batch_stream(self.h)

@@ -119,6 +119,8 @@ struct azu_volume {
 
 namespace azu {
 size_t voxel_bytes(int format);
+// Exact free-brick flags recomputed from the voxels.
+int rebuild_bricks(azu_volume* v, cudaStream_t s);
 // Enqueue helpers shared with the pipeline (pose read from device memory).
 int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d_rgb, const float* d_pose,
                          float fx, float fy, float cx, float cy, int W, int H, float min_d, float max_d,
@@ -127,4 +129,33 @@ int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, f
                        float* d_vertices, float* d_normals, uint8_t* d_colors, const int* d_gate, cudaStream_t s);
 // Writes a host pose into a device slot with a by-value kernel argument.
 int set_pose_async(float* d_pose, const float* pose, cudaStream_t s);
+
+// What a batch needs to integrate and raycast one pipeline's frame.
+struct PipelineFrameView {
+    azu_volume* vol;
+    const float* d_depth_m;
+    const float* d_pose;
+    const int* d_gate;
+    int W, H;
+    float fx, fy, cx, cy, min_d, max_d;
+    float* d_vertices;
+    float* d_normals;
+};
+int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t stream, azu_pipeline** out);
+int pipeline_upload_inputs(azu_pipeline* pl, const uint16_t* depth, const uint8_t* rgb, cudaMemcpyKind kind);
+int pipeline_enqueue_front(azu_pipeline* pl, bool first);
+int pipeline_enqueue_commit(azu_pipeline* pl);
+int pipeline_read_result(azu_pipeline* pl, azu_frame_result* out);
+PipelineFrameView pipeline_frame_view(azu_pipeline* pl);
+}  // namespace azu
+
+struct azu_volume_batch;
+namespace azu {
+// Several volumes integrated / raycast with one launch per stage (FP32, no colour).
+int volume_batch_create(const PipelineFrameView* views, int n, azu_volume_batch** out);
+void volume_batch_destroy(azu_volume_batch* b);
+int volume_batch_set_shapes(azu_volume_batch* b, int int_warps, int ray_w, int ray_h);
+void volume_batch_shapes(const azu_volume_batch* b, int* int_warps, int* ray_w, int* ray_h);
+int volume_batch_integrate(azu_volume_batch* b, cudaStream_t s);
+int volume_batch_raycast(azu_volume_batch* b, cudaStream_t s);
 }  // namespace azu

@@ -93,6 +93,8 @@ struct azu_pipeline {
     azu::PoseState* d_st = nullptr;
     azu_icp_result* d_icp = nullptr;
     int frames = 0;
+    int W = 640, H = 480;
+    bool own_stream = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev[6] = {};
@@ -114,13 +116,13 @@ static int mark(azu_pipeline* pl, int k) {
     return AZU_OK;
 }
 
-// The work of one frame after the inputs are on the device.
-static int enqueue_frame(azu_pipeline* pl, bool first) {
+// Front of one frame after the inputs are on the device: depth, frame maps,
+// prediction and tracking (or the first-frame pose).
+int pipeline_enqueue_front(azu_pipeline* pl, bool first) {
     cudaStream_t s = pl->s;
     const azu_pipeline_params& P = pl->p;
     const float lo = P.min_depth, hi = P.max_depth;
-    const int W = 640, H = 480;
-    const azu_tracker_params& T = P.tracker;
+    const int W = pl->W, H = pl->H;
     if (int rc = mark(pl, 0)) return rc;
     if (P.input_is_mm) {
         if (int rc = mm_to_meters_enqueue(pl->d_in, pl->d_depth_m, W * H, lo, hi, s)) return rc;
@@ -142,15 +144,40 @@ static int enqueue_frame(azu_pipeline* pl, bool first) {
                                        st->prev, st->cur, pl->d_icp, &st->quality, &st->gate, s))
             return rc;
     }
-    if (int rc = mark(pl, 3)) return rc;
+    return mark(pl, 3);
+}
+
+// The model commit that closes a frame (after the gated integrate + raycast).
+int pipeline_enqueue_commit(azu_pipeline* pl) {
+    commit_kernel<<<1, 32, 0, pl->s>>>(pl->d_st);
+    AZU_LAUNCH_CHECK();
+    return AZU_OK;
+}
+
+// Everything a batch needs to integrate and raycast this pipeline's frame.
+PipelineFrameView pipeline_frame_view(azu_pipeline* pl) {
+    const azu_tracker_params& T = pl->p.tracker;
+    return PipelineFrameView{pl->vol, depth_source(pl), pl->d_st->cur, &pl->d_st->gate, pl->W, pl->H, T.fx, T.fy,
+                             T.cx, T.cy, pl->p.min_depth, pl->p.max_depth, pl->d_model_v, pl->d_model_n};
+}
+
+// The work of one frame after the inputs are on the device.
+static int enqueue_frame(azu_pipeline* pl, bool first) {
+    cudaStream_t s = pl->s;
+    const azu_pipeline_params& P = pl->p;
+    const float lo = P.min_depth, hi = P.max_depth;
+    const int W = pl->W, H = pl->H;
+    const azu_tracker_params& T = P.tracker;
+    if (int rc = pipeline_enqueue_front(pl, first)) return rc;
+    const float* dm = depth_source(pl);
+    PoseState* st = pl->d_st;
     if (int rc = volume_integrate_dev(pl->vol, dm, nullptr, st->cur, T.fx, T.fy, T.cx, T.cy, W, H, lo, hi, &st->gate, s))
         return rc;
     if (int rc = mark(pl, 4)) return rc;
     if (int rc = volume_raycast_dev(pl->vol, st->cur, T.fx, T.fy, T.cx, T.cy, W, H, pl->d_model_v, pl->d_model_n,
                                     nullptr, &st->gate, s))
         return rc;
-    commit_kernel<<<1, 32, 0, s>>>(st);
-    AZU_LAUNCH_CHECK();
+    if (int rc = pipeline_enqueue_commit(pl)) return rc;
     if (int rc = mark(pl, 5)) return rc;
     return AZU_OK;
 }
@@ -188,8 +215,8 @@ static int run_frame(azu_pipeline* pl) {
     return AZU_OK;
 }
 
-static int upload_inputs(azu_pipeline* pl, const uint16_t* depth, const uint8_t* rgb, cudaMemcpyKind kind) {
-    const size_t n = 640 * 480;
+int pipeline_upload_inputs(azu_pipeline* pl, const uint16_t* depth, const uint8_t* rgb, cudaMemcpyKind kind) {
+    const size_t n = static_cast<size_t>(pl->W) * pl->H;
     if (pl->p.input_is_mm) {
         AZU_TRY_CUDA(cudaMemcpyAsync(pl->d_in, depth, n * 2, kind, pl->s));
     } else {
@@ -199,7 +226,7 @@ static int upload_inputs(azu_pipeline* pl, const uint16_t* depth, const uint8_t*
     return AZU_OK;
 }
 
-static int read_result(azu_pipeline* pl, azu_frame_result* out) {
+int pipeline_read_result(azu_pipeline* pl, azu_frame_result* out) {
     PoseState st;
     AZU_TRY_CUDA(cudaMemcpyAsync(&st, pl->d_st, sizeof(st), cudaMemcpyDeviceToHost, pl->s));
     AZU_TRY_CUDA(cudaMemcpyAsync(&out->icp, pl->d_icp, sizeof(azu_icp_result), cudaMemcpyDeviceToHost, pl->s));
@@ -244,26 +271,40 @@ extern "C" int azu_pipeline_destroy(azu_pipeline* pl) {
                     (void*)pl->d_st, (void*)pl->d_icp})
         if (q) cudaFree(q);
     for (cudaEvent_t e : pl->ev) if (e) cudaEventDestroy(e);
-    if (pl->s) cudaStreamDestroy(pl->s);
+    if (pl->s && pl->own_stream) cudaStreamDestroy(pl->s);
     delete pl;
     return AZU_OK;
 }
 
-extern "C" int azu_pipeline_create(int device, const azu_pipeline_params* p, azu_pipeline** out) {
+namespace azu {
+// A pipeline on the given stream (not owned), or on its own when null.
+int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t stream, azu_pipeline** out) {
     AZU_CHECK_ARG(p != nullptr && out != nullptr, "null argument");
     *out = nullptr;
+    const int W = p->width > 0 ? p->width : 640, H = p->height > 0 ? p->height : 480;
+    AZU_CHECK_ARG(W >= 8 && H >= 8 && W <= 8192 && H <= 8192 && W % 4 == 0 && H % 4 == 0,
+                  "image size must be multiples of 4 in [8, 8192]");
+    AZU_CHECK_ARG(p->input_is_mm || (W == 640 && H == 480), "the Kinect raw-code path is 640 x 480");
     if (int rc = bind_device(device)) return rc;
     azu_pipeline* pl = new azu_pipeline();
     pl->device = device;
     pl->p = *p;
+    pl->W = W;
+    pl->H = H;
     int rc = AZU_OK;
-    cudaError_t e = cudaStreamCreateWithFlags(&pl->s, cudaStreamNonBlocking);
+    cudaError_t e = cudaSuccess;
+    if (stream) {
+        pl->s = stream;
+        pl->own_stream = false;
+    } else {
+        e = cudaStreamCreateWithFlags(&pl->s, cudaStreamNonBlocking);
+    }
     if (e) { set_error("stream: %s", cudaGetErrorString(e)); rc = AZU_E_CUDA; }
     if (!rc) rc = azu_volume_create(device, &p->volume, pl->s, &pl->vol);
     if (!rc) rc = azu_tracker_create(device, &p->tracker, pl->s, &pl->trk);
     if (!rc && !p->input_is_mm) rc = azu_preprocessor_create(device, p->preprocess_mode, pl->s, &pl->pre);
     if (!rc) {
-        const size_t n = 640 * 480;
+        const size_t n = static_cast<size_t>(W) * H;
         e = cudaMalloc(&pl->d_in, n * 2);
         if (!e) e = cudaMalloc(&pl->d_depth_m, n * 4);
         if (!e) e = cudaMalloc(&pl->d_model_v, n * 12);
@@ -277,6 +318,11 @@ extern "C" int azu_pipeline_create(int device, const azu_pipeline_params* p, azu
     if (rc) { azu_pipeline_destroy(pl); return rc; }
     *out = pl;
     return AZU_OK;
+}
+}  // namespace azu
+
+extern "C" int azu_pipeline_create(int device, const azu_pipeline_params* p, azu_pipeline** out) {
+    return pipeline_create_on(device, p, nullptr, out);
 }
 
 extern "C" int azu_pipeline_reset(azu_pipeline* pl) {
@@ -294,9 +340,9 @@ extern "C" int azu_pipeline_process_frame(azu_pipeline* pl, const uint16_t* h_de
     AZU_CHECK_ARG(pl != nullptr && h_depth != nullptr && out != nullptr, "null argument");
     AZU_CHECK_ARG(pl->p.input_is_mm || h_rgb != nullptr, "the raw-code path needs the RGB frame for guidance");
     AZU_TRY_CUDA(cudaSetDevice(pl->device));
-    if (int rc = upload_inputs(pl, h_depth, h_rgb, cudaMemcpyHostToDevice)) return rc;
+    if (int rc = pipeline_upload_inputs(pl, h_depth, h_rgb, cudaMemcpyHostToDevice)) return rc;
     if (int rc = run_frame(pl)) return rc;
-    return read_result(pl, out);
+    return pipeline_read_result(pl, out);
 }
 
 extern "C" int azu_pipeline_process_frame_device(azu_pipeline* pl, const uint16_t* d_depth, const uint8_t* d_rgb,
@@ -304,16 +350,16 @@ extern "C" int azu_pipeline_process_frame_device(azu_pipeline* pl, const uint16_
     AZU_CHECK_ARG(pl != nullptr && d_depth != nullptr, "null argument");
     AZU_CHECK_ARG(pl->p.input_is_mm || d_rgb != nullptr, "the raw-code path needs the RGB frame for guidance");
     AZU_TRY_CUDA(cudaSetDevice(pl->device));
-    if (int rc = upload_inputs(pl, d_depth, d_rgb, cudaMemcpyDeviceToDevice)) return rc;
+    if (int rc = pipeline_upload_inputs(pl, d_depth, d_rgb, cudaMemcpyDeviceToDevice)) return rc;
     if (int rc = run_frame(pl)) return rc;
-    if (out) return read_result(pl, out);
+    if (out) return pipeline_read_result(pl, out);
     return AZU_OK;
 }
 
 extern "C" int azu_pipeline_last_result(azu_pipeline* pl, azu_frame_result* out) {
     AZU_CHECK_ARG(pl != nullptr && out != nullptr, "null argument");
     AZU_TRY_CUDA(cudaSetDevice(pl->device));
-    return read_result(pl, out);
+    return pipeline_read_result(pl, out);
 }
 
 extern "C" azu_volume* azu_pipeline_volume(azu_pipeline* pl) { return pl ? pl->vol : nullptr; }

@@ -65,10 +65,11 @@ constexpr int kTileShift = 3;  // level-0 depth tiles are 8x8 pixels
 
 // Deepest in-band depth of every 8x8 pixel tile (-inf when the tile has none),
 // level 0 of the tile pyramid. Eight lanes share a tile, one pixel row each.
-__global__ void depth_tiles_kernel(const float* __restrict__ depth, int W, int H, float min_d, float max_d, int tw,
-                                   int ntiles, float* __restrict__ tiles, const int* __restrict__ gate) {
+__device__ __forceinline__ void depth_tiles_body(int blk, const float* __restrict__ depth, int W, int H, float min_d,
+                                                 float max_d, int tw, int ntiles, float* __restrict__ tiles,
+                                                 const int* __restrict__ gate) {
     if (gate && __ldg(gate) == 0) return;
-    const int t = blockIdx.x * (blockDim.x >> 3) + (threadIdx.x >> 3);
+    const int t = blk * (blockDim.x >> 3) + (threadIdx.x >> 3);
     const int r = threadIdx.x & 7;
     float m = -__int_as_float(0x7f800000);
     if (t < ntiles) {
@@ -89,6 +90,10 @@ __global__ void depth_tiles_kernel(const float* __restrict__ depth, int W, int H
     m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
     m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
     if (t < ntiles && r == 0) tiles[t] = m;
+}
+__global__ void depth_tiles_kernel(const float* __restrict__ depth, int W, int H, float min_d, float max_d, int tw,
+                                   int ntiles, float* __restrict__ tiles, const int* __restrict__ gate) {
+    depth_tiles_body(blockIdx.x, depth, W, H, min_d, max_d, tw, ntiles, tiles, gate);
 }
 
 TileMip make_tile_mip(int W, int H) {
@@ -114,10 +119,11 @@ TileMip make_tile_mip(int W, int H) {
 // computed on the device so the pose may come from the tracker without a host
 // round trip. Same float expression trees as the CPU path. Thread 0 writes the
 // constants; the block then builds levels 1.. of the tile pyramid.
-__global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res, float vs, float ox, float oy,
-                                       float oz, float trunc, float fx, float fy, float cx, float cy, int W, int H,
-                                       float max_d, IntegrateConsts* out, unsigned long long* counters,
-                                       float* __restrict__ tiles, TileMip mip) {
+__device__ __forceinline__ void integrate_setup_body(const float* __restrict__ d_pose, int res, float vs, float ox,
+                                                     float oy, float oz, float trunc, float fx, float fy, float cx,
+                                                     float cy, int W, int H, float max_d, IntegrateConsts* out,
+                                                     unsigned long long* counters, float* __restrict__ tiles,
+                                                     const TileMip& mip) {
     if (threadIdx.x == 0) {
         float P[16], inv[16], Rcw[9];
         for (int i = 0; i < 16; ++i) P[i] = d_pose[i];
@@ -199,6 +205,12 @@ __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res
         }
     }
 }
+__global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res, float vs, float ox, float oy,
+                                       float oz, float trunc, float fx, float fy, float cx, float cy, int W, int H,
+                                       float max_d, IntegrateConsts* out, unsigned long long* counters,
+                                       float* __restrict__ tiles, TileMip mip) {
+    integrate_setup_body(d_pose, res, vs, ox, oy, oz, trunc, fx, fy, cx, cy, W, H, max_d, out, counters, tiles, mip);
+}
 
 // Voxel-projective integration (TSDFVolume.cpp:282-329).
 //
@@ -218,19 +230,18 @@ __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res
 // Every test is exact or conservative, so the updated set and the values are
 // the CPU's. Voxels that take no update are never read: HBM traffic is
 // 2 x record size per updated voxel.
+// One warp item (32 rows at one z) of one volume; s_c is the block's staging
+// array, indexed by the warp.
 template <bool kHalf, bool kColor, bool kResid>
-__global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
+__device__ __forceinline__ void integrate_item(
     void* __restrict__ vox, float* __restrict__ color, const IntegrateConsts* __restrict__ icp,
     const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
     float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
     float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb,
-    const float* __restrict__ tiles, TileMip mip) {
-    __shared__ float s_c[kIntWarps][3][32][33];
+    const float* __restrict__ tiles, const TileMip& mip, int item, int warp, int lane, float (*s_c)[3][32][33]) {
     if (gate && __ldg(gate) == 0) return;
     if (!__ldg(&icp->valid)) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ngroups = (res + 31) >> 5;
-    const int item = blockIdx.x * kIntWarps + warp;
     if (item >= res * ngroups) return;
     const int z = item / ngroups;
     const int ybase = (item - z * ngroups) << 5;
@@ -470,6 +481,20 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     }
 }
 
+template <bool kHalf, bool kColor, bool kResid>
+__global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
+    void* __restrict__ vox, float* __restrict__ color, const IntegrateConsts* __restrict__ icp,
+    const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
+    float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
+    float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb,
+    const float* __restrict__ tiles, TileMip mip) {
+    __shared__ float s_c[kIntWarps][3][32][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    integrate_item<kHalf, kColor, kResid>(vox, color, icp, depth, rgb, res, vs, ox, oy, oz, trunc, max_w, fx, fy, cx,
+                                          cy, W, H, min_d, max_d, gate, counters, bricks, nb, tiles, mip,
+                                          blockIdx.x * kIntWarps + warp, warp, lane, s_c);
+}
+
 // ---- raycast ---------------------------------------------------------------
 // State of the brick holding the sample at p: -1 outside the samplable box
 // (the sample is invalid), else the brick's free distance: 0 for a brick that
@@ -494,11 +519,11 @@ __device__ __forceinline__ int brick_state(const VolView& v, const uint8_t* __re
 // pass reads the flags) and kDistCap outside the grid. Three passes (x, y, z)
 // give the distance to the nearest non-free brick, capped.
 constexpr int kDistCap = 12;
-__global__ void brick_dist_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, int nb, int axis,
-                                  int from_flags, const int* __restrict__ gate) {
+__device__ __forceinline__ void brick_dist_body(size_t blk, const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
+                                                int nb, int axis, int from_flags, const int* __restrict__ gate) {
     if (gate && __ldg(gate) == 0) return;
     const size_t n = static_cast<size_t>(nb) * nb * nb;
-    const size_t b = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const size_t b = blk * blockDim.x + threadIdx.x;
     if (b >= n) return;
     const int c[3] = {static_cast<int>(b % nb), static_cast<int>((b / nb) % nb), static_cast<int>(b / nb / nb)};
     const size_t stride = axis == 0 ? 1 : (axis == 1 ? static_cast<size_t>(nb) : static_cast<size_t>(nb) * nb);
@@ -512,6 +537,10 @@ __global__ void brick_dist_kernel(const uint8_t* __restrict__ in, uint8_t* __res
         d = min(d, max(abs(k), val));
     }
     out[b] = static_cast<uint8_t>(d);
+}
+__global__ void brick_dist_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, int nb, int axis,
+                                  int from_flags, const int* __restrict__ gate) {
+    brick_dist_body(blockIdx.x, in, out, nb, axis, from_flags, gate);
 }
 
 // Fast-forward through free space. From a sample t whose brick b has free
@@ -568,15 +597,12 @@ __global__ void rebuild_bricks_kernel(const void* vox, int res, uint8_t* bricks,
 // 32 adjacent pixels of one row, so its rays march side by side and their
 // trilinear gathers share cache lines.
 template <bool kHalf>
-__global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __restrict__ d_pose, float fx,
-                                                     float fy, float cx, float cy, int W, int H, float trunc,
-                                                     float min_depth, float max_depth, float* __restrict__ vout,
-                                                     float* __restrict__ nout, uint8_t* __restrict__ cout,
-                                                     const int* __restrict__ gate, const uint8_t* __restrict__ bdist,
-                                                     int nb) {
+__device__ __forceinline__ void raycast_pixel(const VolView& v, const float* __restrict__ d_pose, float fx, float fy,
+                                              float cx, float cy, int W, int H, float trunc, float min_depth,
+                                              float max_depth, float* __restrict__ vout, float* __restrict__ nout,
+                                              uint8_t* __restrict__ cout, const int* __restrict__ gate,
+                                              const uint8_t* __restrict__ bdist, int nb, int x, int y) {
     if (gate && __ldg(gate) == 0) return;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= W || y >= H) return;
     const int o = y * W + x;
     float R[9];
@@ -704,6 +730,253 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
     vout[3 * o] = vres.x; vout[3 * o + 1] = vres.y; vout[3 * o + 2] = vres.z;
     nout[3 * o] = nres.x; nout[3 * o + 1] = nres.y; nout[3 * o + 2] = nres.z;
     if (cout) { cout[3 * o] = col[0]; cout[3 * o + 1] = col[1]; cout[3 * o + 2] = col[2]; }
+}
+
+template <bool kHalf>
+__global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __restrict__ d_pose, float fx,
+                                                     float fy, float cx, float cy, int W, int H, float trunc,
+                                                     float min_depth, float max_depth, float* __restrict__ vout,
+                                                     float* __restrict__ nout, uint8_t* __restrict__ cout,
+                                                     const int* __restrict__ gate, const uint8_t* __restrict__ bdist,
+                                                     int nb) {
+    raycast_pixel<kHalf>(v, d_pose, fx, fy, cx, cy, W, H, trunc, min_depth, max_depth, vout, nout, cout, gate, bdist,
+                         nb, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+static int ensure_tiles(azu_volume* v, size_t n, cudaStream_t s);
+
+// ---- batches: several volumes, one launch per stage --------------------------
+// A batch integrates and raycasts the current frame of several independent
+// volumes (different resolutions and image sizes) with one launch per stage.
+// Each launch maps its blocks (or warps) onto the volumes through prefix
+// offsets and runs the same per-volume body as the single-volume kernels, so
+// every volume's result is the single-volume result bit for bit. The integrate
+// block size and the raycast tile shape are parameters (the batch autotuner
+// picks them).
+struct IntegrateArgs {
+    void* vox;
+    const IntegrateConsts* icp;
+    const float* depth;
+    int res;
+    float vs, ox, oy, oz, trunc, max_w, fx, fy, cx, cy;
+    int W, H;
+    float min_d, max_d;
+    const int* gate;
+    unsigned long long* counters;
+    uint8_t* bricks;
+    int nb;
+    float* tiles;
+    TileMip mip;
+    IntegrateConsts* icp_out;
+    const float* pose;
+};
+
+struct RaycastArgs {
+    VolView v;
+    const float* pose;
+    float fx, fy, cx, cy;
+    int W, H;
+    float trunc, min_depth, max_depth;
+    float* vout;
+    float* nout;
+    const int* gate;
+    const uint8_t* bricks;
+    uint8_t* bdist;
+    uint8_t* btmp;
+    int nb;
+};
+
+__device__ __forceinline__ int batch_find(const int* __restrict__ off, int n, int i) {
+    int s = 0;
+    while (s + 1 < n && i >= __ldg(off + s + 1)) ++s;
+    return s;
+}
+
+__global__ void depth_tiles_batch_kernel(const IntegrateArgs* __restrict__ A, const int* __restrict__ off, int n) {
+    const int s = batch_find(off, n, blockIdx.x);
+    const IntegrateArgs& a = A[s];
+    depth_tiles_body(blockIdx.x - __ldg(off + s), a.depth, a.W, a.H, a.min_d, a.max_d, a.mip.w[0],
+                     a.mip.w[0] * a.mip.h[0], a.tiles, a.gate);
+}
+
+__global__ void integrate_setup_batch_kernel(const IntegrateArgs* __restrict__ A, unsigned long long** counters) {
+    const IntegrateArgs& a = A[blockIdx.x];
+    integrate_setup_body(a.pose, a.res, a.vs, a.ox, a.oy, a.oz, a.trunc, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.max_d,
+                         a.icp_out, a.counters, a.tiles, a.mip);
+}
+
+template <int kWarps>
+__global__ void __launch_bounds__(kWarps * 32) integrate_batch_kernel(const IntegrateArgs* __restrict__ A,
+                                                                      const int* __restrict__ off, int n) {
+    __shared__ float s_c[kWarps][3][32][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int item = blockIdx.x * kWarps + warp;
+    const int s = batch_find(off, n, item);
+    const IntegrateArgs& a = A[s];
+    integrate_item<false, false, false>(a.vox, nullptr, a.icp, a.depth, nullptr, a.res, a.vs, a.ox, a.oy, a.oz,
+                                        a.trunc, a.max_w, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.min_d, a.max_d,
+                                        a.gate, a.counters, a.bricks, a.nb, a.tiles, a.mip, item - __ldg(off + s),
+                                        warp, lane, s_c);
+}
+
+__global__ void brick_dist_batch_kernel(const RaycastArgs* __restrict__ A, const int* __restrict__ off, int n,
+                                        int pass) {
+    const int s = batch_find(off, n, blockIdx.x);
+    const RaycastArgs& a = A[s];
+    const uint8_t* in = pass == 0 ? a.bricks : (pass == 1 ? a.bdist : a.btmp);
+    uint8_t* out = pass == 1 ? a.btmp : a.bdist;
+    brick_dist_body(blockIdx.x - __ldg(off + s), in, out, a.nb, pass, pass == 0 ? 1 : 0, a.gate);
+}
+
+__global__ void __launch_bounds__(256) raycast_batch_kernel(const RaycastArgs* __restrict__ A,
+                                                            const int* __restrict__ off, int n) {
+    const int s = batch_find(off, n, blockIdx.x);
+    const RaycastArgs& a = A[s];
+    const int tile = blockIdx.x - __ldg(off + s);
+    const int tiles_x = (a.W + blockDim.x - 1) / blockDim.x;
+    const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
+    raycast_pixel<false>(a.v, a.pose, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.trunc, a.min_depth, a.max_depth, a.vout,
+                         a.nout, nullptr, a.gate, a.bdist, a.nb, tx * blockDim.x + threadIdx.x,
+                         ty * blockDim.y + threadIdx.y);
+}
+
+}  // namespace azu
+
+struct azu_volume_batch {
+    int n = 0;
+    std::vector<azu::PipelineFrameView> views;
+    azu::IntegrateArgs* d_int = nullptr;
+    azu::RaycastArgs* d_ray = nullptr;
+    int* d_off = nullptr;  // [0..n] tile blocks, [n+1..2n+1] integrate items, [2n+2..3n+2] bricks, [3n+3..4n+3] ray tiles
+    int tiles_blocks = 0, items = 0, brick_blocks = 0, ray_blocks = 0;
+    int int_warps = 4, ray_w = 32, ray_h = 8;
+};
+
+namespace azu {
+
+static int batch_upload_offsets(azu_volume_batch* b) {
+    const int n = b->n;
+    std::vector<int> off(4 * (n + 1), 0);
+    int tb = 0, it = 0, bb = 0, rb = 0;
+    for (int i = 0; i < n; ++i) {
+        const PipelineFrameView& f = b->views[i];
+        const TileMip mip = make_tile_mip(f.W, f.H);
+        off[i] = tb;
+        tb += (mip.w[0] * mip.h[0] + 31) / 32;
+        off[n + 1 + i] = it;
+        const int res = f.vol->p.resolution;
+        it += res * ((res + 31) / 32);
+        off[2 * (n + 1) + i] = bb;
+        const size_t nbr = static_cast<size_t>(f.vol->nb) * f.vol->nb * f.vol->nb;
+        bb += static_cast<int>((nbr + 255) / 256);
+        off[3 * (n + 1) + i] = rb;
+        rb += ((f.W + b->ray_w - 1) / b->ray_w) * ((f.H + b->ray_h - 1) / b->ray_h);
+    }
+    off[n] = tb;
+    off[n + 1 + n] = it;
+    off[2 * (n + 1) + n] = bb;
+    off[3 * (n + 1) + n] = rb;
+    b->tiles_blocks = tb;
+    b->items = it;
+    b->brick_blocks = bb;
+    b->ray_blocks = rb;
+    AZU_TRY_CUDA(cudaMemcpy(b->d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return AZU_OK;
+}
+
+int volume_batch_create(const PipelineFrameView* views, int n, azu_volume_batch** out) {
+    AZU_CHECK_ARG(views != nullptr && out != nullptr && n >= 1 && n <= 4096, "batch of 1..4096 volumes");
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        const azu_volume* v = views[i].vol;
+        AZU_CHECK_ARG(v != nullptr && v->p.format == AZU_TSDF_FP32 && v->color == nullptr,
+                      "batched volumes are FP32 without colour");
+    }
+    azu_volume_batch* b = new azu_volume_batch();
+    b->n = n;
+    b->views.assign(views, views + n);
+    std::vector<IntegrateArgs> ia(n);
+    std::vector<RaycastArgs> ra(n);
+    int rc = AZU_OK;
+    for (int i = 0; i < n && !rc; ++i) {
+        const PipelineFrameView& f = views[i];
+        azu_volume* v = f.vol;
+        const azu_volume_params& p = v->p;
+        const TileMip mip = make_tile_mip(f.W, f.H);
+        rc = ensure_tiles(v, static_cast<size_t>(mip.total), v->stream.s);
+        ia[i] = IntegrateArgs{v->vox, v->d_iconsts, f.d_depth_m, p.resolution, p.voxel_size, p.origin[0],
+                              p.origin[1], p.origin[2], p.truncation, p.max_weight, f.fx, f.fy, f.cx, f.cy, f.W,
+                              f.H, f.min_d, f.max_d, f.d_gate, v->d_counters, v->bricks, v->nb, v->d_tiles, mip,
+                              v->d_iconsts, f.d_pose};
+        ra[i] = RaycastArgs{make_view(v), f.d_pose, f.fx, f.fy, f.cx, f.cy, f.W, f.H, p.truncation, p.min_depth,
+                            p.max_depth, f.d_vertices, f.d_normals, f.d_gate, v->bricks, v->brick_dist,
+                            v->brick_tmp, v->nb};
+        AZU_CHECK_ARG(v->skip_free, "batched raycasts use free-space skipping");
+    }
+    if (!rc) {
+        cudaError_t e = cudaMalloc(&b->d_int, n * sizeof(IntegrateArgs));
+        if (!e) e = cudaMalloc(&b->d_ray, n * sizeof(RaycastArgs));
+        if (!e) e = cudaMalloc(&b->d_off, 4 * (n + 1) * sizeof(int));
+        if (!e) e = cudaMemcpy(b->d_int, ia.data(), n * sizeof(IntegrateArgs), cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(b->d_ray, ra.data(), n * sizeof(RaycastArgs), cudaMemcpyHostToDevice);
+        if (e) { set_error("batch allocation: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; }
+    }
+    if (!rc) rc = batch_upload_offsets(b);
+    if (rc) { volume_batch_destroy(b); return rc; }
+    *out = b;
+    return AZU_OK;
+}
+
+void volume_batch_destroy(azu_volume_batch* b) {
+    if (!b) return;
+    if (b->d_int) cudaFree(b->d_int);
+    if (b->d_ray) cudaFree(b->d_ray);
+    if (b->d_off) cudaFree(b->d_off);
+    delete b;
+}
+
+int volume_batch_set_shapes(azu_volume_batch* b, int int_warps, int ray_w, int ray_h) {
+    AZU_CHECK_ARG(int_warps == 1 || int_warps == 2 || int_warps == 4, "integrate warps per block: 1, 2 or 4");
+    AZU_CHECK_ARG(ray_w >= 8 && ray_h >= 1 && ray_w * ray_h <= 256 && (ray_w * ray_h) % 32 == 0,
+                  "raycast tile: at most 256 threads, whole warps");
+    b->int_warps = int_warps;
+    b->ray_w = ray_w;
+    b->ray_h = ray_h;
+    return batch_upload_offsets(b);
+}
+
+void volume_batch_shapes(const azu_volume_batch* b, int* int_warps, int* ray_w, int* ray_h) {
+    if (int_warps) *int_warps = b->int_warps;
+    if (ray_w) *ray_w = b->ray_w;
+    if (ray_h) *ray_h = b->ray_h;
+}
+
+int volume_batch_integrate(azu_volume_batch* b, cudaStream_t s) {
+    const int n = b->n;
+    depth_tiles_batch_kernel<<<b->tiles_blocks, 256, 0, s>>>(b->d_int, b->d_off, n);
+    AZU_LAUNCH_CHECK();
+    integrate_setup_batch_kernel<<<n, 256, 0, s>>>(b->d_int, nullptr);
+    AZU_LAUNCH_CHECK();
+    const int* ioff = b->d_off + (n + 1);
+    const int blocks = (b->items + b->int_warps - 1) / b->int_warps;
+    if (b->int_warps == 1) integrate_batch_kernel<1><<<blocks, 32, 0, s>>>(b->d_int, ioff, n);
+    else if (b->int_warps == 2) integrate_batch_kernel<2><<<blocks, 64, 0, s>>>(b->d_int, ioff, n);
+    else integrate_batch_kernel<4><<<blocks, 128, 0, s>>>(b->d_int, ioff, n);
+    AZU_LAUNCH_CHECK();
+    for (const PipelineFrameView& f : b->views) f.vol->integrated_frames++;
+    return AZU_OK;
+}
+
+int volume_batch_raycast(azu_volume_batch* b, cudaStream_t s) {
+    const int n = b->n;
+    const int* boff = b->d_off + 2 * (n + 1);
+    for (int pass = 0; pass < 3; ++pass) {
+        brick_dist_batch_kernel<<<b->brick_blocks, 256, 0, s>>>(b->d_ray, boff, n, pass);
+        AZU_LAUNCH_CHECK();
+    }
+    raycast_batch_kernel<<<b->ray_blocks, dim3(b->ray_w, b->ray_h), 0, s>>>(b->d_ray, b->d_off + 3 * (n + 1), n);
+    AZU_LAUNCH_CHECK();
+    return AZU_OK;
 }
 
 // ---- whole-volume transfers -------------------------------------------------

@@ -325,6 +325,9 @@ typedef struct {
                                 Kinect preprocessor, depth_m = mm * 1e-3);
                                 0: Kinect raw codes through the preprocessor */
     int   use_graph;         /* capture the per-frame work in a CUDA graph */
+    int   width, height;     /* image size; 0 = 640 x 480. Other sizes need
+                                input_is_mm (the Kinect preprocessor is
+                                640 x 480) and the tracker's intrinsics for them */
 } azu_pipeline_params;
 
 typedef struct {
@@ -365,6 +368,40 @@ int azu_pipeline_set_profiling(azu_pipeline* p, int on);
 int azu_pipeline_stage_times(azu_pipeline* p, double ms_total[5], int* frames);
 /* 1 when frames k > 0 replay a captured CUDA graph. */
 int azu_pipeline_uses_graph(azu_pipeline* p);
+
+/* ------------------------------------------------------------------------ */
+/* Batching form (no counterpart in the reference): many independent scenes,   */
+/* each with its own volume, image size and frame count, advanced together.   */
+/* ------------------------------------------------------------------------ */
+
+typedef struct azu_batch azu_batch;
+
+typedef struct {
+    azu_volume_params  volume;     /* FP32, no colour */
+    azu_tracker_params tracker;    /* intrinsics for this scene's image size */
+    int   width, height;           /* multiples of 4 */
+    float min_depth, max_depth;    /* depth band of the millimetre input */
+} azu_batch_scene;
+
+/* n scenes (1..64), each an independent pipeline on millimetre depth. */
+int azu_batch_create(int device, int n, const azu_batch_scene* scenes, azu_batch** out);
+int azu_batch_destroy(azu_batch* b);
+/* One frame for every scene i with depth_mm[i] != NULL (uint16 millimetres,
+ * host or device memory per on_device); scenes with NULL sit this step out.
+ * Per scene as the single pipeline does (first frame at identity, then ICP
+ * and gated fusion); integration and raycasting of all active scenes run as
+ * one launch per stage, and steps replay one CUDA graph per active set.
+ * results (n entries, optional) receive the active scenes' results (sync). */
+int azu_batch_process(azu_batch* b, const uint16_t* const* depth_mm, int on_device, azu_frame_result* results);
+/* Times the integrate block sizes and raycast tile shapes on the batch's own
+ * data (after at least one step) and keeps the fastest; results unchanged. */
+int azu_batch_autotune(azu_batch* b, float* best_integrate_ms, float* best_raycast_ms);
+int azu_batch_set_shapes(azu_batch* b, int int_warps, int ray_w, int ray_h);
+int azu_batch_get_shapes(azu_batch* b, int* int_warps, int* ray_w, int* ray_h);
+azu_volume* azu_batch_volume(azu_batch* b, int i);
+void* azu_batch_stream(azu_batch* b);
+int azu_batch_uses_graph(azu_batch* b);
+int azu_batch_synchronize(azu_batch* b);
 
 #ifdef __cplusplus
 }
