@@ -96,6 +96,9 @@ SIGNATURES = {
     "azu_volume_upload": (C.c_int, [vp, vp, vp, vp]),
     "azu_volume_device_voxels": (vp, [vp]),
     "azu_volume_set_free_space_skipping": (C.c_int, [vp, C.c_int]),
+    "azu_volume_raycast_many": (C.c_int, [vp, fp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                          C.c_int, vp, vp]),
+    "azu_volume_point_cloud": (C.c_int, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64)]),
     "azu_volume_render_depth": (C.c_int, [vp, fp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, vp]),
     "azu_volume_depth_backward": (C.c_int, [vp, fp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
                                             vp, C.c_float, vp, vp, vp, C.POINTER(C.c_double),
@@ -113,6 +116,8 @@ SIGNATURES = {
                                     C.POINTER(IcpResult)]),
     "azu_tracker_build_system": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.c_int, fp, fp, fp, fp, fp,
                                            C.POINTER(C.c_int)]),
+    "azu_tracker_track_many": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int, fp, fp,
+                                         C.POINTER(TrackerParams), C.POINTER(IcpResult)]),
     "azu_tracker_load_live": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.c_int]),
     "azu_icp_build_system_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, vp, C.c_int, C.c_int,
                                                C.POINTER(TrackerParams), fp, fp, vp, fp, fp, fp,

@@ -168,6 +168,29 @@ class TSDFVolume:
             out["colors"] = c.cpu().numpy()
         return out
 
+    def raycast_many(self, poses, K, W, H):
+        """Model images at several poses in one launch (device tensors [n, H, W, 3])."""
+        torch = _torch()
+        P = np.ascontiguousarray(np.asarray(poses, np.float32).reshape(-1, 16))
+        n = P.shape[0]
+        v = torch.empty((n, H, W, 3), dtype=torch.float32, device="cuda")
+        nrm = torch.empty((n, H, W, 3), dtype=torch.float32, device="cuda")
+        _ready()
+        check(self.lib.azu_volume_raycast_many(self.h, P.ctypes.data_as(_abi.fp), n, *map(float, K), W, H, _ptr(v),
+                                               _ptr(nrm)), "raycast_many")
+        _done()
+        return v, nrm
+
+    def point_cloud(self):
+        """extractGlobalPointCloud: (N, 3) float32 world points, (N, 3) uint8 colours."""
+        n = C.c_int64(0)
+        check(self.lib.azu_volume_point_cloud(self.h, None, None, 0, C.byref(n)), "point_cloud")
+        pts = np.empty((max(n.value, 1), 3), np.float32)
+        col = np.empty((max(n.value, 1), 3), np.uint8)
+        check(self.lib.azu_volume_point_cloud(self.h, pts.ctypes.data_as(C.c_void_p), col.ctypes.data_as(C.c_void_p),
+                                              n.value, C.byref(n)), "point_cloud")
+        return pts[:n.value], col[:n.value]
+
     # ---- differentiation form -------------------------------------------
     def render_depth(self, pose, K, W, H) -> np.ndarray:
         torch = _torch()
@@ -267,6 +290,19 @@ class ICPTracker:
         check(self.lib.azu_tracker_track_prepared(self.h, W, H, _ptr(d_mv), _ptr(d_mn), MW, MH, _pose(estimate),
                                                   _pose(ref_pose), C.byref(r)), "track_prepared")
         return result_dict(r)
+
+    def track_many(self, W, H, d_mv, d_mn, MW, MH, estimates, ref_poses=None, params=None) -> list:
+        """One solve per candidate k against model image k (d_mv/d_mn hold them back to back)."""
+        E = np.ascontiguousarray(np.asarray(estimates, np.float32).reshape(-1, 16))
+        n = E.shape[0]
+        R = None if ref_poses is None else np.ascontiguousarray(np.asarray(ref_poses, np.float32).reshape(-1, 16))
+        out = (_abi.IcpResult * n)()
+        _ready()
+        check(self.lib.azu_tracker_track_many(self.h, W, H, _ptr(d_mv), _ptr(d_mn), MW, MH, n,
+                                              E.ctypes.data_as(_abi.fp),
+                                              None if R is None else R.ctypes.data_as(_abi.fp),
+                                              None if params is None else C.byref(params), out), "track_many")
+        return [result_dict(out[k]) for k in range(n)]
 
     def build_system(self, level, d_mv, d_mn, MW, MH, pose, ref_pose) -> dict:
         _ready()

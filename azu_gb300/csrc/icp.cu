@@ -1003,6 +1003,8 @@ struct azu_tracker {
     float* d_est = nullptr;   // 16 estimate, 16 ref, 16 prev
     azu_icp_result* d_result = nullptr;
     float* d_build = nullptr;
+    void* d_many = nullptr;   // track_many: estimates, refs and results
+    size_t many_cap = 0;
 };
 
 namespace azu {
@@ -1034,7 +1036,13 @@ static int alloc_levels(azu_tracker* t, int W, int H) {
 }
 
 // Fills the launch arguments; the caller sets pose pointers and outputs.
+static void fill_args_p(azu_tracker* t, const azu_tracker_params& p, IcpArgs& a, const float* mv, const float* mn,
+                        int MW, int MH);
 static void fill_args(azu_tracker* t, IcpArgs& a, const float* mv, const float* mn, int MW, int MH) {
+    fill_args_p(t, t->p, a, mv, mn, MW, MH);
+}
+static void fill_args_p(azu_tracker* t, const azu_tracker_params& p, IcpArgs& a, const float* mv, const float* mn,
+                        int MW, int MH) {
     std::memset(&a, 0, sizeof(a));
     for (int l = 0; l < 3; ++l) a.lv[l] = IcpLevel{t->V[l], t->N[l], t->W >> l, t->H >> l};
     a.mv = mv;
@@ -1042,7 +1050,6 @@ static void fill_args(azu_tracker* t, IcpArgs& a, const float* mv, const float* 
     a.MW = MW;
     a.MH = MH;
     // scaleIntrinsics (include/sensor/CameraIntrinsics.h:33-40) to the model size.
-    const azu_tracker_params& p = t->p;
     if (MW == 640 && MH == 480) {
         a.fx = p.fx; a.fy = p.fy; a.cx = p.cx; a.cy = p.cy;
     } else {
@@ -1140,6 +1147,7 @@ extern "C" int azu_tracker_destroy(azu_tracker* t) {
     cudaFree(t->ipartials);
     cudaFree(t->bar);
     cudaFree(t->d_est);
+    if (t->d_many) cudaFree(t->d_many);
     cudaFree(t->d_result);
     cudaFree(t->d_build);
     t->stream.release();
@@ -1192,6 +1200,56 @@ extern "C" int azu_tracker_track_prepared(azu_tracker* t, int width, int height,
         set_error("ICP grid barrier timed out");
         return AZU_E_TIMEOUT;
     }
+    return AZU_OK;
+}
+
+extern "C" int azu_tracker_track_many(azu_tracker* t, int width, int height, const float* d_model_vertices,
+                                      const float* d_model_normals, int model_w, int model_h, int count,
+                                      const float* estimates, const float* ref_poses,
+                                      const azu_tracker_params* params, azu_icp_result* out) {
+    AZU_CHECK_ARG(t != nullptr && d_model_vertices != nullptr && d_model_normals != nullptr && estimates != nullptr &&
+                      out != nullptr,
+                  "null argument");
+    AZU_CHECK_ARG(model_w > 0 && model_h > 0 && count >= 1 && count <= 4096, "model size / count");
+    if (!t->prepared || width != t->W || height != t->H) {
+        set_error("track_many called without a matching prepare_live");
+        return AZU_E_STATE;
+    }
+    AZU_TRY_CUDA(cudaSetDevice(t->device));
+    const azu_tracker_params p = params ? sanitize(*params) : t->p;
+    cudaStream_t s = t->stream.s;
+    if (static_cast<size_t>(count) > t->many_cap) {
+        AZU_TRY_CUDA(cudaStreamSynchronize(s));
+        if (t->d_many) cudaFree(t->d_many);
+        t->d_many = nullptr;
+        t->many_cap = 0;
+        AZU_TRY_CUDA(cudaMalloc(&t->d_many, count * (32 * sizeof(float) + sizeof(azu_icp_result))));
+        t->many_cap = count;
+    }
+    float* d_est = reinterpret_cast<float*>(t->d_many);
+    float* d_ref = d_est + 16 * count;
+    azu_icp_result* d_res = reinterpret_cast<azu_icp_result*>(d_est + 32 * count);
+    AZU_TRY_CUDA(cudaMemcpyAsync(d_est, estimates, 16 * count * sizeof(float), cudaMemcpyHostToDevice, s));
+    AZU_TRY_CUDA(cudaMemcpyAsync(d_ref, ref_poses ? ref_poses : estimates, 16 * count * sizeof(float),
+                                 cudaMemcpyHostToDevice, s));
+    const size_t img = static_cast<size_t>(model_w) * model_h * 3;
+    for (int k = 0; k < count; ++k) {
+        IcpArgs a;
+        fill_args_p(t, p, a, d_model_vertices + img * k, d_model_normals + img * k, model_w, model_h);
+        a.d_estimate = d_est + 16 * k;
+        a.d_ref = d_ref + 16 * k;
+        a.d_result = d_res + k;
+        if (int rc = icp_launch(t, a, s)) return rc;
+    }
+    AZU_TRY_CUDA(cudaMemcpyAsync(out, d_res, count * sizeof(azu_icp_result), cudaMemcpyDeviceToHost, s));
+    AZU_TRY_CUDA(cudaStreamSynchronize(s));
+    for (int k = 0; k < count; ++k)
+        if (out[k].status == AZU_E_TIMEOUT) {
+            unsigned z = 0;
+            cudaMemcpy(t->bar + 2, &z, sizeof(z), cudaMemcpyHostToDevice);
+            set_error("ICP grid barrier timed out");
+            return AZU_E_TIMEOUT;
+        }
     return AZU_OK;
 }
 

@@ -743,6 +743,94 @@ __global__ void __launch_bounds__(256) raycast_kernel(VolView v, const float* __
                          nb, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
 }
 
+// ---- global point cloud (TSDFVolume.cpp:571-632) --------------------------------
+// Voxels with weight > 1 and |tsdf| < 0.2 whose colour quantises (a non-finite
+// colour skips the voxel), in index order z, y, x — the order of the
+// reference's loop run on one thread. Two passes over fixed 1024-voxel blocks:
+// count, then (after an exclusive scan of the block counts) emit at the block's
+// offset plus the thread's prefix, so the output order is deterministic.
+constexpr int kPcThreads = 256, kPcPerThread = 4, kPcBlock = kPcThreads * kPcPerThread;
+
+template <bool kHalf>
+__device__ __forceinline__ bool pc_take(const void* vox, const float* color, size_t i, uint8_t q[3]) {
+    const float2 r = Vox<kHalf>::load(vox, i);
+    if (!(r.y > 1.0f && fabsf(r.x) < 0.2f)) return false;
+    const float cr = color ? color[3 * i] : kEmptyColor;
+    const float cg = color ? color[3 * i + 1] : kEmptyColor;
+    const float cb = color ? color[3 * i + 2] : kEmptyColor;
+    return srgb_to_byte(cr, &q[0]) && srgb_to_byte(cg, &q[1]) && srgb_to_byte(cb, &q[2]);
+}
+
+// Block-wide exclusive prefix of one int per thread; returns the block total.
+__device__ __forceinline__ int block_exclusive(int v, int* s_warp, int& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < (kPcThreads / 32) ? s_warp[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < (kPcThreads / 32)) s_warp[lane] = w;  // inclusive warp sums
+    }
+    __syncthreads();
+    total = s_warp[kPcThreads / 32 - 1];
+    const int before = warp > 0 ? s_warp[warp - 1] : 0;
+    __syncthreads();
+    return before + incl - v;
+}
+
+template <bool kHalf>
+__global__ void __launch_bounds__(kPcThreads) pc_count_kernel(const void* vox, const float* color, size_t n,
+                                                             int* block_counts) {
+    __shared__ int s_warp[kPcThreads / 32];
+    const size_t base = static_cast<size_t>(blockIdx.x) * kPcBlock + static_cast<size_t>(threadIdx.x) * kPcPerThread;
+    int c = 0;
+    uint8_t q[3];
+    for (int k = 0; k < kPcPerThread; ++k)
+        if (base + k < n && pc_take<kHalf>(vox, color, base + k, q)) ++c;
+    int total = 0;
+    block_exclusive(c, s_warp, total);
+    if (threadIdx.x == 0) block_counts[blockIdx.x] = total;
+}
+
+template <bool kHalf>
+__global__ void __launch_bounds__(kPcThreads) pc_emit_kernel(const void* vox, const float* color, size_t n, int res,
+                                                            float vs, F3 origin, const long long* block_offsets,
+                                                            float* points, uint8_t* colors) {
+    __shared__ int s_warp[kPcThreads / 32];
+    const size_t base = static_cast<size_t>(blockIdx.x) * kPcBlock + static_cast<size_t>(threadIdx.x) * kPcPerThread;
+    bool take[kPcPerThread];
+    uint8_t q[kPcPerThread][3];
+    int c = 0;
+    for (int k = 0; k < kPcPerThread; ++k) {
+        take[k] = base + k < n && pc_take<kHalf>(vox, color, base + k, q[k]);
+        c += take[k];
+    }
+    int total = 0;
+    long long o = block_offsets[blockIdx.x] + block_exclusive(c, s_warp, total);
+    const size_t rr = static_cast<size_t>(res);
+    for (int k = 0; k < kPcPerThread; ++k) {
+        if (!take[k]) continue;
+        const size_t i = base + k;
+        const int x = static_cast<int>(i % rr), y = static_cast<int>((i / rr) % rr), z = static_cast<int>(i / rr / rr);
+        // voxelToWorld (TSDFVolume.cpp:555-561): origin + (x, y, z) * vs
+        points[3 * o] = fa(origin.x, fm(static_cast<float>(x), vs));
+        points[3 * o + 1] = fa(origin.y, fm(static_cast<float>(y), vs));
+        points[3 * o + 2] = fa(origin.z, fm(static_cast<float>(z), vs));
+        colors[3 * o] = q[k][0];
+        colors[3 * o + 1] = q[k][1];
+        colors[3 * o + 2] = q[k][2];
+        ++o;
+    }
+}
+
 static int ensure_tiles(azu_volume* v, size_t n, cudaStream_t s);
 
 // ---- batches: several volumes, one launch per stage --------------------------
@@ -977,6 +1065,20 @@ int volume_batch_raycast(azu_volume_batch* b, cudaStream_t s) {
     raycast_batch_kernel<<<b->ray_blocks, dim3(b->ray_w, b->ray_h), 0, s>>>(b->d_ray, b->d_off + 3 * (n + 1), n);
     AZU_LAUNCH_CHECK();
     return AZU_OK;
+}
+
+// Many model images at once (the relocaliser's candidate renders): one launch,
+// blockIdx.z = pose; every image is the single raycast's bit for bit.
+template <bool kHalf>
+__global__ void __launch_bounds__(256) raycast_many_kernel(VolView v, const float* __restrict__ d_poses, float fx,
+                                                          float fy, float cx, float cy, int W, int H, float trunc,
+                                                          float min_depth, float max_depth, float* __restrict__ vout,
+                                                          float* __restrict__ nout,
+                                                          const uint8_t* __restrict__ bdist, int nb) {
+    const size_t img = static_cast<size_t>(W) * H * 3 * blockIdx.z;
+    raycast_pixel<kHalf>(v, d_poses + 16 * blockIdx.z, fx, fy, cx, cy, W, H, trunc, min_depth, max_depth, vout + img,
+                         nout + img, nullptr, nullptr, bdist, nb, blockIdx.x * blockDim.x + threadIdx.x,
+                         blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 // ---- whole-volume transfers -------------------------------------------------
@@ -1342,3 +1444,110 @@ extern "C" int azu_volume_set_free_space_skipping(azu_volume* v, int on) {
 }
 
 extern "C" void* azu_volume_device_voxels(azu_volume* v) { return v ? v->vox : nullptr; }
+
+extern "C" int azu_volume_point_cloud(azu_volume* v, float* h_points, uint8_t* h_colors, int64_t capacity,
+                                      int64_t* n_points) {
+    AZU_CHECK_ARG(v != nullptr && n_points != nullptr, "null argument");
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    cudaStream_t s = v->stream.s;
+    const size_t n = static_cast<size_t>(v->p.resolution) * v->p.resolution * v->p.resolution;
+    const size_t nblocks = (n + kPcBlock - 1) / kPcBlock;
+    const bool half = v->p.format != AZU_TSDF_FP32;
+    int* d_counts = nullptr;
+    long long* d_off = nullptr;
+    float* d_pts = nullptr;
+    uint8_t* d_col = nullptr;
+    int rc = AZU_OK;
+    std::vector<int> counts(nblocks);
+    std::vector<long long> off(nblocks);
+    long long total = 0;
+    auto fail = [&](cudaError_t e) {
+        set_error("point cloud: %s", cudaGetErrorString(e));
+        rc = e == cudaErrorMemoryAllocation ? AZU_E_NOMEM : AZU_E_CUDA;
+    };
+    cudaError_t e = cudaMalloc(&d_counts, nblocks * sizeof(int));
+    if (!e) e = cudaMalloc(&d_off, nblocks * sizeof(long long));
+    if (!e) {
+        if (half) pc_count_kernel<true><<<static_cast<unsigned>(nblocks), kPcThreads, 0, s>>>(v->vox, v->color, n, d_counts);
+        else pc_count_kernel<false><<<static_cast<unsigned>(nblocks), kPcThreads, 0, s>>>(v->vox, v->color, n, d_counts);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaMemcpyAsync(counts.data(), d_counts, nblocks * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (!e) e = cudaStreamSynchronize(s);
+    if (e) fail(e);
+    if (!rc) {
+        for (size_t b = 0; b < nblocks; ++b) { off[b] = total; total += counts[b]; }
+        *n_points = total;
+        if (h_points || h_colors) {
+            if (capacity < total) {
+                set_error("point cloud: %lld points, capacity %lld", total, static_cast<long long>(capacity));
+                rc = AZU_E_INVALID;
+            }
+        }
+    }
+    if (!rc && (h_points || h_colors) && total > 0) {
+        e = cudaMemcpyAsync(d_off, off.data(), nblocks * sizeof(long long), cudaMemcpyHostToDevice, s);
+        if (!e) e = cudaMalloc(&d_pts, static_cast<size_t>(total) * 3 * sizeof(float));
+        if (!e) e = cudaMalloc(&d_col, static_cast<size_t>(total) * 3);
+        const F3 org = mk3(v->p.origin[0], v->p.origin[1], v->p.origin[2]);
+        if (!e) {
+            if (half)
+                pc_emit_kernel<true><<<static_cast<unsigned>(nblocks), kPcThreads, 0, s>>>(
+                    v->vox, v->color, n, v->p.resolution, v->p.voxel_size, org, d_off, d_pts, d_col);
+            else
+                pc_emit_kernel<false><<<static_cast<unsigned>(nblocks), kPcThreads, 0, s>>>(
+                    v->vox, v->color, n, v->p.resolution, v->p.voxel_size, org, d_off, d_pts, d_col);
+            e = cudaGetLastError();
+        }
+        if (!e && h_points)
+            e = cudaMemcpyAsync(h_points, d_pts, static_cast<size_t>(total) * 3 * sizeof(float), cudaMemcpyDeviceToHost, s);
+        if (!e && h_colors) e = cudaMemcpyAsync(h_colors, d_col, static_cast<size_t>(total) * 3, cudaMemcpyDeviceToHost, s);
+        if (!e) e = cudaStreamSynchronize(s);
+        if (e) fail(e);
+    }
+    for (void* p : {(void*)d_counts, (void*)d_off, (void*)d_pts, (void*)d_col})
+        if (p) cudaFree(p);
+    return rc;
+}
+
+extern "C" int azu_volume_raycast_many(azu_volume* v, const float* poses, int count, float fx, float fy, float cx,
+                                       float cy, int width, int height, float* d_vertices, float* d_normals) {
+    AZU_CHECK_ARG(v != nullptr && poses != nullptr && d_vertices != nullptr && d_normals != nullptr, "null argument");
+    AZU_CHECK_ARG(count >= 1 && count <= 65535 && width > 0 && height > 0, "count / image size");
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    cudaStream_t s = v->stream.s;
+    float* d_poses = nullptr;
+    AZU_TRY_CUDA(cudaMalloc(&d_poses, 16 * sizeof(float) * count));
+    cudaError_t e = cudaMemcpyAsync(d_poses, poses, 16 * sizeof(float) * count, cudaMemcpyHostToDevice, s);
+    const azu_volume_params& p = v->p;
+    const VolView view = make_view(v);
+    const uint8_t* bricks = nullptr;
+    if (!e && v->skip_free) {
+        const size_t nbr = static_cast<size_t>(v->nb) * v->nb * v->nb;
+        const unsigned g = static_cast<unsigned>((nbr + 255) / 256);
+        brick_dist_kernel<<<g, 256, 0, s>>>(v->bricks, v->brick_dist, v->nb, 0, 1, nullptr);
+        brick_dist_kernel<<<g, 256, 0, s>>>(v->brick_dist, v->brick_tmp, v->nb, 1, 0, nullptr);
+        brick_dist_kernel<<<g, 256, 0, s>>>(v->brick_tmp, v->brick_dist, v->nb, 2, 0, nullptr);
+        e = cudaGetLastError();
+        bricks = v->brick_dist;
+    }
+    if (!e) {
+        const dim3 blk(32, 8), grd((width + 31) / 32, (height + 7) / 8, count);
+        if (p.format != AZU_TSDF_FP32)
+            raycast_many_kernel<true><<<grd, blk, 0, s>>>(view, d_poses, fx, fy, cx, cy, width, height, p.truncation,
+                                                          p.min_depth, p.max_depth, d_vertices, d_normals, bricks,
+                                                          v->nb);
+        else
+            raycast_many_kernel<false><<<grd, blk, 0, s>>>(view, d_poses, fx, fy, cx, cy, width, height,
+                                                           p.truncation, p.min_depth, p.max_depth, d_vertices,
+                                                           d_normals, bricks, v->nb);
+        e = cudaGetLastError();
+    }
+    if (!e) e = cudaStreamSynchronize(s);
+    cudaFree(d_poses);
+    if (e) {
+        set_error("raycast_many: %s", cudaGetErrorString(e));
+        return AZU_E_CUDA;
+    }
+    return AZU_OK;
+}

@@ -132,6 +132,23 @@ int azu_volume_set_free_space_skipping(azu_volume* v, int on);
  * {tsdf, weight} for FP32, uint32 {half, u16} for FP16). */
 void* azu_volume_device_voxels(azu_volume* v);
 
+/* The relocaliser's candidate renders (PipelineController::renderModel,
+ * src/app/PipelineController.cpp:619-657, called per candidate by
+ * tracking::Relocalizer, include/tracking/Relocalizer.h): count raycasts of
+ * this volume at the host poses (16 floats each) into device images
+ * d_vertices / d_normals of count * width * height * 3 floats, in one launch;
+ * each image equals azu_volume_raycast's at that pose. Intrinsics are those of
+ * the render size (the caller scales them, as scaleIntrinsics does). */
+int azu_volume_raycast_many(azu_volume* v, const float* poses, int count, float fx, float fy, float cx, float cy,
+                            int width, int height, float* d_vertices, float* d_normals);
+
+/* TSDFVolume::extractGlobalPointCloud (TSDFVolume.cpp:571-632): voxels with
+ * weight > 1 and |tsdf| < 0.2 whose colour quantises, in index order (z, y, x),
+ * as world positions origin + (x, y, z) * voxel_size (3 floats) and sRGB bytes
+ * (3 per point; 128 grey without colour). With h_points and h_colors NULL only
+ * the count is returned; else capacity (points) must hold them all. */
+int azu_volume_point_cloud(azu_volume* v, float* h_points, uint8_t* h_colors, int64_t capacity, int64_t* n_points);
+
 /* ---- differentiation form (no counterpart in the reference) ------------ */
 /* Depth image of the raycast at `pose` (camera z of the hit, metres; 0 where
  * the raycast returns no vertex): d_depth is a device float[width*height]. */
@@ -205,6 +222,17 @@ int azu_tracker_prepare_live(azu_tracker* t, const float* d_depth_m, int width, 
 int azu_tracker_track_prepared(azu_tracker* t, int width, int height, const float* d_model_vertices,
                                const float* d_model_normals, int model_w, int model_h, const float estimate[16],
                                const float ref_pose[16], azu_icp_result* out);
+/* The relocaliser's candidate scoring (Relocalizer's solve hook, i.e.
+ * ICPTracker::trackPreparedGPU, include/tracking/ICPTracker.h:104-113, once
+ * per candidate): count solves of the prepared live frame, solve k against
+ * model image k (model_w * model_h * 3 floats apart in d_model_vertices /
+ * d_model_normals) from estimates[k] with reference pose ref_poses[k] (NULL:
+ * the estimates), with `params` (NULL: the tracker's) — e.g. the coarse
+ * stage's level-2-only iterations and wider gates. Launched back to back on
+ * the tracker's stream; results (count, host) are read back once. */
+int azu_tracker_track_many(azu_tracker* t, int width, int height, const float* d_model_vertices,
+                           const float* d_model_normals, int model_w, int model_h, int count, const float* estimates,
+                           const float* ref_poses, const azu_tracker_params* params, azu_icp_result* out);
 /* trackGPU (ICPTracker.h:94-100) = prepare_live + track_prepared. */
 int azu_tracker_track(azu_tracker* t, const float* d_depth_m, int width, int height, const float* d_model_vertices,
                       const float* d_model_normals, int model_w, int model_h, const float estimate[16],

@@ -137,6 +137,16 @@ class Volume:
             out["colors"] = c.reshape(H, W, 3)
         return out
 
+    def point_cloud(self):
+        L = lib()
+        L.orc_point_cloud.restype = C.c_int64
+        n = L.orc_point_cloud(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.color), None, None)
+        pts = np.zeros((max(n, 1), 3), np.float32)
+        col = np.zeros((max(n, 1), 3), np.uint8)
+        L.orc_point_cloud(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.color), _p(pts),
+                          _p(col, C.c_uint8))
+        return pts[:n], col[:n]
+
     def extract_mesh(self, max_triangles=2_000_000):
         info = MeshInfo()
         lib().orc_mc_extract(C.byref(self.p), _p(self.tsdf), _p(self.weight), _p(self.color),

@@ -173,6 +173,11 @@ void orc_depth_loss_d(const orc_tsdf_params* p, const double* tsdf, const float*
                       double huber_delta, double* loss, double grad_xi[6], double* grad_tsdf, double* depth_out,
                       double* jac_out, int* n_valid);
 
+/* TSDFVolume::extractGlobalPointCloud (TSDFVolume.cpp:571-632), one thread:
+ * index order z, y, x. Returns the count; pts / cols (3 per point) may be NULL. */
+int64_t orc_point_cloud(const orc_tsdf_params* p, const float* tsdf, const float* weight, const float* color,
+                        float* pts, uint8_t* cols);
+
 #ifdef __cplusplus
 }
 #endif

@@ -382,3 +382,40 @@ extern "C" void orc_tsdf_integrate_prec(const orc_tsdf_params* p, float* tsdf, f
         }
     }
 }
+
+// TSDFVolume::extractGlobalPointCloud (src/tsdf/TSDFVolume.cpp:571-632) on one
+// thread, i.e. in index order z, y, x: voxels with weight > 1 and |tsdf| < 0.2
+// whose colour quantises; world position voxelToWorld (:555-561). Returns the
+// count; fills pts / cols (3 per point) when non-null.
+extern "C" int64_t orc_point_cloud(const orc_tsdf_params* p, const float* tsdf, const float* weight,
+                                   const float* color, float* pts, uint8_t* cols) {
+    const int res = p->res;
+    const V3 origin = originOf(p);
+    int64_t n = 0;
+    for (int z = 0; z < res; ++z)
+        for (int y = 0; y < res; ++y)
+            for (int x = 0; x < res; ++x) {
+                const size_t i = (static_cast<size_t>(z) * res + y) * res + x;
+                if (!(weight[i] > 1.0f && std::fabs(tsdf[i]) < 0.2f)) continue;
+                uint8_t qc[3] = {0, 0, 0};
+                const float r = color ? color[3 * i] : kEmptyColor;
+                const float g = color ? color[3 * i + 1] : kEmptyColor;
+                const float b = color ? color[3 * i + 2] : kEmptyColor;
+                if (!srgbFloatToUint8(r, qc[0]) || !srgbFloatToUint8(g, qc[1]) || !srgbFloatToUint8(b, qc[2]))
+                    continue;
+                if (pts) {
+                    const V3 w = origin + V3(static_cast<float>(x), static_cast<float>(y), static_cast<float>(z)) *
+                                              p->voxel_size;
+                    pts[3 * n] = w.x;
+                    pts[3 * n + 1] = w.y;
+                    pts[3 * n + 2] = w.z;
+                }
+                if (cols) {
+                    cols[3 * n] = qc[0];
+                    cols[3 * n + 1] = qc[1];
+                    cols[3 * n + 2] = qc[2];
+                }
+                ++n;
+            }
+    return n;
+}
