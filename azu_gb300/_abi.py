@@ -155,6 +155,10 @@ SIGNATURES = {
     "azu_pipeline_set_profiling": (C.c_int, [vp, C.c_int]),
     "azu_pipeline_stage_times": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "azu_pipeline_uses_graph": (C.c_int, [vp]),
+    # export
+    "azu_mesh_write_ply": (C.c_int, [C.c_char_p, C.c_int, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp,
+                                     C.c_int64]),
+    "azu_mesh_write_glb": (C.c_int, [C.c_char_p, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64]),
     # batch
     "azu_batch_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(BatchScene), C.POINTER(vp)]),
     "azu_batch_destroy": (C.c_int, [vp]),

@@ -563,3 +563,31 @@ class Batch:
     @property
     def stream(self):
         return self.lib.azu_batch_stream(self.h)
+
+
+def _mesh_args(mesh):
+    pos = np.ascontiguousarray(mesh["positions"], np.float32).reshape(-1, 3)
+    nrm = mesh.get("normals")
+    nrm = None if nrm is None or len(nrm) == 0 else np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+    col = mesh.get("colors")
+    col = None if col is None or len(col) == 0 else np.ascontiguousarray(col, np.uint8).reshape(-1)
+    idx = np.ascontiguousarray(mesh["indices"], np.uint32).reshape(-1)
+    keep = (pos, nrm, col, idx)
+    args = (pos.ctypes.data_as(C.c_void_p), len(pos),
+            None if nrm is None else nrm.ctypes.data_as(C.c_void_p), 0 if nrm is None else len(nrm),
+            None if col is None else col.ctypes.data_as(C.c_void_p), 0 if col is None else col.size,
+            idx.ctypes.data_as(C.c_void_p), idx.size)
+    return keep, args
+
+
+def write_ply(path: str, mesh: dict, binary: bool = True):
+    """PLYExporter (binary little endian or ASCII) of a mesh dict (positions,
+    normals, colors, indices)."""
+    keep, args = _mesh_args(mesh)
+    check(_abi.load().azu_mesh_write_ply(str(path).encode(), int(bool(binary)), *args), "write_ply")
+
+
+def write_glb(path: str, mesh: dict):
+    """GLBExporter of a mesh dict."""
+    keep, args = _mesh_args(mesh)
+    check(_abi.load().azu_mesh_write_glb(str(path).encode(), *args), "write_glb")

@@ -398,6 +398,26 @@ int azu_pipeline_stage_times(azu_pipeline* p, double ms_total[5], int* frames);
 int azu_pipeline_uses_graph(azu_pipeline* p);
 
 /* ------------------------------------------------------------------------ */
+/* Mesh export (host code; src/export/PLYExporter.cpp, GLBExporter.cpp).       */
+/* The mesh is the mesher's MeshData: positions (3 floats per vertex),         */
+/* optional normals (n_normals vertices: 0 or n_vertices), optional sRGB        */
+/* colours (n_color_bytes: 0 or 3 n_vertices) and triangle indices. It is        */
+/* validated with MeshData::validate's rules (include/meshing/MeshData.h:49-95)  */
+/* before any file is opened; a rejected mesh creates no file.                   */
+/* ------------------------------------------------------------------------ */
+
+/* PLYExporter::writeBinary / writeASCII: the reference's bytes. */
+int azu_mesh_write_ply(const char* path, int binary, const float* positions, int64_t n_vertices, const float* normals,
+                       int64_t n_normals, const uint8_t* colors, int64_t n_color_bytes, const uint32_t* indices,
+                       int64_t n_indices);
+/* GLBExporter::write: vertices welded by exact position, glTF axes (x, -y, -z),
+ * unit normals (fallback (0, 0, -1)), linear RGBA float colours, 4-byte
+ * aligned [positions | normals | colours | indices] binary chunk. */
+int azu_mesh_write_glb(const char* path, const float* positions, int64_t n_vertices, const float* normals,
+                       int64_t n_normals, const uint8_t* colors, int64_t n_color_bytes, const uint32_t* indices,
+                       int64_t n_indices);
+
+/* ------------------------------------------------------------------------ */
 /* Batching form (no counterpart in the reference): many independent scenes,   */
 /* each with its own volume, image size and frame count, advanced together.   */
 /* ------------------------------------------------------------------------ */
