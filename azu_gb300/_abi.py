@@ -155,6 +155,18 @@ SIGNATURES = {
     "azu_pipeline_set_profiling": (C.c_int, [vp, C.c_int]),
     "azu_pipeline_stage_times": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "azu_pipeline_uses_graph": (C.c_int, [vp]),
+    # ingest
+    "azu_recording_open": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+    "azu_recording_close": (None, [vp]),
+    "azu_recording_frame_count": (C.c_int, [vp]),
+    "azu_recording_frame_info": (C.c_int, [vp, C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                           C.POINTER(C.c_int)]),
+    "azu_recording_read": (C.c_int, [vp, C.c_int, vp, vp, C.POINTER(C.c_int)]),
+    "azu_ingest_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]),
+    "azu_ingest_destroy": (C.c_int, [vp]),
+    "azu_ingest_next": (C.c_int, [vp, C.POINTER(vp), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "azu_ingest_release": (C.c_int, [vp]),
+    "azu_pipeline_process_frame_packed": (C.c_int, [vp, vp, C.POINTER(FrameResult)]),
     # export
     "azu_mesh_write_ply": (C.c_int, [C.c_char_p, C.c_int, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp,
                                      C.c_int64]),

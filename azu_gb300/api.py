@@ -456,6 +456,13 @@ class Pipeline:
                                                   C.byref(r)), "process_frame")
         return self._frame(r)
 
+    def process_frame_packed(self, h_packed_ptr: int) -> dict:
+        """One frame from a packed host slot (depth | RGB) with one host-to-device copy."""
+        r = _abi.FrameResult()
+        check(self.lib.azu_pipeline_process_frame_packed(self.h, C.c_void_p(h_packed_ptr), C.byref(r)),
+              "process_frame_packed")
+        return self._frame(r)
+
     def process_frame_device(self, d_depth_ptr: int, d_rgb_ptr: int | None = None, sync: bool = False):
         """One frame from device buffers; only enqueued unless sync."""
         r = _abi.FrameResult() if sync else None
@@ -591,3 +598,68 @@ def write_glb(path: str, mesh: dict):
     """GLBExporter of a mesh dict."""
     keep, args = _mesh_args(mesh)
     check(_abi.load().azu_mesh_write_glb(str(path).encode(), *args), "write_glb")
+
+
+class Recording:
+    """A fakenect recording directory (INDEX.txt + PGM depth / PPM RGB), paired
+    like the sensor pairs live frames."""
+
+    def __init__(self, path: str):
+        self.lib = _abi.load()
+        self.h = C.c_void_p()
+        check(self.lib.azu_recording_open(str(path).encode(), C.byref(self.h)), "azu_recording_open")
+
+    def close(self):
+        if self.h:
+            self.lib.azu_recording_close(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        _finalize(self)
+
+    def __len__(self):
+        return self.lib.azu_recording_frame_count(self.h)
+
+    def info(self, k):
+        d, r, v = C.c_uint32(), C.c_uint32(), C.c_int()
+        check(self.lib.azu_recording_frame_info(self.h, k, C.byref(d), C.byref(r), C.byref(v)), "frame_info")
+        return d.value, (r.value if v.value else None)
+
+    def read(self, k):
+        depth = np.empty((480, 640), np.uint16)
+        rgb = np.empty((480, 640, 3), np.uint8)
+        v = C.c_int()
+        check(self.lib.azu_recording_read(self.h, k, depth.ctypes.data_as(C.c_void_p), rgb.ctypes.data_as(C.c_void_p),
+                                          C.byref(v)), "recording_read")
+        return depth, rgb, bool(v.value)
+
+
+class Ingest:
+    """Read-ahead of a recording into pinned slots (depth | RGB per slot)."""
+
+    def __init__(self, rec: Recording, slots=4, first=0, count=None):
+        self.lib = _abi.load()
+        self.rec = rec
+        self.h = C.c_void_p()
+        n = len(rec) - first if count is None else count
+        check(self.lib.azu_ingest_create(rec.h, int(slots), int(first), int(n), C.byref(self.h)), "ingest_create")
+
+    def close(self):
+        if self.h:
+            self.lib.azu_ingest_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        _finalize(self)
+
+    def next(self):
+        """(slot pointer, frame index, rgb_valid), or None at the end."""
+        slot, k, v = C.c_void_p(), C.c_int(), C.c_int()
+        rc = self.lib.azu_ingest_next(self.h, C.byref(slot), C.byref(k), C.byref(v))
+        if rc == 1:
+            return None
+        check(rc, "ingest_next")
+        return slot.value, k.value, bool(v.value)
+
+    def release(self):
+        check(self.lib.azu_ingest_release(self.h), "ingest_release")

@@ -94,6 +94,7 @@ struct azu_pipeline {
     azu_icp_result* d_icp = nullptr;
     int frames = 0;
     int W = 640, H = 480;
+    uint8_t* d_packed = nullptr;  // one frame's depth | rgb, for the single-copy input
     bool own_stream = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -268,7 +269,7 @@ extern "C" int azu_pipeline_destroy(azu_pipeline* pl) {
     azu_tracker_destroy(pl->trk);
     azu_volume_destroy(pl->vol);
     for (void* q : {(void*)pl->d_in, (void*)pl->d_depth_m, (void*)pl->d_model_v, (void*)pl->d_model_n,
-                    (void*)pl->d_st, (void*)pl->d_icp})
+                    (void*)pl->d_st, (void*)pl->d_icp, (void*)pl->d_packed})
         if (q) cudaFree(q);
     for (cudaEvent_t e : pl->ev) if (e) cudaEventDestroy(e);
     if (pl->s && pl->own_stream) cudaStreamDestroy(pl->s);
@@ -354,6 +355,21 @@ extern "C" int azu_pipeline_process_frame_device(azu_pipeline* pl, const uint16_
     if (int rc = run_frame(pl)) return rc;
     if (out) return pipeline_read_result(pl, out);
     return AZU_OK;
+}
+
+extern "C" int azu_pipeline_process_frame_packed(azu_pipeline* pl, const void* h_packed, azu_frame_result* out) {
+    AZU_CHECK_ARG(pl != nullptr && h_packed != nullptr && out != nullptr, "null argument");
+    AZU_TRY_CUDA(cudaSetDevice(pl->device));
+    const size_t n = static_cast<size_t>(pl->W) * pl->H;
+    const size_t bytes = n * (pl->p.input_is_mm ? 2 : 5);
+    if (!pl->d_packed) AZU_TRY_CUDA(cudaMalloc(&pl->d_packed, n * 5));
+    // the one host-to-device copy of the frame; the split happens on the device
+    AZU_TRY_CUDA(cudaMemcpyAsync(pl->d_packed, h_packed, bytes, cudaMemcpyHostToDevice, pl->s));
+    const uint16_t* d_depth = reinterpret_cast<const uint16_t*>(pl->d_packed);
+    const uint8_t* d_rgb = pl->p.input_is_mm ? nullptr : pl->d_packed + n * 2;
+    if (int rc = pipeline_upload_inputs(pl, d_depth, d_rgb, cudaMemcpyDeviceToDevice)) return rc;
+    if (int rc = run_frame(pl)) return rc;
+    return pipeline_read_result(pl, out);
 }
 
 extern "C" int azu_pipeline_last_result(azu_pipeline* pl, azu_frame_result* out) {

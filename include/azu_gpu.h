@@ -398,6 +398,36 @@ int azu_pipeline_stage_times(azu_pipeline* p, double ms_total[5], int* frames);
 int azu_pipeline_uses_graph(azu_pipeline* p);
 
 /* ------------------------------------------------------------------------ */
+/* Sensor-side ingest (host code): fakenect recordings                         */
+/* (tools/FakenectRecording.h:35-81) paired like KinectSensor::onDepth/onRgb    */
+/* (src/sensor/KinectSensor.cpp:262-362: depth-led, nearest RGB within 17 ms    */
+/* of the 60 MHz counter, else depth-only; a depth frame still waiting at the    */
+/* end is published depth-only), read ahead into a ring of pinned slots.        */
+/* ------------------------------------------------------------------------ */
+
+typedef struct azu_recording azu_recording;
+typedef struct azu_ingest azu_ingest;
+
+int azu_recording_open(const char* dir, azu_recording** out);
+void azu_recording_close(azu_recording* r);
+int azu_recording_frame_count(const azu_recording* r);
+int azu_recording_frame_info(const azu_recording* r, int k, uint32_t* depth_ticks, uint32_t* rgb_ticks,
+                             int* rgb_valid);
+/* Frame k's raw depth (640x480 uint16) and RGB (640x480x3, zeros without). */
+int azu_recording_read(const azu_recording* r, int k, uint16_t* depth, uint8_t* rgb, int* rgb_valid);
+/* A reader thread fills `slots` pinned slots (depth then RGB, back to back)
+ * with frames first .. first+count-1 in order. */
+int azu_ingest_create(azu_recording* rec, int slots, int first, int count, azu_ingest** out);
+int azu_ingest_destroy(azu_ingest* g);
+/* The next frame's slot (blocks until read); 1 at the end of the range. */
+int azu_ingest_next(azu_ingest* g, const void** slot, int* frame_index, int* rgb_valid);
+/* Hands the oldest consumed slot back to the reader. */
+int azu_ingest_release(azu_ingest* g);
+/* One frame from a packed host buffer (depth then RGB, as an ingest slot) with
+ * a single host-to-device copy; otherwise as azu_pipeline_process_frame. */
+int azu_pipeline_process_frame_packed(azu_pipeline* p, const void* h_packed, azu_frame_result* out);
+
+/* ------------------------------------------------------------------------ */
 /* Mesh export (host code; src/export/PLYExporter.cpp, GLBExporter.cpp).       */
 /* The mesh is the mesher's MeshData: positions (3 floats per vertex),         */
 /* optional normals (n_normals vertices: 0 or n_vertices), optional sRGB        */
