@@ -150,3 +150,42 @@ def test_mesh_fused_sequence(cuda_lib, orc):
     om = o.extract_mesh()
     assert len(om["indices"]) > 30000
     _mesh_equal(gm, om)
+
+
+def test_mesh_ragged_tiles_and_cap(cuda_lib, orc):
+    """A resolution that fills no classify tile evenly, an off-centre sphere
+    touching the volume's faces, and a cap that falls inside a 256-cube block."""
+    from azu_gb300 import api
+    t, w, prm = F.sphere_volume(res=77, vs=0.02, radius=0.55, trunc=0.06, center=0.5)
+    w = w.copy()
+    w[::97] = 0.0  # scattered unobserved voxels
+    o = orc.Volume(orc.tsdf_params(**prm))
+    o.tsdf[:] = t
+    o.weight[:] = w
+    full = o.extract_mesh()
+    assert len(full["indices"]) // 3 > 10000
+    g = _vol_from(prm, t, w)
+    _mesh_equal(api.MarchingCubes().extract(g), full)
+    cap = len(full["indices"]) // 3 // 2 + 3
+    _mesh_equal(api.MarchingCubes(max_triangles=cap).extract(g), o.extract_mesh(max_triangles=cap))
+
+
+def test_mesh_noise_volume_regrows_candidate_list(cuda_lib, orc):
+    """Random signs make nearly every cube a candidate: more than the first
+    candidate list holds, so the extraction grows it and runs again."""
+    from azu_gb300 import api
+    rng = np.random.default_rng(11)
+    res = 48
+    t = rng.uniform(-1, 1, res ** 3).astype(np.float32)
+    w = (rng.uniform(0, 1, res ** 3) > 0.1).astype(np.float32)
+    prm = dict(resolution=res, voxel_size=0.01, truncation=0.03, max_weight=64.0, origin=(0.1, -0.2, 0.3),
+               min_depth=0.3, max_depth=5.0)
+    o = orc.Volume(orc.tsdf_params(**prm))
+    o.tsdf[:] = t
+    o.weight[:] = w
+    om = o.extract_mesh()
+    assert len(om["indices"]) // 3 > 100000
+    mc = api.MarchingCubes()
+    g = _vol_from(prm, t, w)
+    _mesh_equal(mc.extract(g), om)
+    _mesh_equal(mc.extract(g), om)  # the grown list is reused
