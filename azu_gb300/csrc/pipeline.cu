@@ -12,8 +12,15 @@
 //              retries from prev; Good/Poor move cur, Failed keeps it
 //   integrate  only when the grade is Good (a device flag gates the kernels)
 //   raycast    the new model at cur (same gate)
-// Frames k > 0 replay one captured CUDA graph; host inputs and the result are
-// copied outside it.
+// A pipeline made by azu_pipeline_create runs the input and frame stages on a
+// second stream: frame k+1's upload, preprocessing and frame maps overlap
+// frame k's integrate and raycast (they only wait for frame k's tracking, and
+// the depth map alternates between two buffers), and a call that returns the
+// result returns once the pose is known, with the fusion of the frame still
+// running on the pipeline's stream. Each part replays its own captured CUDA
+// graph (frames k > 0); host inputs and the result are copied outside them.
+// Results are those of the strictly sequential schedule: every stage reads
+// what it read there.
 #include <cstring>
 
 #include "azu_internal.h"
@@ -98,6 +105,15 @@ struct azu_pipeline {
     bool own_stream = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // two-stream schedule (standalone pipelines)
+    cudaStream_t s2 = nullptr;                    // inputs, preprocessing, frame maps
+    cudaEvent_t ev_front = nullptr, ev_track = nullptr, ev_result = nullptr;
+    float* d_depth2[2] = {nullptr, nullptr};      // the frame's depth (metres), alternating
+    int buf = 0;
+    cudaGraph_t g_part[5] = {};                   // front[2], track, tail[2]
+    cudaGraphExec_t x_part[5] = {};
+    azu::PoseState* h_st = nullptr;               // pinned result staging
+    azu_icp_result* h_icp = nullptr;
     cudaEvent_t ev[6] = {};
     double stage_ms[5] = {0, 0, 0, 0, 0};
     int stage_frames = 0;
@@ -107,33 +123,51 @@ struct azu_pipeline {
 
 namespace azu {
 
+static bool two_streams(const azu_pipeline* pl) { return pl->s2 != nullptr; }
+static cudaStream_t front_stream(const azu_pipeline* pl) { return pl->s2 ? pl->s2 : pl->s; }
+
 static const float* depth_source(azu_pipeline* pl) {
+    if (two_streams(pl)) return pl->d_depth2[pl->buf];
     return pl->p.input_is_mm ? pl->d_depth_m : preprocess_depth_m(pl->pre);
 }
 
-static int mark(azu_pipeline* pl, int k) {
-    // External records stay ordinary, host-visible events when captured into the graph.
-    if (pl->profiling) AZU_TRY_CUDA(cudaEventRecordWithFlags(pl->ev[k], pl->s, cudaEventRecordExternal));
+static int mark(azu_pipeline* pl, int k, cudaStream_t s) {
+    if (!pl->profiling) return AZU_OK;
+    // External records stay ordinary, host-visible events when captured into a
+    // graph; outside a capture the record is a plain one.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    AZU_TRY_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusActive)
+        AZU_TRY_CUDA(cudaEventRecordWithFlags(pl->ev[k], s, cudaEventRecordExternal));
+    else
+        AZU_TRY_CUDA(cudaEventRecord(pl->ev[k], s));
     return AZU_OK;
 }
 
-// Front of one frame after the inputs are on the device: depth, frame maps,
-// prediction and tracking (or the first-frame pose).
-int pipeline_enqueue_front(azu_pipeline* pl, bool first) {
-    cudaStream_t s = pl->s;
+// Input stage: depth in metres (preprocessed Kinect codes or mm), then the
+// tracker's live frame maps.
+static int enqueue_input(azu_pipeline* pl, cudaStream_t s) {
     const azu_pipeline_params& P = pl->p;
     const float lo = P.min_depth, hi = P.max_depth;
     const int W = pl->W, H = pl->H;
-    if (int rc = mark(pl, 0)) return rc;
+    if (int rc = mark(pl, 0, s)) return rc;
     if (P.input_is_mm) {
-        if (int rc = mm_to_meters_enqueue(pl->d_in, pl->d_depth_m, W * H, lo, hi, s)) return rc;
+        float* out = two_streams(pl) ? pl->d_depth2[pl->buf] : pl->d_depth_m;
+        if (int rc = mm_to_meters_enqueue(pl->d_in, out, W * H, lo, hi, s)) return rc;
     } else {
         if (int rc = preprocess_enqueue(pl->pre, lo, hi, s)) return rc;
+        // the next frame's preprocessing overwrites the preprocessor's output
+        if (two_streams(pl))
+            AZU_TRY_CUDA(cudaMemcpyAsync(pl->d_depth2[pl->buf], preprocess_depth_m(pl->pre),
+                                         static_cast<size_t>(W) * H * 4, cudaMemcpyDeviceToDevice, s));
     }
-    if (int rc = mark(pl, 1)) return rc;
-    const float* dm = depth_source(pl);
-    if (int rc = tracker_prepare_dev(pl->trk, dm, W, H, s)) return rc;
-    if (int rc = mark(pl, 2)) return rc;
+    if (int rc = mark(pl, 1, s)) return rc;
+    if (int rc = tracker_prepare_dev(pl->trk, depth_source(pl), W, H, s)) return rc;
+    return mark(pl, 2, s);
+}
+
+// Prediction and tracking (or the first-frame pose).
+static int enqueue_track(azu_pipeline* pl, bool first, cudaStream_t s) {
     PoseState* st = pl->d_st;
     if (first) {
         first_frame_kernel<<<1, 32, 0, s>>>(st);
@@ -141,11 +175,18 @@ int pipeline_enqueue_front(azu_pipeline* pl, bool first) {
     } else {
         predict_kernel<<<1, 32, 0, s>>>(st);
         AZU_LAUNCH_CHECK();
-        if (int rc = tracker_track_dev(pl->trk, pl->d_model_v, pl->d_model_n, W, H, st->pred, st->model_pose,
+        if (int rc = tracker_track_dev(pl->trk, pl->d_model_v, pl->d_model_n, pl->W, pl->H, st->pred, st->model_pose,
                                        st->prev, st->cur, pl->d_icp, &st->quality, &st->gate, s))
             return rc;
     }
-    return mark(pl, 3);
+    return mark(pl, 3, s);
+}
+
+// Front of one frame after the inputs are on the device, on the pipeline's
+// stream: depth, frame maps, prediction and tracking.
+int pipeline_enqueue_front(azu_pipeline* pl, bool first) {
+    if (int rc = enqueue_input(pl, pl->s)) return rc;
+    return enqueue_track(pl, first, pl->s);
 }
 
 // The model commit that closes a frame (after the gated integrate + raycast).
@@ -162,54 +203,85 @@ PipelineFrameView pipeline_frame_view(azu_pipeline* pl) {
                              T.cx, T.cy, pl->p.min_depth, pl->p.max_depth, pl->d_model_v, pl->d_model_n};
 }
 
-// The work of one frame after the inputs are on the device.
-static int enqueue_frame(azu_pipeline* pl, bool first) {
-    cudaStream_t s = pl->s;
+// Gated integrate + raycast of the frame and the model commit.
+static int enqueue_tail(azu_pipeline* pl, cudaStream_t s) {
     const azu_pipeline_params& P = pl->p;
-    const float lo = P.min_depth, hi = P.max_depth;
-    const int W = pl->W, H = pl->H;
     const azu_tracker_params& T = P.tracker;
-    if (int rc = pipeline_enqueue_front(pl, first)) return rc;
-    const float* dm = depth_source(pl);
+    const int W = pl->W, H = pl->H;
     PoseState* st = pl->d_st;
-    if (int rc = volume_integrate_dev(pl->vol, dm, nullptr, st->cur, T.fx, T.fy, T.cx, T.cy, W, H, lo, hi, &st->gate, s))
+    if (int rc = volume_integrate_dev(pl->vol, depth_source(pl), nullptr, st->cur, T.fx, T.fy, T.cx, T.cy, W, H,
+                                      P.min_depth, P.max_depth, &st->gate, s))
         return rc;
-    if (int rc = mark(pl, 4)) return rc;
+    if (int rc = mark(pl, 4, s)) return rc;
     if (int rc = volume_raycast_dev(pl->vol, st->cur, T.fx, T.fy, T.cx, T.cy, W, H, pl->d_model_v, pl->d_model_n,
                                     nullptr, &st->gate, s))
         return rc;
     if (int rc = pipeline_enqueue_commit(pl)) return rc;
-    if (int rc = mark(pl, 5)) return rc;
+    return mark(pl, 5, s);
+}
+
+// Runs `enqueue` on stream s through the captured graph in (graph, exec),
+// capturing it on first use. A capture that fails turns graphs off for the
+// pipeline and runs the work eagerly (capture is an optimisation only).
+template <typename F>
+static int run_part(azu_pipeline* pl, cudaGraph_t& graph, cudaGraphExec_t& exec, cudaStream_t s, F enqueue) {
+    if (!pl->p.use_graph) return enqueue();
+    if (!exec) {
+        AZU_TRY_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue();
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(s, &g);
+        cudaError_t ei = cudaErrorUnknown;
+        if (!rc && e == cudaSuccess) ei = cudaGraphInstantiate(&exec, g, 0);
+        if (rc || e != cudaSuccess || ei != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            exec = nullptr;
+            cudaGetLastError();
+            pl->p.use_graph = 0;
+            pl->graph_failed = 1;
+            return enqueue();
+        }
+        graph = g;
+    }
+    AZU_TRY_CUDA(cudaGraphLaunch(exec, s));
     return AZU_OK;
 }
 
-static int run_frame(azu_pipeline* pl) {
+static int run_frame(azu_pipeline* pl, bool stage_result = false) {
     const bool first = pl->frames == 0;
-    if (first || !pl->p.use_graph) {
-        if (int rc = enqueue_frame(pl, first)) return rc;
-    } else {
-        if (!pl->exec) {
-            AZU_TRY_CUDA(cudaStreamBeginCapture(pl->s, cudaStreamCaptureModeThreadLocal));
-            const int rc = enqueue_frame(pl, false);
-            cudaGraph_t g = nullptr;
-            const cudaError_t e = cudaStreamEndCapture(pl->s, &g);
-            cudaError_t ei = cudaErrorUnknown;
-            if (!rc && e == cudaSuccess) ei = cudaGraphInstantiate(&pl->exec, g, 0);
-            if (rc || e != cudaSuccess || ei != cudaSuccess) {
-                // Capture is an optimisation only: run this and later frames eagerly.
-                if (g) cudaGraphDestroy(g);
-                pl->exec = nullptr;
-                cudaGetLastError();
-                pl->p.use_graph = 0;
-                pl->graph_failed = 1;
-                if (int rc2 = enqueue_frame(pl, false)) return rc2;
-                pl->frames++;
-                pl->vol->integrated_frames++;
-                return AZU_OK;
-            }
-            pl->graph = g;
+    if (two_streams(pl)) {
+        // input stage on s2 once frame k-1's tracking no longer needs the live
+        // maps (and frame k-2's fusion no longer needs this depth buffer)
+        const int b = pl->buf;
+        cudaStream_t s = pl->s, s2 = pl->s2;
+        AZU_TRY_CUDA(cudaStreamWaitEvent(s2, pl->ev_track, 0));
+        int rc = first ? enqueue_input(pl, s2)
+                       : run_part(pl, pl->g_part[b], pl->x_part[b], s2, [&] { return enqueue_input(pl, s2); });
+        if (rc) return rc;
+        AZU_TRY_CUDA(cudaEventRecord(pl->ev_front, s2));
+        AZU_TRY_CUDA(cudaStreamWaitEvent(s, pl->ev_front, 0));
+        rc = first ? enqueue_track(pl, true, s)
+                   : run_part(pl, pl->g_part[2], pl->x_part[2], s, [&] { return enqueue_track(pl, false, s); });
+        if (rc) return rc;
+        AZU_TRY_CUDA(cudaEventRecord(pl->ev_track, s));
+        if (stage_result) {
+            AZU_TRY_CUDA(cudaMemcpyAsync(pl->h_st, pl->d_st, sizeof(PoseState), cudaMemcpyDeviceToHost, s));
+            AZU_TRY_CUDA(cudaMemcpyAsync(pl->h_icp, pl->d_icp, sizeof(azu_icp_result), cudaMemcpyDeviceToHost, s));
+            AZU_TRY_CUDA(cudaEventRecord(pl->ev_result, s));
         }
-        AZU_TRY_CUDA(cudaGraphLaunch(pl->exec, pl->s));
+        rc = first ? enqueue_tail(pl, s)
+                   : run_part(pl, pl->g_part[3 + b], pl->x_part[3 + b], s, [&] { return enqueue_tail(pl, s); });
+        if (rc) return rc;
+        pl->buf ^= 1;
+    } else if (first || !pl->p.use_graph) {
+        if (int rc = pipeline_enqueue_front(pl, first)) return rc;
+        if (int rc = enqueue_tail(pl, pl->s)) return rc;
+    } else {
+        if (int rc = run_part(pl, pl->graph, pl->exec, pl->s, [&] {
+                if (int r = pipeline_enqueue_front(pl, false)) return r;
+                return enqueue_tail(pl, pl->s);
+            }))
+            return rc;
     }
     pl->frames++;
     pl->vol->integrated_frames++;
@@ -218,13 +290,43 @@ static int run_frame(azu_pipeline* pl) {
 
 int pipeline_upload_inputs(azu_pipeline* pl, const uint16_t* depth, const uint8_t* rgb, cudaMemcpyKind kind) {
     const size_t n = static_cast<size_t>(pl->W) * pl->H;
+    cudaStream_t s = front_stream(pl);
     if (pl->p.input_is_mm) {
-        AZU_TRY_CUDA(cudaMemcpyAsync(pl->d_in, depth, n * 2, kind, pl->s));
+        AZU_TRY_CUDA(cudaMemcpyAsync(pl->d_in, depth, n * 2, kind, s));
     } else {
-        AZU_TRY_CUDA(cudaMemcpyAsync(preprocess_input(pl->pre), depth, n * 2, kind, pl->s));
-        if (rgb) AZU_TRY_CUDA(cudaMemcpyAsync(preprocess_rgb_input(pl->pre), rgb, n * 3, kind, pl->s));
+        AZU_TRY_CUDA(cudaMemcpyAsync(preprocess_input(pl->pre), depth, n * 2, kind, s));
+        if (rgb) AZU_TRY_CUDA(cudaMemcpyAsync(preprocess_rgb_input(pl->pre), rgb, n * 3, kind, s));
     }
     return AZU_OK;
+}
+
+// The result of the frame just run with stage_result: it is known once the
+// tracking is done (integrated = the gate the fusion runs under), so this
+// waits for that point only.
+static int read_staged_result(azu_pipeline* pl, azu_frame_result* out) {
+    AZU_TRY_CUDA(cudaEventSynchronize(pl->ev_result));
+    const PoseState& st = *pl->h_st;
+    std::memcpy(out->pose, st.cur, sizeof(out->pose));
+    out->icp = *pl->h_icp;
+    out->quality = st.quality;
+    out->integrated = st.gate;
+    out->frame_index = st.frame_index;
+    if (st.quality == -1) std::memset(&out->icp, 0, sizeof(out->icp));
+    if (out->icp.status == AZU_E_TIMEOUT) {
+        set_error("ICP grid barrier timed out");
+        return AZU_E_TIMEOUT;
+    }
+    return AZU_OK;
+}
+
+// One frame whose inputs are being uploaded, with its result read back.
+static int run_frame_with_result(azu_pipeline* pl, azu_frame_result* out) {
+    if (two_streams(pl) && !pl->profiling) {
+        if (int rc = run_frame(pl, true)) return rc;
+        return read_staged_result(pl, out);
+    }
+    if (int rc = run_frame(pl)) return rc;
+    return pipeline_read_result(pl, out);
 }
 
 int pipeline_read_result(azu_pipeline* pl, azu_frame_result* out) {
@@ -259,19 +361,37 @@ int pipeline_read_result(azu_pipeline* pl, azu_frame_result* out) {
 
 using namespace azu;
 
+static void drop_graphs(azu_pipeline* pl) {
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    pl->exec = nullptr;
+    pl->graph = nullptr;
+    for (int k = 0; k < 5; ++k) {
+        if (pl->x_part[k]) cudaGraphExecDestroy(pl->x_part[k]);
+        if (pl->g_part[k]) cudaGraphDestroy(pl->g_part[k]);
+        pl->x_part[k] = nullptr;
+        pl->g_part[k] = nullptr;
+    }
+}
+
 extern "C" int azu_pipeline_destroy(azu_pipeline* pl) {
     if (!pl) return AZU_OK;
     cudaSetDevice(pl->device);
+    if (pl->s2) cudaStreamSynchronize(pl->s2);
     if (pl->s) cudaStreamSynchronize(pl->s);
-    if (pl->exec) cudaGraphExecDestroy(pl->exec);
-    if (pl->graph) cudaGraphDestroy(pl->graph);
+    drop_graphs(pl);
     azu_preprocessor_destroy(pl->pre);
     azu_tracker_destroy(pl->trk);
     azu_volume_destroy(pl->vol);
     for (void* q : {(void*)pl->d_in, (void*)pl->d_depth_m, (void*)pl->d_model_v, (void*)pl->d_model_n,
-                    (void*)pl->d_st, (void*)pl->d_icp, (void*)pl->d_packed})
+                    (void*)pl->d_st, (void*)pl->d_icp, (void*)pl->d_packed, (void*)pl->d_depth2[0],
+                    (void*)pl->d_depth2[1]})
         if (q) cudaFree(q);
+    if (pl->h_st) cudaFreeHost(pl->h_st);
+    if (pl->h_icp) cudaFreeHost(pl->h_icp);
     for (cudaEvent_t e : pl->ev) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {pl->ev_front, pl->ev_track, pl->ev_result}) if (e) cudaEventDestroy(e);
+    if (pl->s2) cudaStreamDestroy(pl->s2);
     if (pl->s && pl->own_stream) cudaStreamDestroy(pl->s);
     delete pl;
     return AZU_OK;
@@ -314,6 +434,15 @@ int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t st
         if (!e) e = cudaMalloc(&pl->d_icp, sizeof(azu_icp_result));
         if (!e) e = cudaMemsetAsync(pl->d_icp, 0, sizeof(azu_icp_result), pl->s);
         for (int k = 0; !e && k < 6; ++k) e = cudaEventCreate(&pl->ev[k]);
+        if (!e && pl->own_stream) {
+            // the second stream of the two-stream schedule
+            e = cudaStreamCreateWithFlags(&pl->s2, cudaStreamNonBlocking);
+            for (cudaEvent_t* ev : {&pl->ev_front, &pl->ev_track, &pl->ev_result})
+                if (!e) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+            for (int k = 0; !e && k < 2; ++k) e = cudaMalloc(&pl->d_depth2[k], n * 4);
+            if (!e) e = cudaHostAlloc(&pl->h_st, sizeof(PoseState), cudaHostAllocDefault);
+            if (!e) e = cudaHostAlloc(&pl->h_icp, sizeof(azu_icp_result), cudaHostAllocDefault);
+        }
         if (e) { set_error("pipeline allocation: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; }
     }
     if (rc) { azu_pipeline_destroy(pl); return rc; }
@@ -329,9 +458,12 @@ extern "C" int azu_pipeline_create(int device, const azu_pipeline_params* p, azu
 extern "C" int azu_pipeline_reset(azu_pipeline* pl) {
     AZU_CHECK_ARG(pl != nullptr, "null handle");
     AZU_TRY_CUDA(cudaSetDevice(pl->device));
+    if (pl->s2) AZU_TRY_CUDA(cudaStreamSynchronize(pl->s2));
+    AZU_TRY_CUDA(cudaStreamSynchronize(pl->s));
     if (int rc = azu_volume_reset(pl->vol)) return rc;
     if (pl->pre) if (int rc = azu_preprocessor_reset(pl->pre)) return rc;
     pl->frames = 0;
+    pl->buf = 0;
     pl->vol->integrated_frames = 0;
     return AZU_OK;
 }
@@ -342,8 +474,7 @@ extern "C" int azu_pipeline_process_frame(azu_pipeline* pl, const uint16_t* h_de
     AZU_CHECK_ARG(pl->p.input_is_mm || h_rgb != nullptr, "the raw-code path needs the RGB frame for guidance");
     AZU_TRY_CUDA(cudaSetDevice(pl->device));
     if (int rc = pipeline_upload_inputs(pl, h_depth, h_rgb, cudaMemcpyHostToDevice)) return rc;
-    if (int rc = run_frame(pl)) return rc;
-    return pipeline_read_result(pl, out);
+    return run_frame_with_result(pl, out);
 }
 
 extern "C" int azu_pipeline_process_frame_device(azu_pipeline* pl, const uint16_t* d_depth, const uint8_t* d_rgb,
@@ -352,9 +483,8 @@ extern "C" int azu_pipeline_process_frame_device(azu_pipeline* pl, const uint16_
     AZU_CHECK_ARG(pl->p.input_is_mm || d_rgb != nullptr, "the raw-code path needs the RGB frame for guidance");
     AZU_TRY_CUDA(cudaSetDevice(pl->device));
     if (int rc = pipeline_upload_inputs(pl, d_depth, d_rgb, cudaMemcpyDeviceToDevice)) return rc;
-    if (int rc = run_frame(pl)) return rc;
-    if (out) return pipeline_read_result(pl, out);
-    return AZU_OK;
+    if (out) return run_frame_with_result(pl, out);
+    return run_frame(pl);
 }
 
 extern "C" int azu_pipeline_process_frame_packed(azu_pipeline* pl, const void* h_packed, azu_frame_result* out) {
@@ -364,12 +494,11 @@ extern "C" int azu_pipeline_process_frame_packed(azu_pipeline* pl, const void* h
     const size_t bytes = n * (pl->p.input_is_mm ? 2 : 5);
     if (!pl->d_packed) AZU_TRY_CUDA(cudaMalloc(&pl->d_packed, n * 5));
     // the one host-to-device copy of the frame; the split happens on the device
-    AZU_TRY_CUDA(cudaMemcpyAsync(pl->d_packed, h_packed, bytes, cudaMemcpyHostToDevice, pl->s));
+    AZU_TRY_CUDA(cudaMemcpyAsync(pl->d_packed, h_packed, bytes, cudaMemcpyHostToDevice, front_stream(pl)));
     const uint16_t* d_depth = reinterpret_cast<const uint16_t*>(pl->d_packed);
     const uint8_t* d_rgb = pl->p.input_is_mm ? nullptr : pl->d_packed + n * 2;
     if (int rc = pipeline_upload_inputs(pl, d_depth, d_rgb, cudaMemcpyDeviceToDevice)) return rc;
-    if (int rc = run_frame(pl)) return rc;
-    return pipeline_read_result(pl, out);
+    return run_frame_with_result(pl, out);
 }
 
 extern "C" int azu_pipeline_last_result(azu_pipeline* pl, azu_frame_result* out) {
@@ -393,9 +522,10 @@ extern "C" void* azu_pipeline_stream(azu_pipeline* pl) { return pl ? static_cast
 extern "C" int azu_pipeline_set_profiling(azu_pipeline* pl, int on) {
     AZU_CHECK_ARG(pl != nullptr, "null handle");
     if ((on != 0) != pl->profiling) {
-        // Event records are part of the captured graph: recapture.
-        if (pl->exec) { cudaGraphExecDestroy(pl->exec); pl->exec = nullptr; }
-        if (pl->graph) { cudaGraphDestroy(pl->graph); pl->graph = nullptr; }
+        // Event records are part of the captured graphs: recapture.
+        if (pl->s2) AZU_TRY_CUDA(cudaStreamSynchronize(pl->s2));
+        AZU_TRY_CUDA(cudaStreamSynchronize(pl->s));
+        drop_graphs(pl);
     }
     pl->profiling = on != 0;
     for (double& v : pl->stage_ms) v = 0.0;

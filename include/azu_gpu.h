@@ -370,11 +370,20 @@ int azu_pipeline_create(int device, const azu_pipeline_params* p, azu_pipeline**
 int azu_pipeline_destroy(azu_pipeline* p);
 int azu_pipeline_reset(azu_pipeline* p);
 /* One frame from host buffers: H2D of depth (and rgb, may be NULL), the whole
- * frame on the device, D2H of the result. Synchronous. */
+ * frame on the device, D2H of the result. Returns once the result is known,
+ * i.e. after tracking: the frame's integrate and raycast are still running on
+ * the pipeline's stream (every call on the pipeline, its volume and its
+ * tracker is ordered after them; synchronise that stream before touching
+ * their device buffers directly). The next frame's upload, preprocessing and
+ * frame maps run on a second stream beside them; results are those of
+ * finishing each frame before the next. With stage profiling on, the call
+ * returns after the whole frame. */
 int azu_pipeline_process_frame(azu_pipeline* p, const uint16_t* h_depth, const uint8_t* h_rgb,
                                azu_frame_result* out);
 /* Same from device buffers; out may be NULL (no host sync: the frame is only
- * enqueued and the result stays on the device). */
+ * enqueued and the result stays on the device). The input buffers may be
+ * reused once the call returns with a result, or after the pipeline's stream
+ * has been synchronised. */
 int azu_pipeline_process_frame_device(azu_pipeline* p, const uint16_t* d_depth, const uint8_t* d_rgb,
                                       azu_frame_result* out);
 /* Reads back the result of the last enqueued frame (synchronises). */

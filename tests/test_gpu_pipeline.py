@@ -59,3 +59,41 @@ def test_graph_replay_equals_eager(cuda_lib, seq):
         rb = b.process_frame(seq.depth_mm[k])
         assert np.array_equal(ra["pose"], rb["pose"]) and ra["quality"] == rb["quality"]
     assert a.lib.azu_pipeline_uses_graph(a.h) == 1
+
+
+@pytest.mark.parametrize("input_is_mm", [False, True])
+def test_overlapped_schedule_equals_sequential(cuda_lib, seq, input_is_mm):
+    """Frame k+1's input stage runs beside frame k's fusion and results come
+    back once the pose is known; that must give exactly what a schedule that
+    finishes every frame before the next gives: the same poses every frame and
+    the same volume at the end, also when frames are only enqueued."""
+    import torch
+    from azu_gb300 import api, synth
+    rgb = synth.grey_rgb()
+    frames = [seq.depth_mm[k] if input_is_mm else synth.encode_raw(seq.depth_mm[k]) for k in range(len(seq.poses))]
+    seqp = _pipeline(seq, input_is_mm)
+    seqp.set_profiling(True)  # stage timing reads every frame back whole
+    fast = _pipeline(seq, input_is_mm)
+    ref = [seqp.process_frame(d, None if input_is_mm else rgb) for d in frames]
+    got = [fast.process_frame(d, None if input_is_mm else rgb) for d in frames]
+    for a, b in zip(ref, got):
+        assert np.array_equal(a["pose"].view(np.uint32), b["pose"].view(np.uint32))
+        assert (a["quality"], a["integrated"], a["frame_index"]) == (b["quality"], b["integrated"], b["frame_index"])
+        assert a["icp"]["inliers"] == b["icp"]["inliers"]
+    # enqueue only, no host round trip between frames
+    queued = _pipeline(seq, input_is_mm)
+    d_in = torch.from_numpy(np.stack(frames).astype(np.uint16).view(np.int16)).cuda()
+    d_rgb = torch.from_numpy(rgb).cuda()
+    for k in range(len(frames)):
+        queued.process_frame_device(d_in[k].data_ptr(), None if input_is_mm else d_rgb.data_ptr())
+    last = queued.last_result()
+    assert np.array_equal(last["pose"].view(np.uint32), ref[-1]["pose"].view(np.uint32))
+    vp = api.volume_params(seq.volume["resolution"], seq.volume["voxel_size"], seq.volume["truncation"],
+                           seq.volume["max_weight"], seq.volume["origin"], seq.min_depth, seq.max_depth,
+                           seq.volume["format"])
+    vols = [api.TSDFVolume.borrowed(p.volume_handle(), vp).download() for p in (seqp, fast, queued)]
+    for t, w in vols[1:]:
+        assert np.array_equal(t.view(np.uint32), vols[0][0].view(np.uint32))
+        assert np.array_equal(w, vols[0][1])
+    for p in (seqp, fast, queued):
+        p.close()
