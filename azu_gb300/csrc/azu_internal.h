@@ -93,7 +93,9 @@ struct azu_volume {
     float* color = nullptr;     // 3 floats per voxel when p.color
     float* d_pose = nullptr;    // 16 floats: pose slot for host-pose calls
     azu::IntegrateConsts* d_iconsts = nullptr;
-    unsigned long long* d_counters = nullptr;  // [0] newly observed (cumulative), [1] updated (last), [2] colour (last)
+    unsigned long long* d_counters = nullptr;  // [0] newly observed (cumulative), [1] updated (last), [2] colour (last),
+                                               // [3] updated (cumulative), [4] integrate work counter
+    int int_blocks = 0;                        // resident blocks of the persistent integrate kernel
     float* d_depth_stage = nullptr;            // host-depth staging (integrate_host)
     uint8_t* d_rgb_stage = nullptr;
     size_t stage_pixels = 0;

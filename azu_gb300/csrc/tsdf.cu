@@ -185,6 +185,7 @@ __device__ __forceinline__ void integrate_setup_body(const float* __restrict__ d
         *out = ic;
         counters[1] = 0;
         counters[2] = 0;
+        counters[4] = 0;  // next warp item of the integrate kernel
     }
     // tile pyramid: level l from level l-1, 2x2 children
     for (int l = 1; l < mip.levels; ++l) {
@@ -481,6 +482,9 @@ __device__ __forceinline__ void integrate_item(
     }
 }
 
+// Persistent: every warp takes the next item (32 rows at one z) from a counter
+// until none is left, so warps whose items are culled early move on instead of
+// idling beside a busy warp of their block.
 template <bool kHalf, bool kColor, bool kResid>
 __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     void* __restrict__ vox, float* __restrict__ color, const IntegrateConsts* __restrict__ icp,
@@ -489,10 +493,18 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb,
     const float* __restrict__ tiles, TileMip mip) {
     __shared__ float s_c[kIntWarps][3][32][33];
+    if (gate && __ldg(gate) == 0) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    integrate_item<kHalf, kColor, kResid>(vox, color, icp, depth, rgb, res, vs, ox, oy, oz, trunc, max_w, fx, fy, cx,
-                                          cy, W, H, min_d, max_d, gate, counters, bricks, nb, tiles, mip,
-                                          blockIdx.x * kIntWarps + warp, warp, lane, s_c);
+    const int n_items = res * ((res + 31) >> 5);
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = static_cast<int>(atomicAdd(&counters[4], 1ull));
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= n_items) break;
+        integrate_item<kHalf, kColor, kResid>(vox, color, icp, depth, rgb, res, vs, ox, oy, oz, trunc, max_w, fx, fy,
+                                              cx, cy, W, H, min_d, max_d, nullptr, counters, bricks, nb, tiles, mip,
+                                              item, warp, lane, s_c);
+    }
 }
 
 // ---- raycast ---------------------------------------------------------------
@@ -1142,8 +1154,25 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
     AZU_LAUNCH_CHECK();
     const int ngroups = (p.resolution + 31) / 32;
     const long items = static_cast<long>(p.resolution) * ngroups;
-    const int blocks = static_cast<int>((items + kIntWarps - 1) / kIntWarps);
     const bool half = p.format != AZU_TSDF_FP32;
+    if (!v->int_blocks) {
+        // resident blocks of the persistent integrate kernel: the fewest any variant fits
+        int sms = 0, occ = 1 << 20;
+        AZU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, v->device));
+        const void* variants[] = {(const void*)integrate_kernel<false, false, false>,
+                                  (const void*)integrate_kernel<false, true, false>,
+                                  (const void*)integrate_kernel<true, false, false>,
+                                  (const void*)integrate_kernel<true, true, false>,
+                                  (const void*)integrate_kernel<true, false, true>,
+                                  (const void*)integrate_kernel<true, true, true>};
+        for (const void* f : variants) {
+            int o = 0;
+            AZU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, f, kIntWarps * 32, 0));
+            occ = std::min(occ, o);
+        }
+        v->int_blocks = std::max(1, sms * std::max(occ, 1));
+    }
+    const int blocks = static_cast<int>(std::min<long>(v->int_blocks, (items + kIntWarps - 1) / kIntWarps));
     const bool resid = p.format == AZU_TSDF_FP16R;
     const bool col = v->color != nullptr;
 #define AZU_INT_ARGS                                                                                             \
@@ -1246,7 +1275,7 @@ extern "C" int azu_volume_reset(azu_volume* v) {
     if (v->p.format != AZU_TSDF_FP32) reset_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
     else reset_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
     AZU_LAUNCH_CHECK();
-    AZU_TRY_CUDA(cudaMemsetAsync(v->d_counters, 0, 4 * sizeof(unsigned long long), v->stream.s));
+    AZU_TRY_CUDA(cudaMemsetAsync(v->d_counters, 0, 5 * sizeof(unsigned long long), v->stream.s));
     AZU_TRY_CUDA(cudaMemsetAsync(v->bricks, 1, static_cast<size_t>(v->nb) * v->nb * v->nb, v->stream.s));
     v->integrated_frames = 0;
     return AZU_OK;
@@ -1264,7 +1293,7 @@ extern "C" int azu_volume_create(int device, const azu_volume_params* p, void* s
     if (!rc) rc = volume_alloc(v);
     if (!rc) { cudaError_t e = cudaMalloc(&v->d_pose, 16 * sizeof(float)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
     if (!rc) { cudaError_t e = cudaMalloc(&v->d_iconsts, sizeof(IntegrateConsts)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
-    if (!rc) { cudaError_t e = cudaMalloc(&v->d_counters, 4 * sizeof(unsigned long long)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
+    if (!rc) { cudaError_t e = cudaMalloc(&v->d_counters, 5 * sizeof(unsigned long long)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
     if (!rc) rc = azu_volume_reset(v);
     if (rc) {
         azu_volume_destroy(v);
