@@ -225,9 +225,9 @@ __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res
 //          the chunk if its nearest voxel is beyond it by more than trunc;
 //   chain (lane = row): replay the sequential c-steps, parking c of live rows
 //          in shared memory;
-//   update (lane = x): for each live row, project every voxel exactly, test its
-//          8x8 tile, then gather depth and read-modify-write the voxel, all
-//          coalesced.
+//   update (lane = x): for each live row, project every voxel exactly, gather
+//          its depth and read-modify-write the voxel, all coalesced (a per-voxel
+//          tile test before the gather only lengthened the dependent chain).
 // Every test is exact or conservative, so the updated set and the values are
 // the CPU's. Voxels that take no update are never read: HBM traffic is
 // 2 x record size per updated voxel.
@@ -380,7 +380,6 @@ __device__ __forceinline__ void integrate_item(
         // update (lane = x), live rows in batches of 8 so their loads overlap
         const int x = xc + lane;
         const bool x_on = x >= x0 && x <= x1;
-        const int tw0 = mip.w[0];
         unsigned rem = live_rows;
 #pragma unroll 1
         while (rem) {
@@ -391,12 +390,11 @@ __device__ __forceinline__ void integrate_item(
                 rem &= rem - 1;
             }
             int pix[8];
-            float cz[8], tm[8];
+            float cz[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 pix[j] = -1;
                 cz[j] = 0.0f;
-                tm[j] = 0.0f;
                 if (rsel[j] >= 0 && x_on) {
                     const F3 cv = mk3(s_c[warp][0][rsel[j]][lane], s_c[warp][1][rsel[j]][lane],
                                       s_c[warp][2][rsel[j]][lane]);
@@ -408,19 +406,13 @@ __device__ __forceinline__ void integrate_item(
                             const int ui = static_cast<int>(uf), vi = static_cast<int>(vf);
                             pix[j] = vi * W + ui;
                             cz[j] = cv.z;
-                            tm[j] = __ldg(tiles + (vi >> kTileShift) * tw0 + (ui >> kTileShift));
                         }
                     }
                 }
             }
             float sdf[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                // fs is monotone in the depth: below -trunc for the tile's
-                // deepest in-band depth means no pixel of the tile updates it
-                if (pix[j] >= 0 && fs(tm[j], cz[j]) < -trunc) pix[j] = -1;
-                sdf[j] = pix[j] >= 0 ? __ldg(depth + pix[j]) : 0.0f;
-            }
+            for (int j = 0; j < 8; ++j) sdf[j] = pix[j] >= 0 ? __ldg(depth + pix[j]) : 0.0f;
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const float d = sdf[j];
