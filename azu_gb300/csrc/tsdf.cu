@@ -62,6 +62,7 @@ __global__ void reset_kernel(void* vox, float* color, size_t n) {
 // ---- integration -----------------------------------------------------------
 constexpr int kIntWarps = 4;
 constexpr int kTileShift = 3;  // level-0 depth tiles are 8x8 pixels
+constexpr int kCullSeg = 16;   // voxels per culling piece of a 32-voxel chunk
 
 // Deepest in-band depth of every 8x8 pixel tile (-inf when the tile has none),
 // level 0 of the tile pyramid. Eight lanes share a tile, one pixel row each.
@@ -312,38 +313,37 @@ __device__ __forceinline__ void integrate_item(
         for (int x = x0; x < xfirst; ++x) c = add3(c, step);
 
     for (int xc = xfirst; xc <= wxe; xc += 32) {
-        // cull (lane = row). The lane's c belongs to x = max(xc, x0).
+        // cull (lane = row), per kCullSeg-voxel piece of the chunk so each
+        // piece's pixels fit a finer tile level. The lane's c belongs to
+        // x = max(xc, x0).
         bool live = false;
         if (row_on) {
             const int xcur = max(xc, x0);
             const int xa = max(xcur, xs), xb = min(min(xc + 31, x1), xe);
-            if (xa <= xb) {
-                const float ka = static_cast<float>(xa - xcur), kb = static_cast<float>(xb - xcur);
+            auto piece_live = [&](int pa, int pb) {
+                const float ka = static_cast<float>(pa - xcur), kb = static_cast<float>(pb - xcur);
                 const F3 ca = mk3(fmaf(ka, step.x, c.x), fmaf(ka, step.y, c.y), fmaf(ka, step.z, c.z));
                 const F3 cb = mk3(fmaf(kb, step.x, c.x), fmaf(kb, step.y, c.y), fmaf(kb, step.z, c.z));
-                if (!(ca.z >= z_safe && cb.z >= z_safe)) {
-                    live = true;  // near or behind the camera plane: no bound
-                } else {
-                    const float ua = fx * __fdividef(ca.x, ca.z) + cx, ub = fx * __fdividef(cb.x, cb.z) + cx;
-                    const float va = fy * __fdividef(ca.y, ca.z) + cy, vb = fy * __fdividef(cb.y, cb.z) + cy;
-                    const float ulo = fminf(ua, ub) - 2.0f, uhi = fmaxf(ua, ub) + 3.0f;
-                    const float vlo = fminf(va, vb) - 2.0f, vhi = fmaxf(va, vb) + 3.0f;
-                    if (uhi >= 0.0f && ulo < fW && vhi >= 0.0f && vlo < fH) {
-                        const int iu0 = static_cast<int>(fmaxf(ulo, 0.0f));
-                        const int iu1 = static_cast<int>(fminf(uhi, fW - 1.0f));
-                        const int iv0 = static_cast<int>(fmaxf(vlo, 0.0f));
-                        const int iv1 = static_cast<int>(fminf(vhi, fH - 1.0f));
-                        const int ext = max(iu1 - iu0, iv1 - iv0) >> kTileShift;
-                        const int l = min(ext ? 32 - __clz(ext) : 0, mip.levels - 1);
-                        const int sh = kTileShift + l, w = mip.w[l];
-                        const float* tl = tiles + mip.off[l];
-                        const int a0 = (iv0 >> sh) * w, a1 = (iv1 >> sh) * w, b0 = iu0 >> sh, b1 = iu1 >> sh;
-                        const float tm = fmaxf(fmaxf(__ldg(tl + a0 + b0), __ldg(tl + a0 + b1)),
-                                               fmaxf(__ldg(tl + a1 + b0), __ldg(tl + a1 + b1)));
-                        live = !(fminf(ca.z, cb.z) > tm + cull_off);
-                    }
-                }
-            }
+                if (!(ca.z >= z_safe && cb.z >= z_safe)) return true;  // near or behind the camera plane: no bound
+                const float ua = fx * __fdividef(ca.x, ca.z) + cx, ub = fx * __fdividef(cb.x, cb.z) + cx;
+                const float va = fy * __fdividef(ca.y, ca.z) + cy, vb = fy * __fdividef(cb.y, cb.z) + cy;
+                const float ulo = fminf(ua, ub) - 2.0f, uhi = fmaxf(ua, ub) + 3.0f;
+                const float vlo = fminf(va, vb) - 2.0f, vhi = fmaxf(va, vb) + 3.0f;
+                if (!(uhi >= 0.0f && ulo < fW && vhi >= 0.0f && vlo < fH)) return false;
+                const int iu0 = static_cast<int>(fmaxf(ulo, 0.0f));
+                const int iu1 = static_cast<int>(fminf(uhi, fW - 1.0f));
+                const int iv0 = static_cast<int>(fmaxf(vlo, 0.0f));
+                const int iv1 = static_cast<int>(fminf(vhi, fH - 1.0f));
+                const int ext = max(iu1 - iu0, iv1 - iv0) >> kTileShift;
+                const int l = min(ext ? 32 - __clz(ext) : 0, mip.levels - 1);
+                const int sh = kTileShift + l, w = mip.w[l];
+                const float* tl = tiles + mip.off[l];
+                const int a0 = (iv0 >> sh) * w, a1 = (iv1 >> sh) * w, b0 = iu0 >> sh, b1 = iu1 >> sh;
+                const float tm = fmaxf(fmaxf(__ldg(tl + a0 + b0), __ldg(tl + a0 + b1)),
+                                       fmaxf(__ldg(tl + a1 + b0), __ldg(tl + a1 + b1)));
+                return !(fminf(ca.z, cb.z) > tm + cull_off);
+            };
+            for (int pa = xa; pa <= xb && !live; pa += kCullSeg) live = piece_live(pa, min(pa + kCullSeg - 1, xb));
         }
         const unsigned live_rows = __ballot_sync(0xffffffffu, live);
         // chain (lane = row): the sequential c-steps of the chunk
