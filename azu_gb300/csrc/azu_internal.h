@@ -124,9 +124,14 @@ size_t voxel_bytes(int format);
 // Exact free-brick flags recomputed from the voxels.
 int rebuild_bricks(azu_volume* v, cudaStream_t s);
 // Enqueue helpers shared with the pipeline (pose read from device memory).
+// d_tiles_built: the depth map's tile pyramid from volume_build_tiles_dev, or
+// null to build it here into the volume's own buffer.
 int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d_rgb, const float* d_pose,
                          float fx, float fy, float cx, float cy, int W, int H, float min_d, float max_d,
-                         const int* d_gate, cudaStream_t s);
+                         const int* d_gate, cudaStream_t s, const float* d_tiles_built = nullptr);
+int volume_build_tiles_dev(const float* d_depth_m, int W, int H, float min_d, float max_d, float* tiles,
+                           cudaStream_t s);
+TileMip make_tile_mip(int W, int H);
 int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, float cx, float cy, int W, int H,
                        float* d_vertices, float* d_normals, uint8_t* d_colors, const int* d_gate, cudaStream_t s);
 // Writes a host pose into a device slot with a by-value kernel argument.

@@ -8,6 +8,7 @@
 //   input      preprocess Kinect raw codes (or mm -> metres)
 //   frame      vertices, normals, 3-level pyramid
 //   predict    constant velocity: pred = cur * (last^-1 * cur); prev = cur; last = cur
+//              (computed by the previous frame's commit)
 //   track      persistent ICP from pred against the model; on a Failed grade it
 //              retries from prev; Good/Poor move cur, Failed keeps it
 //   integrate  only when the grade is Good (a device flag gates the kernels)
@@ -52,24 +53,23 @@ struct PoseState {
     int integrated;
 };
 
-// PipelineController.cpp:1175-1177 (velocity model off, the default).
-__global__ void predict_kernel(PoseState* st) {
-    if (threadIdx.x != 0) return;
-    float inv[16], m[16];
-    for (int i = 0; i < 16; ++i) st->prev[i] = st->cur[i];
-    inverse4(st->last, inv);
-    mm4(inv, st->cur, m);
-    mm4(st->cur, m, st->pred);
-    for (int i = 0; i < 16; ++i) st->last[i] = st->cur[i];
-}
-
 // After a gated integrate + raycast: the model now shows the scene at cur.
+// Then the next frame's prediction, PipelineController.cpp:1175-1177 (velocity
+// model off, the default): prev = cur; pred = cur * (last^-1 * cur); last = cur.
+// cur is final once this frame's tracking has run, so it is done here rather
+// than in a launch of its own at the next frame's start.
 __global__ void commit_kernel(PoseState* st) {
     if (threadIdx.x != 0) return;
     st->integrated = st->gate;
     if (st->gate)
         for (int i = 0; i < 16; ++i) st->model_pose[i] = st->cur[i];
     st->frame_index += 1;
+    float inv[16], m[16];
+    for (int i = 0; i < 16; ++i) st->prev[i] = st->cur[i];
+    inverse4(st->last, inv);
+    mm4(inv, st->cur, m);
+    mm4(st->cur, m, st->pred);
+    for (int i = 0; i < 16; ++i) st->last[i] = st->cur[i];
 }
 
 __global__ void first_frame_kernel(PoseState* st) {
@@ -109,6 +109,7 @@ struct azu_pipeline {
     cudaStream_t s2 = nullptr;                    // inputs, preprocessing, frame maps
     cudaEvent_t ev_front = nullptr, ev_track = nullptr, ev_result = nullptr;
     float* d_depth2[2] = {nullptr, nullptr};      // the frame's depth (metres), alternating
+    float* d_tiles2[2] = {nullptr, nullptr};      // its depth tile pyramid
     int buf = 0;
     cudaGraph_t g_part[5] = {};                   // front[2], track, tail[2]
     cudaGraphExec_t x_part[5] = {};
@@ -163,6 +164,9 @@ static int enqueue_input(azu_pipeline* pl, cudaStream_t s) {
     }
     if (int rc = mark(pl, 1, s)) return rc;
     if (int rc = tracker_prepare_dev(pl->trk, depth_source(pl), W, H, s)) return rc;
+    // the integration's depth tiles depend on the depth only
+    if (two_streams(pl))
+        if (int rc = volume_build_tiles_dev(depth_source(pl), W, H, lo, hi, pl->d_tiles2[pl->buf], s)) return rc;
     return mark(pl, 2, s);
 }
 
@@ -173,8 +177,7 @@ static int enqueue_track(azu_pipeline* pl, bool first, cudaStream_t s) {
         first_frame_kernel<<<1, 32, 0, s>>>(st);
         AZU_LAUNCH_CHECK();
     } else {
-        predict_kernel<<<1, 32, 0, s>>>(st);
-        AZU_LAUNCH_CHECK();
+        // pred / prev / last were set by the previous frame's commit
         if (int rc = tracker_track_dev(pl->trk, pl->d_model_v, pl->d_model_n, pl->W, pl->H, st->pred, st->model_pose,
                                        st->prev, st->cur, pl->d_icp, &st->quality, &st->gate, s))
             return rc;
@@ -210,7 +213,8 @@ static int enqueue_tail(azu_pipeline* pl, cudaStream_t s) {
     const int W = pl->W, H = pl->H;
     PoseState* st = pl->d_st;
     if (int rc = volume_integrate_dev(pl->vol, depth_source(pl), nullptr, st->cur, T.fx, T.fy, T.cx, T.cy, W, H,
-                                      P.min_depth, P.max_depth, &st->gate, s))
+                                      P.min_depth, P.max_depth, &st->gate, s,
+                                      two_streams(pl) ? pl->d_tiles2[pl->buf] : nullptr))
         return rc;
     if (int rc = mark(pl, 4, s)) return rc;
     if (int rc = volume_raycast_dev(pl->vol, st->cur, T.fx, T.fy, T.cx, T.cy, W, H, pl->d_model_v, pl->d_model_n,
@@ -385,7 +389,7 @@ extern "C" int azu_pipeline_destroy(azu_pipeline* pl) {
     azu_volume_destroy(pl->vol);
     for (void* q : {(void*)pl->d_in, (void*)pl->d_depth_m, (void*)pl->d_model_v, (void*)pl->d_model_n,
                     (void*)pl->d_st, (void*)pl->d_icp, (void*)pl->d_packed, (void*)pl->d_depth2[0],
-                    (void*)pl->d_depth2[1]})
+                    (void*)pl->d_depth2[1], (void*)pl->d_tiles2[0], (void*)pl->d_tiles2[1]})
         if (q) cudaFree(q);
     if (pl->h_st) cudaFreeHost(pl->h_st);
     if (pl->h_icp) cudaFreeHost(pl->h_icp);
@@ -440,6 +444,8 @@ int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t st
             for (cudaEvent_t* ev : {&pl->ev_front, &pl->ev_track, &pl->ev_result})
                 if (!e) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
             for (int k = 0; !e && k < 2; ++k) e = cudaMalloc(&pl->d_depth2[k], n * 4);
+            const size_t nt = static_cast<size_t>(make_tile_mip(W, H).total);
+            for (int k = 0; !e && k < 2; ++k) e = cudaMalloc(&pl->d_tiles2[k], nt * 4);
             if (!e) e = cudaHostAlloc(&pl->h_st, sizeof(PoseState), cudaHostAllocDefault);
             if (!e) e = cudaHostAlloc(&pl->h_icp, sizeof(azu_icp_result), cudaHostAllocDefault);
         }

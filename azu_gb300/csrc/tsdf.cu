@@ -116,15 +116,38 @@ TileMip make_tile_mip(int W, int H) {
     return m;
 }
 
+// Tile pyramid, one block: level l from level l-1, 2x2 children.
+__device__ __forceinline__ void build_tile_pyramid(float* __restrict__ tiles, const TileMip& mip) {
+    for (int l = 1; l < mip.levels; ++l) {
+        __syncthreads();
+        const float* src = tiles + mip.off[l - 1];
+        float* dst = tiles + mip.off[l];
+        const int sw = mip.w[l - 1], sh = mip.h[l - 1], w = mip.w[l], n = w * mip.h[l];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int ty = i / w, tx = i - ty * w;
+            const int x0 = 2 * tx, y0 = 2 * ty;
+            float m = src[y0 * sw + x0];
+            if (x0 + 1 < sw) m = fmaxf(m, src[y0 * sw + x0 + 1]);
+            if (y0 + 1 < sh) {
+                m = fmaxf(m, src[(y0 + 1) * sw + x0]);
+                if (x0 + 1 < sw) m = fmaxf(m, src[(y0 + 1) * sw + x0 + 1]);
+            }
+            dst[i] = m;
+        }
+    }
+}
+__global__ void tile_pyramid_kernel(float* __restrict__ tiles, TileMip mip) { build_tile_pyramid(tiles, mip); }
+
 // Frustum AABB and camera transform for one integration (TSDFVolume.cpp:238-264),
 // computed on the device so the pose may come from the tracker without a host
 // round trip. Same float expression trees as the CPU path. Thread 0 writes the
-// constants; the block then builds levels 1.. of the tile pyramid.
+// constants; the block then builds levels 1.. of the tile pyramid unless they
+// were built with the depth map.
 __device__ __forceinline__ void integrate_setup_body(const float* __restrict__ d_pose, int res, float vs, float ox,
                                                      float oy, float oz, float trunc, float fx, float fy, float cx,
                                                      float cy, int W, int H, float max_d, IntegrateConsts* out,
                                                      unsigned long long* counters, float* __restrict__ tiles,
-                                                     const TileMip& mip) {
+                                                     const TileMip& mip, bool pyramid) {
     if (threadIdx.x == 0) {
         float P[16], inv[16], Rcw[9];
         for (int i = 0; i < 16; ++i) P[i] = d_pose[i];
@@ -188,30 +211,14 @@ __device__ __forceinline__ void integrate_setup_body(const float* __restrict__ d
         counters[2] = 0;
         counters[4] = 0;  // next warp item of the integrate kernel
     }
-    // tile pyramid: level l from level l-1, 2x2 children
-    for (int l = 1; l < mip.levels; ++l) {
-        __syncthreads();
-        const float* src = tiles + mip.off[l - 1];
-        float* dst = tiles + mip.off[l];
-        const int sw = mip.w[l - 1], sh = mip.h[l - 1], w = mip.w[l], n = w * mip.h[l];
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int ty = i / w, tx = i - ty * w;
-            const int x0 = 2 * tx, y0 = 2 * ty;
-            float m = src[y0 * sw + x0];
-            if (x0 + 1 < sw) m = fmaxf(m, src[y0 * sw + x0 + 1]);
-            if (y0 + 1 < sh) {
-                m = fmaxf(m, src[(y0 + 1) * sw + x0]);
-                if (x0 + 1 < sw) m = fmaxf(m, src[(y0 + 1) * sw + x0 + 1]);
-            }
-            dst[i] = m;
-        }
-    }
+    if (pyramid) build_tile_pyramid(tiles, mip);
 }
 __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res, float vs, float ox, float oy,
                                        float oz, float trunc, float fx, float fy, float cx, float cy, int W, int H,
                                        float max_d, IntegrateConsts* out, unsigned long long* counters,
-                                       float* __restrict__ tiles, TileMip mip) {
-    integrate_setup_body(d_pose, res, vs, ox, oy, oz, trunc, fx, fy, cx, cy, W, H, max_d, out, counters, tiles, mip);
+                                       float* __restrict__ tiles, TileMip mip, int pyramid) {
+    integrate_setup_body(d_pose, res, vs, ox, oy, oz, trunc, fx, fy, cx, cy, W, H, max_d, out, counters, tiles, mip,
+                         pyramid != 0);
 }
 
 // Voxel-projective integration (TSDFVolume.cpp:282-329).
@@ -894,7 +901,7 @@ __global__ void depth_tiles_batch_kernel(const IntegrateArgs* __restrict__ A, co
 __global__ void integrate_setup_batch_kernel(const IntegrateArgs* __restrict__ A, unsigned long long** counters) {
     const IntegrateArgs& a = A[blockIdx.x];
     integrate_setup_body(a.pose, a.res, a.vs, a.ox, a.oy, a.oz, a.trunc, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.max_d,
-                         a.icp_out, a.counters, a.tiles, a.mip);
+                         a.icp_out, a.counters, a.tiles, a.mip, true);
 }
 
 template <int kWarps>
@@ -1129,20 +1136,38 @@ static int ensure_tiles(azu_volume* v, size_t n, cudaStream_t s) {
     return AZU_OK;
 }
 
+// Depth tile pyramid of a depth map (level 0 + coarser levels) into `tiles`
+// (make_tile_mip(W, H).total floats).
+int volume_build_tiles_dev(const float* d_depth_m, int W, int H, float min_d, float max_d, float* tiles,
+                           cudaStream_t s) {
+    AZU_CHECK_ARG(W <= kMaxTilePixels && H <= kMaxTilePixels, "image larger than 16384 pixels a side");
+    const TileMip mip = make_tile_mip(W, H);
+    const int nt0 = mip.w[0] * mip.h[0];
+    depth_tiles_kernel<<<(nt0 + 31) / 32, 256, 0, s>>>(d_depth_m, W, H, min_d, max_d, mip.w[0], nt0, tiles, nullptr);
+    AZU_LAUNCH_CHECK();
+    tile_pyramid_kernel<<<1, 256, 0, s>>>(tiles, mip);
+    AZU_LAUNCH_CHECK();
+    return AZU_OK;
+}
+
 int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d_rgb, const float* d_pose, float fx,
                          float fy, float cx, float cy, int W, int H, float min_d, float max_d, const int* d_gate,
-                         cudaStream_t s) {
+                         cudaStream_t s, const float* d_tiles_built) {
     const azu_volume_params& p = v->p;
     AZU_CHECK_ARG(W <= kMaxTilePixels && H <= kMaxTilePixels, "image larger than 16384 pixels a side");
     const TileMip mip = make_tile_mip(W, H);
-    if (int rc = ensure_tiles(v, static_cast<size_t>(mip.total), s)) return rc;
-    const int nt0 = mip.w[0] * mip.h[0];
-    depth_tiles_kernel<<<(nt0 + 31) / 32, 256, 0, s>>>(d_depth_m, W, H, min_d, max_d, mip.w[0], nt0, v->d_tiles,
-                                                        d_gate);
-    AZU_LAUNCH_CHECK();
+    float* tiles = const_cast<float*>(d_tiles_built);
+    if (!tiles) {
+        if (int rc = ensure_tiles(v, static_cast<size_t>(mip.total), s)) return rc;
+        tiles = v->d_tiles;
+        const int nt0 = mip.w[0] * mip.h[0];
+        depth_tiles_kernel<<<(nt0 + 31) / 32, 256, 0, s>>>(d_depth_m, W, H, min_d, max_d, mip.w[0], nt0, tiles,
+                                                            d_gate);
+        AZU_LAUNCH_CHECK();
+    }
     integrate_setup_kernel<<<1, 256, 0, s>>>(d_pose, p.resolution, p.voxel_size, p.origin[0], p.origin[1],
                                              p.origin[2], p.truncation, fx, fy, cx, cy, W, H, max_d, v->d_iconsts,
-                                             v->d_counters, v->d_tiles, mip);
+                                             v->d_counters, tiles, mip, d_tiles_built ? 0 : 1);
     AZU_LAUNCH_CHECK();
     const int ngroups = (p.resolution + 31) / 32;
     const long items = static_cast<long>(p.resolution) * ngroups;
@@ -1170,7 +1195,7 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
 #define AZU_INT_ARGS                                                                                             \
     v->vox, v->color, v->d_iconsts, d_depth_m, d_rgb, p.resolution, p.voxel_size, p.origin[0], p.origin[1],     \
         p.origin[2], p.truncation, p.max_weight, fx, fy, cx, cy, W, H, min_d, max_d, d_gate, v->d_counters,   \
-        v->bricks, v->nb, v->d_tiles, mip
+        v->bricks, v->nb, tiles, mip
     if (!half && !col) integrate_kernel<false, false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (!half && col) integrate_kernel<false, true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (!resid && !col) integrate_kernel<true, false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
@@ -1186,7 +1211,8 @@ int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, f
                        float* d_vertices, float* d_normals, uint8_t* d_colors, const int* d_gate, cudaStream_t s) {
     const azu_volume_params& p = v->p;
     const VolView view = make_view(v);
-    const dim3 blk(32, 8), grd((W + 31) / 32, (H + 7) / 8);
+    // 16 x 8 pixel blocks: each warp marches a 16 x 2 patch (closer rays than a 32 x 1 row)
+    const dim3 blk(16, 8), grd((W + 15) / 16, (H + 7) / 8);
     const uint8_t* bricks = nullptr;
     if (v->skip_free) {
         const size_t nbr = static_cast<size_t>(v->nb) * v->nb * v->nb;
