@@ -63,6 +63,7 @@ __global__ void reset_kernel(void* vox, float* color, size_t n) {
 constexpr int kIntWarps = 4;
 constexpr int kTileShift = 3;  // level-0 depth tiles are 8x8 pixels
 constexpr int kCullSeg = 16;   // voxels per culling piece of a 32-voxel chunk
+constexpr int kIntParts = 2;   // x-parts per 32-row item of the persistent kernel (shorter items, shorter tail)
 
 // Deepest in-band depth of every 8x8 pixel tile (-inf when the tile has none),
 // level 0 of the tile pyramid. Eight lanes share a tile, one pixel row each.
@@ -247,10 +248,15 @@ __device__ __forceinline__ void integrate_item(
     const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
     float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
     float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb,
-    const float* __restrict__ tiles, const TileMip& mip, int item, int warp, int lane, float (*s_c)[3][32][33]) {
+    const float* __restrict__ tiles, const TileMip& mip, int item, int warp, int lane, float (*s_c)[3][32][33],
+    int nparts = 1) {
     if (gate && __ldg(gate) == 0) return;
     if (!__ldg(&icp->valid)) return;
     const int ngroups = (res + 31) >> 5;
+    // the item's part of the rows: x in [part * span, (part + 1) * span)
+    const int part = item % nparts;
+    item /= nparts;
+    const int span = (((res + nparts - 1) / nparts) + 31) & ~31;
     if (item >= res * ngroups) return;
     const int z = item / ngroups;
     const int ybase = (item - z * ngroups) << 5;
@@ -314,7 +320,9 @@ __device__ __forceinline__ void integrate_item(
         wxs = min(wxs, __shfl_xor_sync(0xffffffffu, wxs, o));
         wxe = max(wxe, __shfl_xor_sync(0xffffffffu, wxe, o));
     }
-    if (wxs > wxe) return;  // no row of this warp reaches the image
+    wxs = max(wxs, part * span);
+    wxe = min(wxe, (part + 1) * span - 1);
+    if (wxs > wxe) return;  // no row of this warp reaches the image in this part
     const int xfirst = wxs & ~31;
     if (row_on)
         for (int x = x0; x < xfirst; ++x) c = add3(c, step);
@@ -494,7 +502,7 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     __shared__ float s_c[kIntWarps][3][32][33];
     if (gate && __ldg(gate) == 0) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n_items = res * ((res + 31) >> 5);
+    const int n_items = res * ((res + 31) >> 5) * kIntParts;
     for (;;) {
         int item = 0;
         if (lane == 0) item = static_cast<int>(atomicAdd(&counters[4], 1ull));
@@ -502,7 +510,7 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
         if (item >= n_items) break;
         integrate_item<kHalf, kColor, kResid>(vox, color, icp, depth, rgb, res, vs, ox, oy, oz, trunc, max_w, fx, fy,
                                               cx, cy, W, H, min_d, max_d, nullptr, counters, bricks, nb, tiles, mip,
-                                              item, warp, lane, s_c);
+                                              item, warp, lane, s_c, kIntParts);
     }
 }
 
