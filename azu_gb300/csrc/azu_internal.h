@@ -151,6 +151,9 @@ struct PipelineFrameView {
 int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t stream, azu_pipeline** out);
 int pipeline_upload_inputs(azu_pipeline* pl, const uint16_t* depth, const uint8_t* rgb, cudaMemcpyKind kind);
 int pipeline_enqueue_front(azu_pipeline* pl, bool first);
+int pipeline_enqueue_front_on(azu_pipeline* pl, bool first, cudaStream_t s);
+int tracker_set_grid(azu_tracker* t, int blocks);
+int tracker_slots(const azu_tracker* t);
 int pipeline_enqueue_commit(azu_pipeline* pl);
 int pipeline_read_result(azu_pipeline* pl, azu_frame_result* out);
 PipelineFrameView pipeline_frame_view(azu_pipeline* pl);

@@ -1,16 +1,18 @@
 // Batching form (no counterpart in the reference): many independent scenes,
 // each with its own volume, image size and frame count, advanced one frame at
-// a time together. Per scene the frame's front (millimetre depth -> metres,
-// vertices/normals/pyramid, prediction, persistent ICP) runs as in the single
-// pipeline; integration and raycasting of all active scenes then run as ONE
-// launch per stage (tsdf.cu batches), and the whole step replays as one CUDA
-// graph per set of active scenes. Every scene's result equals its result
-// through the single pipeline bit for bit.
+// a time together. The scenes' fronts (millimetre depth -> metres,
+// vertices/normals/pyramid, persistent ICP) run side by side, each on its own
+// stream with its ICP on an equal share of the SMs (the ICP's partial slots,
+// hence its sums, do not depend on the grid); integration and raycasting of
+// all active scenes then run as ONE launch per stage (tsdf.cu batches), and
+// the whole step replays as one CUDA graph per set of active scenes. Every
+// scene's result equals its result through the single pipeline bit for bit.
 //
 // Autotuner: the integrate block size (1, 2 or 4 warps) and the raycast tile
 // shape are timed on the batch's own data — raycasts as they are (they are
 // idempotent at a fixed pose), integrations on a scratch copy of the voxels
 // that is restored afterwards — and the fastest pair is kept.
+#include <algorithm>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -22,6 +24,9 @@ struct azu_batch {
     int device = 0;
     cudaStream_t s = nullptr;
     std::vector<azu_pipeline*> scenes;
+    std::vector<cudaStream_t> fs;    // per scene: the stream of its front
+    std::vector<cudaEvent_t> fdone;  // per scene: its front is done
+    cudaEvent_t fork = nullptr;
     std::vector<int> frames;
     std::map<unsigned long long, azu_volume_batch*> vbatch;  // by active mask (first 64 scenes)
     std::map<unsigned long long, cudaGraphExec_t> graphs;
@@ -61,8 +66,16 @@ static int volume_batch_for(azu_batch* b, const std::vector<int>& active, azu_vo
 
 // The device work of one step for the given scenes (inputs already uploaded).
 static int enqueue_step(azu_batch* b, const std::vector<int>& active, bool first, azu_volume_batch* vb) {
-    for (int i : active)
-        if (int rc = pipeline_enqueue_front(b->scenes[i], first)) return rc;
+    AZU_TRY_CUDA(cudaEventRecord(b->fork, b->s));
+    for (int i : active) {
+        azu_pipeline* pl = b->scenes[i];
+        azu_tracker* t = azu_pipeline_tracker(pl);
+        if (int rc = tracker_set_grid(t, std::max(1, tracker_slots(t) / static_cast<int>(active.size())))) return rc;
+        AZU_TRY_CUDA(cudaStreamWaitEvent(b->fs[i], b->fork, 0));
+        if (int rc = pipeline_enqueue_front_on(pl, first, b->fs[i])) return rc;
+        AZU_TRY_CUDA(cudaEventRecord(b->fdone[i], b->fs[i]));
+        AZU_TRY_CUDA(cudaStreamWaitEvent(b->s, b->fdone[i], 0));
+    }
     if (int rc = volume_batch_integrate(vb, b->s)) return rc;
     if (int rc = volume_batch_raycast(vb, b->s)) return rc;
     for (int i : active)
@@ -110,6 +123,9 @@ extern "C" int azu_batch_destroy(azu_batch* b) {
     drop_graphs(b);
     for (auto& v : b->vbatch) volume_batch_destroy(v.second);
     for (azu_pipeline* pl : b->scenes) azu_pipeline_destroy(pl);
+    for (cudaStream_t q : b->fs) if (q) cudaStreamDestroy(q);
+    for (cudaEvent_t e : b->fdone) if (e) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->s) cudaStreamDestroy(b->s);
     delete b;
     return AZU_OK;
@@ -146,6 +162,19 @@ extern "C" int azu_batch_create(int device, int n, const azu_batch_scene* scenes
         azu_pipeline* pl = nullptr;
         rc = pipeline_create_on(device, &pp, b->s, &pl);
         if (!rc) b->scenes.push_back(pl);
+        cudaStream_t q = nullptr;
+        cudaEvent_t e = nullptr;
+        if (!rc && (cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)) {
+            set_error("batch front stream");
+            rc = AZU_E_CUDA;
+        }
+        b->fs.push_back(q);
+        b->fdone.push_back(e);
+    }
+    if (!rc && cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+        set_error("batch fork event");
+        rc = AZU_E_CUDA;
     }
     if (rc) {
         azu_batch_destroy(b);

@@ -67,8 +67,9 @@ struct IcpArgs {
     azu_icp_result* d_result;
     int* d_quality;
     int* d_gate;          // set to 1 when the frame grades Good
-    double* partials;     // [2][kNF][nblocks]: double in the precision form, else float
-    int* ipartials;       // [2][kNI][nblocks]
+    double* partials;     // [2][kNF][vblocks]: double in the precision form, else float
+    int* ipartials;       // [2][kNI][vblocks]
+    int vblocks;          // partial slots: the pixel split and summation order (>= the launch's blocks)
     unsigned* bar;        // [0] arrivals, [1] generation
     unsigned* err;
     unsigned* state;      // iteration outcome published by the last-arriving block
@@ -262,7 +263,7 @@ __device__ __forceinline__ void associate_range(const IcpArgs& a, const Rel& r, 
 // reads them coalesced; the partial buffers and the shared staging are sized
 // for double and reinterpreted for float.
 template <typename T>
-__device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc, int slot, double* s_red_raw) {
+__device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc, int slot, int vb, double* s_red_raw) {
     constexpr int kNV = kNF + kNI;  // 34
     T* s_red = reinterpret_cast<T*>(s_red_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -281,15 +282,15 @@ __device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc,
         s_red[warp * kNV + 33] = e1;
     }
     __syncthreads();
-    const int k = threadIdx.x, nb = gridDim.x;
+    const int k = threadIdx.x, nb = a.vblocks;
     if (k < kNF) {
         T sum = T(0);
         for (int w = 0; w < nw; ++w) sum += s_red[w * kNV + k];
-        reinterpret_cast<T*>(a.partials)[(static_cast<size_t>(slot) * kNF + k) * nb + blockIdx.x] = sum;
+        reinterpret_cast<T*>(a.partials)[(static_cast<size_t>(slot) * kNF + k) * nb + vb] = sum;
     } else if (k < kNV) {
         T sum = T(0);
         for (int w = 0; w < nw; ++w) sum += s_red[w * kNV + k];
-        a.ipartials[(static_cast<size_t>(slot) * kNI + (k - kNF)) * nb + blockIdx.x] = static_cast<int>(sum);
+        a.ipartials[(static_cast<size_t>(slot) * kNI + (k - kNF)) * nb + vb] = static_cast<int>(sum);
     }
     __syncthreads();
 }
@@ -305,7 +306,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // recursive halving as the plain path); the sum over the block's warps is
 // compensated (each value carries the exact error of its additions), and the
 // block partial enters the FP64 cross-block sum as (double) s + (double) c.
-__device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, double* s_red_raw) {
+__device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, int vb, double* s_red_raw) {
     constexpr int kNV = kNF + kNI;
     float* s_red = reinterpret_cast<float*>(s_red_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -324,7 +325,7 @@ __device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, do
         s_red[warp * kNV + 33] = e1;
     }
     __syncthreads();
-    const int k = threadIdx.x, nb = gridDim.x;
+    const int k = threadIdx.x, nb = a.vblocks;
     if (k < kNV) {
         float sum = 0.0f, c = 0.0f;
         for (int w = 0; w < nw; ++w) {
@@ -334,17 +335,34 @@ __device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, do
             c = __fadd_rn(c, err);
         }
         if (k < kNF)
-            a.partials[(static_cast<size_t>(slot) * kNF + k) * nb + blockIdx.x] =
+            a.partials[(static_cast<size_t>(slot) * kNF + k) * nb + vb] =
                 static_cast<double>(sum) + static_cast<double>(c);
         else
-            a.ipartials[(static_cast<size_t>(slot) * kNI + (k - kNF)) * nb + blockIdx.x] = static_cast<int>(sum);
+            a.ipartials[(static_cast<size_t>(slot) * kNI + (k - kNF)) * nb + vb] = static_cast<int>(sum);
     }
     __syncthreads();
 }
 
-__device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, double* s_red, int* /*unused*/) {
-    if (a.precision) reduce_block_comp(a, acc, slot, s_red);
-    else reduce_block_t<float>(a, acc, slot, s_red);
+__device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, int vb, double* s_red) {
+    if (a.precision) reduce_block_comp(a, acc, slot, vb, s_red);
+    else reduce_block_t<float>(a, acc, slot, vb, s_red);
+}
+
+// One association pass over the pixels of every partial slot this block owns
+// (slot vb: pixels vb * blockDim + t + k * vblocks * blockDim). The split and
+// each slot's sum are those of a launch with vblocks blocks whatever the grid,
+// so a smaller grid (several scenes tracked side by side) gives the same sums.
+__device__ __forceinline__ void associate_all(const IcpArgs& a, const Rel& rel, const IcpLevel& L, int n, int slot,
+                                              double* s_red) {
+    for (int vb = blockIdx.x; vb < a.vblocks; vb += gridDim.x) {
+        Acc acc;
+#pragma unroll
+        for (int k = 0; k < kNF; ++k) acc.f[k] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
+        associate_range(a, rel, L, vb * blockDim.x + threadIdx.x, a.vblocks * blockDim.x, n, acc);
+        reduce_block(a, acc, slot, vb, s_red);
+    }
 }
 
 // Sum of all block partials of `slot` in one fixed order (lane l takes blocks
@@ -359,7 +377,7 @@ __device__ __forceinline__ void reduce_grid_t(const IcpArgs& a, int slot, double
     T* s_sum = reinterpret_cast<T*>(s_sum_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
-    const int nb = gridDim.x;
+    const int nb = a.vblocks;
     for (int k = warp; k < kNF + kNI; k += nw) {
         if (k < kNF) {
             const T* src = reinterpret_cast<const T*>(a.partials) + (static_cast<size_t>(slot) * kNF + k) * nb;
@@ -822,7 +840,6 @@ __device__ int classify(const azu_icp_result& r, const float* prev) {
 
 __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
     __shared__ double s_red[(kIcpThreads / 32) * (kNF + kNI)];
-    int* s_ired = nullptr;
     __shared__ SolveSmem sm;
     __shared__ LevelState st;
     __shared__ Rel s_rel;
@@ -849,13 +866,9 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
         if (threadIdx.x == 0) compute_rel(s_start, s_refinv, s_rel);
         __syncthreads();
         const Rel rel = s_rel;
-        Acc acc;
-        for (int k = 0; k < kNF; ++k) acc.f[k] = 0.0f;
-        for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
         const int iw = L.W - 2, ih = L.H - 2;
         const int n = iw > 0 && ih > 0 ? iw * ih : 0;
-        associate_range(a, rel, L, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, acc);
-        reduce_block(a, acc, 0, s_red, s_ired);
+        associate_all(a, rel, L, n, 0, s_red);
         grid_sync(a.bar, a.err, gridDim.x, gen);
         reduce_grid(a, 0, sm.sum, sm.isum);
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -906,13 +919,7 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
                 if (threadIdx.x == 0) compute_rel(st.pose, s_refinv, s_rel);
                 __syncthreads();
                 const Rel rel = s_rel;
-                Acc acc;
-#pragma unroll
-                for (int k = 0; k < kNF; ++k) acc.f[k] = 0.0f;
-#pragma unroll
-                for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
-                associate_range(a, rel, L, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, n, acc);
-                reduce_block(a, acc, slot, s_red, s_ired);
+                associate_all(a, rel, L, n, slot, s_red);
                 constexpr int kWords = static_cast<int>(sizeof(LevelState) / 4);
                 unsigned* st_words = reinterpret_cast<unsigned*>(&st);
                 if (arrive_last(a.bar, a.err, gridDim.x, &s_last)) {
@@ -996,7 +1003,8 @@ struct azu_tracker {
     float* D[3] = {nullptr, nullptr, nullptr};
     int W = 0, H = 0;
     bool prepared = false;
-    int nblocks = 0;
+    int nblocks = 0;      // partial slots (and the default grid): the SMs' resident blocks
+    int grid_blocks = 0;  // launch grid, <= nblocks (batches track scenes side by side)
     double* partials = nullptr;
     int* ipartials = nullptr;
     unsigned* bar = nullptr;  // [0] arrivals [1] generation [2] error [4..] published state
@@ -1063,14 +1071,24 @@ static void fill_args_p(azu_tracker* t, const azu_tracker_params& p, IcpArgs& a,
     a.build_level = -1;
     a.partials = t->partials;
     a.ipartials = t->ipartials;
+    a.vblocks = t->nblocks;
     a.bar = t->bar;
     a.err = t->bar + 2;
     a.state = t->bar + 4;
 }
 
+// Launch grid of the tracker's ICP (0: all partial slots, one block each);
+// any grid gives the same sums.
+int tracker_set_grid(azu_tracker* t, int blocks) {
+    AZU_CHECK_ARG(t != nullptr, "null handle");
+    t->grid_blocks = blocks <= 0 ? 0 : std::min(blocks, t->nblocks);
+    return AZU_OK;
+}
+int tracker_slots(const azu_tracker* t) { return t ? t->nblocks : 0; }
+
 int icp_launch(azu_tracker* t, const IcpArgs& a, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(t->nblocks);
+    cfg.gridDim = dim3(t->grid_blocks > 0 ? t->grid_blocks : t->nblocks);
     cfg.blockDim = dim3(kIcpThreads);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -1444,6 +1462,7 @@ extern "C" int azu_icp_build_system_noalloc(const float* d_live_vertices, const 
     a.d_ref = d_poses + 16;
     a.partials = reinterpret_cast<double*>(slot.base + kOffPartials);
     a.ipartials = reinterpret_cast<int*>(slot.base + kOffIPartials);
+    a.vblocks = slot.nblocks;
     a.bar = d_bar;
     a.err = d_bar + 2;
     a.state = nullptr;  // build mode publishes no iteration state

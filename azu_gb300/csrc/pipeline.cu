@@ -185,12 +185,13 @@ static int enqueue_track(azu_pipeline* pl, bool first, cudaStream_t s) {
     return mark(pl, 3, s);
 }
 
-// Front of one frame after the inputs are on the device, on the pipeline's
-// stream: depth, frame maps, prediction and tracking.
-int pipeline_enqueue_front(azu_pipeline* pl, bool first) {
-    if (int rc = enqueue_input(pl, pl->s)) return rc;
-    return enqueue_track(pl, first, pl->s);
+// Front of one frame after the inputs are on the device, on stream s (the
+// pipeline's own by default): depth, frame maps and tracking.
+int pipeline_enqueue_front_on(azu_pipeline* pl, bool first, cudaStream_t s) {
+    if (int rc = enqueue_input(pl, s)) return rc;
+    return enqueue_track(pl, first, s);
 }
+int pipeline_enqueue_front(azu_pipeline* pl, bool first) { return pipeline_enqueue_front_on(pl, first, pl->s); }
 
 // The model commit that closes a frame (after the gated integrate + raycast).
 int pipeline_enqueue_commit(azu_pipeline* pl) {
