@@ -906,24 +906,34 @@ __global__ void depth_tiles_batch_kernel(const IntegrateArgs* __restrict__ A, co
                      a.mip.w[0] * a.mip.h[0], a.tiles, a.gate);
 }
 
-__global__ void integrate_setup_batch_kernel(const IntegrateArgs* __restrict__ A, unsigned long long** counters) {
+__global__ void integrate_setup_batch_kernel(const IntegrateArgs* __restrict__ A, unsigned* __restrict__ work) {
     const IntegrateArgs& a = A[blockIdx.x];
     integrate_setup_body(a.pose, a.res, a.vs, a.ox, a.oy, a.oz, a.trunc, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.max_d,
                          a.icp_out, a.counters, a.tiles, a.mip, true);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *work = 0;  // next item of the batch integrate
 }
 
+// Persistent over the items of all scenes (32 rows x half a row each, scene by
+// prefix offsets): every warp takes the next item from the batch's counter.
 template <int kWarps>
 __global__ void __launch_bounds__(kWarps * 32) integrate_batch_kernel(const IntegrateArgs* __restrict__ A,
-                                                                      const int* __restrict__ off, int n) {
+                                                                      const int* __restrict__ off, int n,
+                                                                      unsigned* __restrict__ work) {
     __shared__ float s_c[kWarps][3][32][33];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int item = blockIdx.x * kWarps + warp;
-    const int s = batch_find(off, n, item);
-    const IntegrateArgs& a = A[s];
-    integrate_item<false, false, false>(a.vox, nullptr, a.icp, a.depth, nullptr, a.res, a.vs, a.ox, a.oy, a.oz,
-                                        a.trunc, a.max_w, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.min_d, a.max_d,
-                                        a.gate, a.counters, a.bricks, a.nb, a.tiles, a.mip, item - __ldg(off + s),
-                                        warp, lane, s_c);
+    const int total = __ldg(off + n);
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = static_cast<int>(atomicAdd(work, 1u));
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) break;
+        const int s = batch_find(off, n, item);
+        const IntegrateArgs& a = A[s];
+        integrate_item<false, false, false>(a.vox, nullptr, a.icp, a.depth, nullptr, a.res, a.vs, a.ox, a.oy, a.oz,
+                                            a.trunc, a.max_w, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.min_d, a.max_d,
+                                            a.gate, a.counters, a.bricks, a.nb, a.tiles, a.mip, item - __ldg(off + s),
+                                            warp, lane, s_c, kIntParts);
+    }
 }
 
 __global__ void brick_dist_batch_kernel(const RaycastArgs* __restrict__ A, const int* __restrict__ off, int n,
@@ -955,7 +965,9 @@ struct azu_volume_batch {
     azu::IntegrateArgs* d_int = nullptr;
     azu::RaycastArgs* d_ray = nullptr;
     int* d_off = nullptr;  // [0..n] tile blocks, [n+1..2n+1] integrate items, [2n+2..3n+2] bricks, [3n+3..4n+3] ray tiles
+    unsigned* d_work = nullptr;  // next integrate item
     int tiles_blocks = 0, items = 0, brick_blocks = 0, ray_blocks = 0;
+    int int_grid[3] = {0, 0, 0};  // resident blocks of the persistent integrate, by 1, 2, 4 warps
     int int_warps = 4, ray_w = 32, ray_h = 8;
 };
 
@@ -972,7 +984,7 @@ static int batch_upload_offsets(azu_volume_batch* b) {
         tb += (mip.w[0] * mip.h[0] + 31) / 32;
         off[n + 1 + i] = it;
         const int res = f.vol->p.resolution;
-        it += res * ((res + 31) / 32);
+        it += res * ((res + 31) / 32) * kIntParts;
         off[2 * (n + 1) + i] = bb;
         const size_t nbr = static_cast<size_t>(f.vol->nb) * f.vol->nb * f.vol->nb;
         bb += static_cast<int>((nbr + 255) / 256);
@@ -1024,6 +1036,16 @@ int volume_batch_create(const PipelineFrameView* views, int n, azu_volume_batch*
         cudaError_t e = cudaMalloc(&b->d_int, n * sizeof(IntegrateArgs));
         if (!e) e = cudaMalloc(&b->d_ray, n * sizeof(RaycastArgs));
         if (!e) e = cudaMalloc(&b->d_off, 4 * (n + 1) * sizeof(int));
+        if (!e) e = cudaMalloc(&b->d_work, sizeof(unsigned));
+        int sms = 0;
+        if (!e) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, views[0].vol->device);
+        const void* kernels[3] = {(const void*)integrate_batch_kernel<1>, (const void*)integrate_batch_kernel<2>,
+                                  (const void*)integrate_batch_kernel<4>};
+        for (int k = 0; k < 3 && !e; ++k) {
+            int occ = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernels[k], 32 << k, 0);
+            b->int_grid[k] = std::max(1, sms * std::max(occ, 1));
+        }
         if (!e) e = cudaMemcpy(b->d_int, ia.data(), n * sizeof(IntegrateArgs), cudaMemcpyHostToDevice);
         if (!e) e = cudaMemcpy(b->d_ray, ra.data(), n * sizeof(RaycastArgs), cudaMemcpyHostToDevice);
         if (e) { set_error("batch allocation: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; }
@@ -1039,6 +1061,7 @@ void volume_batch_destroy(azu_volume_batch* b) {
     if (b->d_int) cudaFree(b->d_int);
     if (b->d_ray) cudaFree(b->d_ray);
     if (b->d_off) cudaFree(b->d_off);
+    if (b->d_work) cudaFree(b->d_work);
     delete b;
 }
 
@@ -1062,13 +1085,14 @@ int volume_batch_integrate(azu_volume_batch* b, cudaStream_t s) {
     const int n = b->n;
     depth_tiles_batch_kernel<<<b->tiles_blocks, 256, 0, s>>>(b->d_int, b->d_off, n);
     AZU_LAUNCH_CHECK();
-    integrate_setup_batch_kernel<<<n, 256, 0, s>>>(b->d_int, nullptr);
+    integrate_setup_batch_kernel<<<n, 256, 0, s>>>(b->d_int, b->d_work);
     AZU_LAUNCH_CHECK();
     const int* ioff = b->d_off + (n + 1);
-    const int blocks = (b->items + b->int_warps - 1) / b->int_warps;
-    if (b->int_warps == 1) integrate_batch_kernel<1><<<blocks, 32, 0, s>>>(b->d_int, ioff, n);
-    else if (b->int_warps == 2) integrate_batch_kernel<2><<<blocks, 64, 0, s>>>(b->d_int, ioff, n);
-    else integrate_batch_kernel<4><<<blocks, 128, 0, s>>>(b->d_int, ioff, n);
+    const int k = b->int_warps == 1 ? 0 : (b->int_warps == 2 ? 1 : 2);
+    const int blocks = std::min(b->int_grid[k], (b->items + b->int_warps - 1) / b->int_warps);
+    if (b->int_warps == 1) integrate_batch_kernel<1><<<blocks, 32, 0, s>>>(b->d_int, ioff, n, b->d_work);
+    else if (b->int_warps == 2) integrate_batch_kernel<2><<<blocks, 64, 0, s>>>(b->d_int, ioff, n, b->d_work);
+    else integrate_batch_kernel<4><<<blocks, 128, 0, s>>>(b->d_int, ioff, n, b->d_work);
     AZU_LAUNCH_CHECK();
     for (const PipelineFrameView& f : b->views) f.vol->integrated_frames++;
     return AZU_OK;
