@@ -8,6 +8,8 @@
 
 #include "../../include/azu_gpu.h"
 
+struct azu_icp_batch;  // scenes tracked side by side (icp.cu)
+
 namespace azu {
 
 // Thread-local last-error text behind azu_last_error().
@@ -152,8 +154,25 @@ int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t st
 int pipeline_upload_inputs(azu_pipeline* pl, const uint16_t* depth, const uint8_t* rgb, cudaMemcpyKind kind);
 int pipeline_enqueue_front(azu_pipeline* pl, bool first);
 int pipeline_enqueue_front_on(azu_pipeline* pl, bool first, cudaStream_t s);
-int tracker_set_grid(azu_tracker* t, int blocks);
-int tracker_slots(const azu_tracker* t);
+// The device buffers one pipeline frame's tracking reads and writes.
+struct TrackDev {
+    const float* mv;
+    const float* mn;
+    int MW, MH;
+    const float* d_estimate;
+    const float* d_ref;
+    const float* d_prev;
+    float* d_pose_out;
+    azu_icp_result* d_result;
+    int* d_quality;
+    int* d_gate;
+};
+int icp_batch_create(azu_tracker* const* t, const TrackDev* d, int n, azu_icp_batch** out);
+void icp_batch_destroy(azu_icp_batch* b);
+int icp_batch_launch(azu_icp_batch* b, cudaStream_t s);
+TrackDev pipeline_track_dev(azu_pipeline* pl);
+int pipeline_enqueue_input_on(azu_pipeline* pl, cudaStream_t s);
+int pipeline_enqueue_track_on(azu_pipeline* pl, bool first, cudaStream_t s);
 int pipeline_enqueue_commit(azu_pipeline* pl);
 int pipeline_read_result(azu_pipeline* pl, azu_frame_result* out);
 PipelineFrameView pipeline_frame_view(azu_pipeline* pl);

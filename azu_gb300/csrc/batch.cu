@@ -1,12 +1,13 @@
 // Batching form (no counterpart in the reference): many independent scenes,
 // each with its own volume, image size and frame count, advanced one frame at
-// a time together. The scenes' fronts (millimetre depth -> metres,
-// vertices/normals/pyramid, persistent ICP) run side by side, each on its own
-// stream with its ICP on an equal share of the SMs (the ICP's partial slots,
-// hence its sums, do not depend on the grid); integration and raycasting of
-// all active scenes then run as ONE launch per stage (tsdf.cu batches), and
-// the whole step replays as one CUDA graph per set of active scenes. Every
-// scene's result equals its result through the single pipeline bit for bit.
+// a time together. The scenes' input stages (millimetre depth -> metres,
+// vertices/normals/pyramid, depth tiles) run side by side, each on its own
+// stream; then ONE cooperative ICP launch tracks every scene on an equal
+// share of the SMs (the ICP's partial slots, hence its sums, do not depend on
+// the blocks it runs on); integration and raycasting of all active scenes run
+// as ONE launch per stage (tsdf.cu batches), and the whole step replays as one
+// CUDA graph per set of active scenes. Every scene's result equals its result
+// through the single pipeline bit for bit.
 //
 // Autotuner: the integrate block size (1, 2 or 4 warps) and the raycast tile
 // shape are timed on the batch's own data — raycasts as they are (they are
@@ -29,6 +30,7 @@ struct azu_batch {
     cudaEvent_t fork = nullptr;
     std::vector<int> frames;
     std::map<unsigned long long, azu_volume_batch*> vbatch;  // by active mask (first 64 scenes)
+    std::map<unsigned long long, azu_icp_batch*> ibatch;
     std::map<unsigned long long, cudaGraphExec_t> graphs;
     int int_warps = 4, ray_w = 32, ray_h = 8;
     bool tuned = false;
@@ -42,6 +44,26 @@ static unsigned long long mask_of(const std::vector<int>& active) {
     unsigned long long m = 0;
     for (int i : active) m |= 1ull << (i & 63);
     return m ^ (static_cast<unsigned long long>(active.size()) << 58);
+}
+
+static int icp_batch_for(azu_batch* b, const std::vector<int>& active, azu_icp_batch** out) {
+    const unsigned long long key = mask_of(active);
+    auto it = b->ibatch.find(key);
+    if (it != b->ibatch.end()) {
+        *out = it->second;
+        return AZU_OK;
+    }
+    std::vector<azu_tracker*> t;
+    std::vector<TrackDev> d;
+    for (int i : active) {
+        t.push_back(azu_pipeline_tracker(b->scenes[i]));
+        d.push_back(pipeline_track_dev(b->scenes[i]));
+    }
+    azu_icp_batch* ib = nullptr;
+    if (int rc = icp_batch_create(t.data(), d.data(), static_cast<int>(active.size()), &ib)) return rc;
+    b->ibatch[key] = ib;
+    *out = ib;
+    return AZU_OK;
 }
 
 static int volume_batch_for(azu_batch* b, const std::vector<int>& active, azu_volume_batch** out) {
@@ -65,16 +87,20 @@ static int volume_batch_for(azu_batch* b, const std::vector<int>& active, azu_vo
 }
 
 // The device work of one step for the given scenes (inputs already uploaded).
-static int enqueue_step(azu_batch* b, const std::vector<int>& active, bool first, azu_volume_batch* vb) {
+static int enqueue_step(azu_batch* b, const std::vector<int>& active, bool first, azu_volume_batch* vb,
+                        azu_icp_batch* ib) {
     AZU_TRY_CUDA(cudaEventRecord(b->fork, b->s));
     for (int i : active) {
-        azu_pipeline* pl = b->scenes[i];
-        azu_tracker* t = azu_pipeline_tracker(pl);
-        if (int rc = tracker_set_grid(t, std::max(1, tracker_slots(t) / static_cast<int>(active.size())))) return rc;
         AZU_TRY_CUDA(cudaStreamWaitEvent(b->fs[i], b->fork, 0));
-        if (int rc = pipeline_enqueue_front_on(pl, first, b->fs[i])) return rc;
+        if (int rc = pipeline_enqueue_input_on(b->scenes[i], b->fs[i])) return rc;
         AZU_TRY_CUDA(cudaEventRecord(b->fdone[i], b->fs[i]));
         AZU_TRY_CUDA(cudaStreamWaitEvent(b->s, b->fdone[i], 0));
+    }
+    if (first) {
+        for (int i : active)
+            if (int rc = pipeline_enqueue_track_on(b->scenes[i], true, b->s)) return rc;
+    } else if (int rc = icp_batch_launch(ib, b->s)) {
+        return rc;
     }
     if (int rc = volume_batch_integrate(vb, b->s)) return rc;
     if (int rc = volume_batch_raycast(vb, b->s)) return rc;
@@ -122,6 +148,7 @@ extern "C" int azu_batch_destroy(azu_batch* b) {
     if (b->s) cudaStreamSynchronize(b->s);
     drop_graphs(b);
     for (auto& v : b->vbatch) volume_batch_destroy(v.second);
+    for (auto& v : b->ibatch) icp_batch_destroy(v.second);
     for (azu_pipeline* pl : b->scenes) azu_pipeline_destroy(pl);
     for (cudaStream_t q : b->fs) if (q) cudaStreamDestroy(q);
     for (cudaEvent_t e : b->fdone) if (e) cudaEventDestroy(e);
@@ -303,15 +330,17 @@ extern "C" int azu_batch_process(azu_batch* b, const uint16_t* const* depth_mm, 
             return rc;
     azu_volume_batch* vb = nullptr;
     if (int rc = volume_batch_for(b, active, &vb)) return rc;
+    azu_icp_batch* ib = nullptr;
+    if (int rc = icp_batch_for(b, active, &ib)) return rc;
     if (first || !b->use_graph) {
-        if (int rc = enqueue_step(b, active, first, vb)) return rc;
+        if (int rc = enqueue_step(b, active, first, vb, ib)) return rc;
     } else {
         const unsigned long long key = mask_of(active);
         auto it = b->graphs.find(key);
         cudaGraphExec_t exec = nullptr;
         if (it == b->graphs.end()) {
             AZU_TRY_CUDA(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal));
-            const int rc = enqueue_step(b, active, false, vb);
+            const int rc = enqueue_step(b, active, false, vb, ib);
             cudaGraph_t g = nullptr;
             const cudaError_t e = cudaStreamEndCapture(b->s, &g);
             cudaError_t ei = cudaErrorUnknown;
@@ -320,7 +349,7 @@ extern "C" int azu_batch_process(azu_batch* b, const uint16_t* const* depth_mm, 
             if (rc || e != cudaSuccess || ei != cudaSuccess) {
                 cudaGetLastError();
                 b->use_graph = false;  // capture is an optimisation only
-                if (int rc2 = enqueue_step(b, active, false, vb)) return rc2;
+                if (int rc2 = enqueue_step(b, active, false, vb, ib)) return rc2;
                 exec = nullptr;
             } else {
                 b->graphs[key] = exec;

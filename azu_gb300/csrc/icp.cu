@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 #include <mutex>
 
 #include "azu_internal.h"
@@ -353,8 +354,8 @@ __device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, int vb, doubl
 // each slot's sum are those of a launch with vblocks blocks whatever the grid,
 // so a smaller grid (several scenes tracked side by side) gives the same sums.
 __device__ __forceinline__ void associate_all(const IcpArgs& a, const Rel& rel, const IcpLevel& L, int n, int slot,
-                                              double* s_red) {
-    for (int vb = blockIdx.x; vb < a.vblocks; vb += gridDim.x) {
+                                              double* s_red, int gb, int gn) {
+    for (int vb = gb; vb < a.vblocks; vb += gn) {
         Acc acc;
 #pragma unroll
         for (int k = 0; k < kNF; ++k) acc.f[k] = 0.0f;
@@ -838,7 +839,10 @@ __device__ int classify(const azu_icp_result& r, const float* prev) {
     return q;
 }
 
-__global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
+// The whole track of one scene by a group of gn co-resident blocks (this one
+// is block gb of the group): a whole grid for a single tracker, a share of one
+// for scenes tracked side by side.
+__device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
     __shared__ double s_red[(kIcpThreads / 32) * (kNF + kNI)];
     __shared__ SolveSmem sm;
     __shared__ LevelState st;
@@ -868,10 +872,10 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
         const Rel rel = s_rel;
         const int iw = L.W - 2, ih = L.H - 2;
         const int n = iw > 0 && ih > 0 ? iw * ih : 0;
-        associate_all(a, rel, L, n, 0, s_red);
-        grid_sync(a.bar, a.err, gridDim.x, gen);
+        associate_all(a, rel, L, n, 0, s_red, gb, gn);
+        grid_sync(a.bar, a.err, gn, gen);
         reduce_grid(a, 0, sm.sum, sm.isum);
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (gb == 0 && threadIdx.x == 0) {
             int k = 0;
             for (int i = 0; i < 6; ++i)
                 for (int j = i; j < 6; ++j) {
@@ -919,10 +923,10 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
                 if (threadIdx.x == 0) compute_rel(st.pose, s_refinv, s_rel);
                 __syncthreads();
                 const Rel rel = s_rel;
-                associate_all(a, rel, L, n, slot, s_red);
+                associate_all(a, rel, L, n, slot, s_red, gb, gn);
                 constexpr int kWords = static_cast<int>(sizeof(LevelState) / 4);
                 unsigned* st_words = reinterpret_cast<unsigned*>(&st);
-                if (arrive_last(a.bar, a.err, gridDim.x, &s_last)) {
+                if (arrive_last(a.bar, a.err, gn, &s_last)) {
                     reduce_grid(a, slot, sm.sum, sm.isum);
                     if (threadIdx.x < 32) solve_step(a, level, sm, st);
                     __syncthreads();
@@ -973,7 +977,7 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
         if (!s_retry) break;
     }
 
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (gb == 0 && threadIdx.x == 0) {
         azu_icp_result res = s_res;
         res.status = ld_acquire(a.err) ? AZU_E_TIMEOUT : AZU_OK;
         *a.d_result = res;
@@ -991,6 +995,21 @@ __global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) {
     }
 }
 
+__global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) { icp_body(a, blockIdx.x, gridDim.x); }
+
+// Scenes tracked side by side in one cooperative launch: scene s owns blocks
+// [first[s], first[s + 1]) and its own barrier words and partial slots.
+__global__ void __launch_bounds__(kIcpThreads) icp_batch_kernel(const IcpArgs* __restrict__ args,
+                                                                const int* __restrict__ first, int n) {
+    __shared__ IcpArgs sa;
+    int s = 0;
+    while (s + 1 < n && static_cast<int>(blockIdx.x) >= __ldg(first + s + 1)) ++s;
+    const int f0 = __ldg(first + s), f1 = __ldg(first + s + 1);
+    if (threadIdx.x == 0) sa = args[s];
+    __syncthreads();
+    icp_body(sa, static_cast<int>(blockIdx.x) - f0, f1 - f0);
+}
+
 }  // namespace azu
 
 // ---------------------------------------------------------------------------
@@ -1003,8 +1022,7 @@ struct azu_tracker {
     float* D[3] = {nullptr, nullptr, nullptr};
     int W = 0, H = 0;
     bool prepared = false;
-    int nblocks = 0;      // partial slots (and the default grid): the SMs' resident blocks
-    int grid_blocks = 0;  // launch grid, <= nblocks (batches track scenes side by side)
+    int nblocks = 0;  // partial slots and launch grid: the SMs' resident blocks
     double* partials = nullptr;
     int* ipartials = nullptr;
     unsigned* bar = nullptr;  // [0] arrivals [1] generation [2] error [4..] published state
@@ -1077,18 +1095,9 @@ static void fill_args_p(azu_tracker* t, const azu_tracker_params& p, IcpArgs& a,
     a.state = t->bar + 4;
 }
 
-// Launch grid of the tracker's ICP (0: all partial slots, one block each);
-// any grid gives the same sums.
-int tracker_set_grid(azu_tracker* t, int blocks) {
-    AZU_CHECK_ARG(t != nullptr, "null handle");
-    t->grid_blocks = blocks <= 0 ? 0 : std::min(blocks, t->nblocks);
-    return AZU_OK;
-}
-int tracker_slots(const azu_tracker* t) { return t ? t->nblocks : 0; }
-
 int icp_launch(azu_tracker* t, const IcpArgs& a, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(t->grid_blocks > 0 ? t->grid_blocks : t->nblocks);
+    cfg.gridDim = dim3(t->nblocks);
     cfg.blockDim = dim3(kIcpThreads);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -1101,19 +1110,89 @@ int icp_launch(azu_tracker* t, const IcpArgs& a, cudaStream_t s) {
 }
 
 // Pipeline entry: track against device poses; result/grade stay on the device.
+static void track_args(azu_tracker* t, const TrackDev& d, IcpArgs& a) {
+    fill_args(t, a, d.mv, d.mn, d.MW, d.MH);
+    a.d_estimate = d.d_estimate;
+    a.d_ref = d.d_ref;
+    a.d_prev = d.d_prev;
+    a.d_pose_out = d.d_pose_out;
+    a.d_result = d.d_result;
+    a.d_quality = d.d_quality;
+    a.d_gate = d.d_gate;
+}
+
 int tracker_track_dev(azu_tracker* t, const float* mv, const float* mn, int MW, int MH, const float* d_estimate,
                       const float* d_ref, const float* d_prev, float* d_pose_out, azu_icp_result* d_result,
                       int* d_quality, int* d_gate, cudaStream_t s) {
     IcpArgs a;
-    fill_args(t, a, mv, mn, MW, MH);
-    a.d_estimate = d_estimate;
-    a.d_ref = d_ref;
-    a.d_prev = d_prev;
-    a.d_pose_out = d_pose_out;
-    a.d_result = d_result;
-    a.d_quality = d_quality;
-    a.d_gate = d_gate;
+    track_args(t, TrackDev{mv, mn, MW, MH, d_estimate, d_ref, d_prev, d_pose_out, d_result, d_quality, d_gate}, a);
     return icp_launch(t, a, s);
+}
+
+}  // namespace azu
+
+// Scenes tracked side by side (the batch): one cooperative launch, the
+// resident blocks split evenly, each scene's ICP on its own share. Any share
+// gives the sums of the scene's own tracker (its partial slots are fixed).
+struct azu_icp_batch {
+    int n = 0, grid = 0;
+    azu::IcpArgs* d_args = nullptr;
+    int* d_first = nullptr;
+};
+
+namespace azu {
+
+void icp_batch_destroy(azu_icp_batch* b) {
+    if (!b) return;
+    if (b->d_args) cudaFree(b->d_args);
+    if (b->d_first) cudaFree(b->d_first);
+    delete b;
+}
+
+int icp_batch_create(azu_tracker* const* t, const TrackDev* d, int n, azu_icp_batch** out) {
+    AZU_CHECK_ARG(t != nullptr && d != nullptr && out != nullptr && n >= 1, "null argument");
+    *out = nullptr;
+    int sms = 0, occ = 0;
+    AZU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t[0]->device));
+    AZU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, icp_batch_kernel, kIcpThreads, 0));
+    const int grid = sms * std::min(occ, 2);
+    AZU_CHECK_ARG(grid >= n, "more scenes than resident ICP blocks");
+    std::vector<IcpArgs> args(n);
+    std::vector<int> first(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        AZU_CHECK_ARG(t[i] != nullptr, "null tracker");
+        track_args(t[i], d[i], args[i]);
+        first[i + 1] = first[i] + grid / n;
+    }
+    azu_icp_batch* b = new azu_icp_batch();
+    b->n = n;
+    b->grid = first[n];
+    cudaError_t e = cudaMalloc(&b->d_args, n * sizeof(IcpArgs));
+    if (!e) e = cudaMalloc(&b->d_first, (n + 1) * sizeof(int));
+    if (!e) e = cudaMemcpy(b->d_args, args.data(), n * sizeof(IcpArgs), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(b->d_first, first.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice);
+    if (e) {
+        set_error("icp batch: %s", cudaGetErrorString(e));
+        icp_batch_destroy(b);
+        return AZU_E_NOMEM;
+    }
+    *out = b;
+    return AZU_OK;
+}
+
+int icp_batch_launch(azu_icp_batch* b, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(b->grid);
+    cfg.blockDim = dim3(kIcpThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    AZU_TRY_CUDA(cudaLaunchKernelEx(&cfg, icp_batch_kernel, static_cast<const IcpArgs*>(b->d_args),
+                                    static_cast<const int*>(b->d_first), b->n));
+    return AZU_OK;
 }
 
 int tracker_prepare_dev(azu_tracker* t, const float* d_depth, int W, int H, cudaStream_t s) {

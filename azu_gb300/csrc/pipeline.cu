@@ -185,6 +185,17 @@ static int enqueue_track(azu_pipeline* pl, bool first, cudaStream_t s) {
     return mark(pl, 3, s);
 }
 
+int pipeline_enqueue_input_on(azu_pipeline* pl, cudaStream_t s) { return enqueue_input(pl, s); }
+int pipeline_enqueue_track_on(azu_pipeline* pl, bool first, cudaStream_t s) { return enqueue_track(pl, first, s); }
+
+// What this pipeline's tracking of a frame reads and writes (a batch tracks
+// its scenes together with it).
+TrackDev pipeline_track_dev(azu_pipeline* pl) {
+    PoseState* st = pl->d_st;
+    return TrackDev{pl->d_model_v, pl->d_model_n, pl->W, pl->H, st->pred, st->model_pose, st->prev, st->cur,
+                    pl->d_icp, &st->quality, &st->gate};
+}
+
 // Front of one frame after the inputs are on the device, on stream s (the
 // pipeline's own by default): depth, frame maps and tracking.
 int pipeline_enqueue_front_on(azu_pipeline* pl, bool first, cudaStream_t s) {
