@@ -27,7 +27,6 @@ import re
 import statistics
 import subprocess
 import sys
-import threading
 import time
 
 import numpy as np
@@ -51,7 +50,8 @@ def _dist():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms (nvidia-smi's
+    own loop, in a child process) during a timed region."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -60,28 +60,31 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.samples = []
-        self._stop = threading.Event()
-        self._th = None
-
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if out.returncode == 0 and out.stdout.strip():
-                    self.samples.append([v.strip() for v in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        self._p = None
 
     def __enter__(self):
-        self._th = threading.Thread(target=self._run, daemon=True)
-        self._th.start()
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                        "--format=csv,noheader,nounits", "-lms", "50"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.05)  # the first sample lands before the region starts
+        except Exception:
+            self._p = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._th.join(timeout=10)
+        if self._p is None:
+            return
+        self._p.terminate()
+        try:
+            out, _ = self._p.communicate(timeout=10)
+        except Exception:
+            self._p.kill()
+            out, _ = self._p.communicate()
+        for line in (out or "").splitlines():
+            vals = [v.strip() for v in line.split(",")]
+            if len(vals) >= 7:
+                self.samples.append(vals)
 
     def summary(self):
         if not self.samples:
@@ -491,17 +494,18 @@ def run_gpu(args):
     Ke = K
     qual = []
     barrier()
-    t0 = time.perf_counter()
-    e0.record(stream)
-    for k in range(Ke):
-        r = pl.process_frame(h_raw_np[frame % SEQ_FRAMES], h_rgb_np)
-        qual.append(r["quality"])
-        frame += 1
-        if frame % MESH_EVERY == 0:
-            mc.extract_counts(vol)
-    e1.record(stream)
-    barrier()
-    e2e_wall = time.perf_counter() - t0
+    with ClockSampler(dev) as clk_e2e:
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for k in range(Ke):
+            r = pl.process_frame(h_raw_np[frame % SEQ_FRAMES], h_rgb_np)
+            qual.append(r["quality"])
+            frame += 1
+            if frame % MESH_EVERY == 0:
+                mc.extract_counts(vol)
+        e1.record(stream)
+        barrier()
+        e2e_wall = time.perf_counter() - t0
     e2e_ms = e0.elapsed_time(e1)
     # per-stage device times, from a short run with stage events (each frame
     # then completes before the call returns)
@@ -551,7 +555,8 @@ def run_gpu(args):
                    "cache": "inputs larger than L2 (1.07 GB volume read and written each frame)",
                    "graph": bool(pl.lib.azu_pipeline_uses_graph(pl.h)), "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": int(raw[0].nbytes + rgb.nbytes),
-                "d2h_bytes_per_step": D2H_RESULT_BYTES, "wall_frames_per_s": Ke / e2e_wall},
+                "d2h_bytes_per_step": D2H_RESULT_BYTES, "wall_frames_per_s": Ke / e2e_wall,
+                "clocks": clk_e2e.summary()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "integrate (setup + voxel update)", "peak_source": peak_kind,
