@@ -35,7 +35,7 @@ int launch_prepare_live(const float* d_depth, int W, int H, float fx, float fy, 
 
 constexpr int kNF = 28;   // 21 A + 6 b + residual
 constexpr int kNI = 6;    // inliers, valid_live, valid_model, projected, dist_filtered, angle_filtered
-constexpr int kIcpThreads = 256;
+constexpr int kIcpThreads = 512;
 constexpr unsigned kSpinLimit = 1u << 22;
 
 constexpr float kHuberK = 0.02f;
@@ -368,7 +368,8 @@ __device__ __forceinline__ void associate_all(const IcpArgs& a, const Rel& rel, 
 
 // Sum of all block partials of `slot` in one fixed order (lane l takes blocks
 // l, l + 32, ...; then a fixed shuffle tree), so the result does not depend
-// on which block computes it. All loads of a lane are issued before the adds.
+// on which block computes it. The loads of several values are issued before
+// any add.
 // The sums land in s_sum as T (float sums in the first half of the storage).
 constexpr int kMaxGridBlocks = 512;
 constexpr int kPerLane = kMaxGridBlocks / 32;
@@ -407,6 +408,50 @@ __device__ __forceinline__ void reduce_grid_t(const IcpArgs& a, int slot, double
             for (int j = 0; j < kPerLane; ++j) sum += v[j];
             for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
             if (lane == 0) s_isum[kk] = sum;
+        }
+    }
+    __syncthreads();
+}
+
+// FP32 path: a warp takes two values per round with all their loads in flight
+// (one L2 round trip per two values); per value the same order as above.
+template <>
+__device__ __forceinline__ void reduce_grid_t<float>(const IcpArgs& a, int slot, double* s_sum_raw, int* s_isum) {
+    float* s_sum = reinterpret_cast<float*>(s_sum_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    const int nb = a.vblocks;
+    for (int k0 = warp; k0 < kNF + kNI; k0 += 2 * nw) {
+        unsigned w[2][kPerLane];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int k = k0 + r * nw;
+            const unsigned* src =
+                k < kNF ? reinterpret_cast<const unsigned*>(a.partials) + (static_cast<size_t>(slot) * kNF + k) * nb
+                        : reinterpret_cast<const unsigned*>(a.ipartials) +
+                              (static_cast<size_t>(slot) * kNI + (k - kNF)) * nb;
+#pragma unroll
+            for (int j = 0; j < kPerLane; ++j) {
+                const int b = lane + 32 * j;
+                w[r][j] = (b < nb && k < kNF + kNI) ? __ldcg(src + b) : 0u;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int k = k0 + r * nw;
+            if (k < kNF) {
+                float sum = 0.0f;
+#pragma unroll
+                for (int j = 0; j < kPerLane; ++j) sum += __uint_as_float(w[r][j]);
+                for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+                if (lane == 0) s_sum[k] = sum;
+            } else if (k < kNF + kNI) {
+                int sum = 0;
+#pragma unroll
+                for (int j = 0; j < kPerLane; ++j) sum += static_cast<int>(w[r][j]);
+                for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+                if (lane == 0) s_isum[k - kNF] = sum;
+            }
         }
     }
     __syncthreads();
