@@ -1479,9 +1479,10 @@ extern "C" int azu_tracker_load_live(azu_tracker* t, int level, const float* d_v
 // device array that every GPU loading the library holds until exit.
 //
 // Limit: the array holds partials for kStaticMaxBlocks (512) cooperative
-// blocks; the launch uses one block per 256 threads of co-resident occupancy
-// (at most 2 per SM, 304 on a GB300), and a device that would need more is
-// rejected with AZU_E_UNSUPPORTED. Images may be up to 8192 x 8192.
+// blocks; the launch uses one block of kIcpThreads threads per unit of
+// co-resident occupancy (at most 2 per SM, 152 on a GB300), and a device that
+// would need more is rejected with AZU_E_UNSUPPORTED. Images may be up to
+// 8192 x 8192.
 //
 // The first call on a device resolves the array's device address with that
 // device current; make that first call before any stream capture. Every call
