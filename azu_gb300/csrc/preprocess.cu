@@ -199,22 +199,43 @@ __global__ void __launch_bounds__(256) hole_fill_kernel(const uint16_t* __restri
 }
 
 // guidedDepthFilter (:637-715) with computeDepthGradient (:120-141).
-__global__ void __launch_bounds__(256) guided_kernel(const uint16_t* __restrict__ in, uint16_t* __restrict__ out,
-                                                     const float* __restrict__ luma, const float* __restrict__ dw_tab,
-                                                     float lo, float hi) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+// The block's 32 x 8 pixels and their 4-pixel apron (reflected at the image
+// border like every neighbour index) are staged once in shared memory as raw
+// code, metres and luma, so each of the 81 taps reads them there instead of
+// recomputing the code -> metres division per tap; the taps and their order
+// are unchanged.
+constexpr int kGTx = 32, kGTy = 8, kGR = 4, kGW = kGTx + 2 * kGR, kGH = kGTy + 2 * kGR;
+__global__ void __launch_bounds__(kGTx * kGTy) guided_kernel(const uint16_t* __restrict__ in,
+                                                           uint16_t* __restrict__ out,
+                                                           const float* __restrict__ luma,
+                                                           const float* __restrict__ dw_tab, float lo, float hi) {
+    __shared__ uint16_t s_raw[kGH][kGW];
+    __shared__ float s_m[kGH][kGW];
+    __shared__ float s_l[kGH][kGW];
+    const int x0 = blockIdx.x * kGTx, y0 = blockIdx.y * kGTy;
+    for (int i = threadIdx.y * kGTx + threadIdx.x; i < kGW * kGH; i += kGTx * kGTy) {
+        const int ty = i / kGW, tx = i - ty * kGW;
+        const int gi = reflect(y0 - kGR + ty, PH) * PW + reflect(x0 - kGR + tx, PW);
+        const uint16_t r = in[gi];
+        s_raw[ty][tx] = r;
+        s_m[ty][tx] = depth_m(r, lo, hi);
+        s_l[ty][tx] = __ldg(luma + gi);
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
     if (x >= PW || y >= PH) return;
     const int idx = y * PW + x;
-    const uint16_t rc = in[idx];
-    const float cd = depth_m(rc, lo, hi);
+    const int cx = threadIdx.x + kGR, cy = threadIdx.y + kGR;
+    const uint16_t rc = s_raw[cy][cx];
+    const float cd = s_m[cy][cx];
     if (cd == 0.0f) {
         out[idx] = rc;
         return;
     }
-    const float cl = __ldg(luma + idx);
+    const float cl = s_l[cy][cx];
     float edge = 1.0f;
     if (x > 0 && x < PW - 1 && y > 0 && y < PH - 1) {
-        const uint16_t r = in[idx + 1], l = in[idx - 1], d = in[idx + PW], u = in[idx - PW];
+        const uint16_t r = s_raw[cy][cx + 1], l = s_raw[cy][cx - 1], d = s_raw[cy + 1][cx], u = s_raw[cy - 1][cx];
         if (usable_raw(rc, lo, hi) && usable_raw(r, lo, hi) && usable_raw(l, lo, hi) && usable_raw(d, lo, hi) &&
             usable_raw(u, lo, hi)) {
             const float gx = fabsf(fs(static_cast<float>(r), static_cast<float>(l)));
@@ -229,13 +250,11 @@ __global__ void __launch_bounds__(256) guided_kernel(const uint16_t* __restrict_
     const float* dwrow = dw_tab + static_cast<size_t>(rc) * kRawCodes;
     float sw = 0.0f, sd = 0.0f;
     for (int dy = -4; dy <= 4; ++dy) {
-        const int sy = reflect(y + dy, PH);
         for (int dx = -4; dx <= 4; ++dx) {
-            const int ni = sy * PW + reflect(x + dx, PW);
-            const uint16_t rn = in[ni];
-            const float nd = depth_m(rn, lo, hi);
+            const float nd = s_m[cy + dy][cx + dx];
             if (nd == 0.0f) continue;
-            const float gdl = fs(__ldg(luma + ni), cl);
+            const uint16_t rn = s_raw[cy + dy][cx + dx];
+            const float gdl = fs(s_l[cy + dy][cx + dx], cl);
             const float lw = (gdl == 0.0f) ? 1.0f : expf(fd(-fm(gdl, gdl), ldenom));
             const float w = fm(fm(fm(c_tab.guided_spatial[dx * dx + dy * dy], lw), __ldg(dwrow + rn)), ef);
             sw = fa(sw, w);
@@ -352,7 +371,8 @@ int preprocess_enqueue(azu_preprocessor* p, float lo, float hi, cudaStream_t s) 
     depth_median_kernel<<<g, b, 0, s>>>(p->d_in, p->d_a, lo, hi);
     if (full) {
         hole_fill_kernel<<<g, b, 0, s>>>(p->d_a, p->d_b, lo, hi);
-        guided_kernel<<<g, b, 0, s>>>(p->d_b, p->d_a, p->d_luma, p->d_dw, lo, hi);
+        guided_kernel<<<dim3(PW / kGTx, PH / kGTy), dim3(kGTx, kGTy), 0, s>>>(p->d_b, p->d_a, p->d_luma, p->d_dw,
+                                                                           lo, hi);
     }
     ema_kernel<<<g, b, 0, s>>>(p->d_a, p->d_out, p->d_ema, p->d_depth_m, lo, hi, full ? 1 : 0);
     AZU_LAUNCH_CHECK();
