@@ -102,7 +102,13 @@ __global__ void __launch_bounds__(256) rgb_median_kernel(const uint8_t* __restri
 
 // applyCAS_CPU at sharpness 0.5 + rgbLuma / 255 (SuperResolution.cpp:118-166,
 // SignalConditioner_omp.cpp:381-385).
+// The byte / 255 quotients come from a per-block table of the 256 values
+// (the same division, once per byte value instead of 15 times per pixel).
 __global__ void __launch_bounds__(256) cas_luma_kernel(const uint8_t* __restrict__ src, float* __restrict__ luma) {
+    __shared__ float s_unit[256];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid < 256) s_unit[tid] = fd(static_cast<float>(tid), 255.0f);
+    __syncthreads();
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= PW || y >= PH) return;
     const float t = 0.5f;
@@ -111,9 +117,9 @@ __global__ void __launch_bounds__(256) cas_luma_kernel(const uint8_t* __restrict
         xx = reflect(xx, PW);
         yy = reflect(yy, PH);
         const int i = (yy * PW + xx) * 3;
-        out[0] = fd(static_cast<float>(src[i]), 255.0f);
-        out[1] = fd(static_cast<float>(src[i + 1]), 255.0f);
-        out[2] = fd(static_cast<float>(src[i + 2]), 255.0f);
+        out[0] = s_unit[src[i]];
+        out[1] = s_unit[src[i + 1]];
+        out[2] = s_unit[src[i + 2]];
     };
     float a[3], b[3], c[3], d[3], e[3];
     px(x, y - 1, a); px(x - 1, y, b); px(x, y, c); px(x + 1, y, d); px(x, y + 1, e);
@@ -139,22 +145,30 @@ __global__ void __launch_bounds__(256) cas_luma_kernel(const uint8_t* __restrict
                           255.0f);
 }
 
-// denoiseDepthSpatial (:442-482).
-__global__ void __launch_bounds__(256) depth_median_kernel(const uint16_t* __restrict__ in, uint16_t* __restrict__ out,
-                                                           float lo, float hi) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+// denoiseDepthSpatial (:442-482). The block's pixels and a 1-pixel apron
+// (reflected at the border) are converted to metres once, in shared memory.
+constexpr int kMTx = 32, kMTy = 8, kMW = kMTx + 2, kMH = kMTy + 2;
+__global__ void __launch_bounds__(kMTx * kMTy) depth_median_kernel(const uint16_t* __restrict__ in,
+                                                                  uint16_t* __restrict__ out, float lo, float hi) {
+    __shared__ float s_m[kMH][kMW];
+    const int x0 = blockIdx.x * kMTx, y0 = blockIdx.y * kMTy;
+    for (int i = threadIdx.y * kMTx + threadIdx.x; i < kMW * kMH; i += kMTx * kMTy) {
+        const int ty = i / kMW, tx = i - ty * kMW;
+        s_m[ty][tx] = depth_m(in[reflect(y0 - 1 + ty, PH) * PW + reflect(x0 - 1 + tx, PW)], lo, hi);
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
     if (x >= PW || y >= PH) return;
     const int idx = y * PW + x;
-    const uint16_t r0 = in[idx];
-    uint16_t res = r0;
-    if (depth_m(r0, lo, hi) != 0.0f) {
+    const int cx = threadIdx.x + 1, cy = threadIdx.y + 1;
+    uint16_t res = in[idx];
+    if (s_m[cy][cx] != 0.0f) {
         float w[9];
         int n = 0;
         for (int dy = -1; dy <= 1; ++dy) {
-            const int sy = reflect(y + dy, PH);
             for (int dx = -1; dx <= 1; ++dx) {
-                const float s = depth_m(in[sy * PW + reflect(x + dx, PW)], lo, hi);
-                if (s != 0.0f) w[n++] = s;
+                const float v = s_m[cy + dy][cx + dx];
+                if (v != 0.0f) w[n++] = v;
             }
         }
         if (n >= 3) {
@@ -368,7 +382,7 @@ int preprocess_enqueue(azu_preprocessor* p, float lo, float hi, cudaStream_t s) 
     rgb_bilateral_kernel<<<g, b, 0, s>>>(p->d_rgb_in, p->d_rgb_tmp, p->d_range_w);
     rgb_median_kernel<<<g, b, 0, s>>>(p->d_rgb_tmp, p->d_rgb_out);
     cas_luma_kernel<<<g, b, 0, s>>>(p->d_rgb_out, p->d_luma);
-    depth_median_kernel<<<g, b, 0, s>>>(p->d_in, p->d_a, lo, hi);
+    depth_median_kernel<<<dim3(PW / kMTx, PH / kMTy), dim3(kMTx, kMTy), 0, s>>>(p->d_in, p->d_a, lo, hi);
     if (full) {
         hole_fill_kernel<<<g, b, 0, s>>>(p->d_a, p->d_b, lo, hi);
         guided_kernel<<<dim3(PW / kGTx, PH / kGTy), dim3(kGTx, kGTy), 0, s>>>(p->d_b, p->d_a, p->d_luma, p->d_dw,
