@@ -538,28 +538,40 @@ __device__ __forceinline__ int brick_state(const VolView& v, const uint8_t* __re
 // pass reads the flags) and kDistCap outside the grid. Three passes (x, y, z)
 // give the distance to the nearest non-free brick, capped.
 constexpr int kDistCap = 12;
-__device__ __forceinline__ void brick_dist_body(size_t blk, const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
-                                                int nb, int axis, int from_flags, const int* __restrict__ gate) {
-    if (gate && __ldg(gate) == 0) return;
-    const size_t n = static_cast<size_t>(nb) * nb * nb;
-    const size_t b = blk * blockDim.x + threadIdx.x;
-    if (b >= n) return;
-    const int c[3] = {static_cast<int>(b % nb), static_cast<int>((b / nb) % nb), static_cast<int>(b / nb / nb)};
-    const size_t stride = axis == 0 ? 1 : (axis == 1 ? static_cast<size_t>(nb) : static_cast<size_t>(nb) * nb);
-    const int pos = c[axis];
+__device__ __forceinline__ void brick_dist_at(int x, int y, int z, const uint8_t* __restrict__ in,
+                                              uint8_t* __restrict__ out, int nb, int axis, int from_flags) {
+    const int b = (z * nb + y) * nb + x;  // nb <= 256: 32-bit
+    const int stride = axis == 0 ? 1 : (axis == 1 ? nb : nb * nb);
+    const int pos = axis == 0 ? x : (axis == 1 ? y : z);
     int d = kDistCap;
+#pragma unroll
     for (int k = -kDistCap + 1; k < kDistCap; ++k) {
         const int q = pos + k;
         if (q < 0 || q >= nb) continue;
-        const uint8_t raw = __ldg(in + b + static_cast<ptrdiff_t>(k) * static_cast<ptrdiff_t>(stride));
+        const uint8_t raw = __ldg(in + b + k * stride);
         const int val = from_flags ? (raw ? kDistCap : 0) : raw;
         d = min(d, max(abs(k), val));
     }
     out[b] = static_cast<uint8_t>(d);
 }
-__global__ void brick_dist_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, int nb, int axis,
-                                  int from_flags, const int* __restrict__ gate) {
-    brick_dist_body(blockIdx.x, in, out, nb, axis, from_flags, gate);
+__device__ __forceinline__ void brick_dist_body(size_t blk, const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
+                                                int nb, int axis, int from_flags, const int* __restrict__ gate) {
+    if (gate && __ldg(gate) == 0) return;
+    const unsigned n = static_cast<unsigned>(nb) * nb * nb;
+    const unsigned b = static_cast<unsigned>(blk) * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const unsigned row = b / static_cast<unsigned>(nb);
+    brick_dist_at(static_cast<int>(b - row * nb), static_cast<int>(row % nb), static_cast<int>(row / nb), in, out, nb,
+                  axis, from_flags);
+}
+// Grid (ceil(nb / 64), nb, nb) of 64 threads: brick (x, y, z) without divisions.
+__global__ void __launch_bounds__(64) brick_dist_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
+                                                        int nb, int axis, int from_flags,
+                                                        const int* __restrict__ gate) {
+    if (gate && __ldg(gate) == 0) return;
+    const int x = blockIdx.x * 64 + threadIdx.x;
+    if (x >= nb) return;
+    brick_dist_at(x, blockIdx.y, blockIdx.z, in, out, nb, axis, from_flags);
 }
 
 // Fast-forward through free space. From a sample t whose brick b has free
@@ -1247,11 +1259,10 @@ int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, f
     const dim3 blk(16, 8), grd((W + 15) / 16, (H + 7) / 8);
     const uint8_t* bricks = nullptr;
     if (v->skip_free) {
-        const size_t nbr = static_cast<size_t>(v->nb) * v->nb * v->nb;
-        const unsigned g = static_cast<unsigned>((nbr + 255) / 256);
-        brick_dist_kernel<<<g, 256, 0, s>>>(v->bricks, v->brick_dist, v->nb, 0, 1, d_gate);
-        brick_dist_kernel<<<g, 256, 0, s>>>(v->brick_dist, v->brick_tmp, v->nb, 1, 0, d_gate);
-        brick_dist_kernel<<<g, 256, 0, s>>>(v->brick_tmp, v->brick_dist, v->nb, 2, 0, d_gate);
+        const dim3 g((v->nb + 63) / 64, v->nb, v->nb);
+        brick_dist_kernel<<<g, 64, 0, s>>>(v->bricks, v->brick_dist, v->nb, 0, 1, d_gate);
+        brick_dist_kernel<<<g, 64, 0, s>>>(v->brick_dist, v->brick_tmp, v->nb, 1, 0, d_gate);
+        brick_dist_kernel<<<g, 64, 0, s>>>(v->brick_tmp, v->brick_dist, v->nb, 2, 0, d_gate);
         AZU_LAUNCH_CHECK();
         bricks = v->brick_dist;
     }
@@ -1602,11 +1613,10 @@ extern "C" int azu_volume_raycast_many(azu_volume* v, const float* poses, int co
     const VolView view = make_view(v);
     const uint8_t* bricks = nullptr;
     if (!e && v->skip_free) {
-        const size_t nbr = static_cast<size_t>(v->nb) * v->nb * v->nb;
-        const unsigned g = static_cast<unsigned>((nbr + 255) / 256);
-        brick_dist_kernel<<<g, 256, 0, s>>>(v->bricks, v->brick_dist, v->nb, 0, 1, nullptr);
-        brick_dist_kernel<<<g, 256, 0, s>>>(v->brick_dist, v->brick_tmp, v->nb, 1, 0, nullptr);
-        brick_dist_kernel<<<g, 256, 0, s>>>(v->brick_tmp, v->brick_dist, v->nb, 2, 0, nullptr);
+        const dim3 g((v->nb + 63) / 64, v->nb, v->nb);
+        brick_dist_kernel<<<g, 64, 0, s>>>(v->bricks, v->brick_dist, v->nb, 0, 1, nullptr);
+        brick_dist_kernel<<<g, 64, 0, s>>>(v->brick_dist, v->brick_tmp, v->nb, 1, 0, nullptr);
+        brick_dist_kernel<<<g, 64, 0, s>>>(v->brick_tmp, v->brick_dist, v->nb, 2, 0, nullptr);
         e = cudaGetLastError();
         bricks = v->brick_dist;
     }
