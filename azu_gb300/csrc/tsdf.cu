@@ -957,7 +957,7 @@ __global__ void brick_dist_batch_kernel(const RaycastArgs* __restrict__ A, const
     brick_dist_body(blockIdx.x - __ldg(off + s), in, out, a.nb, pass, pass == 0 ? 1 : 0, a.gate);
 }
 
-__global__ void __launch_bounds__(256) raycast_batch_kernel(const RaycastArgs* __restrict__ A,
+__global__ void __launch_bounds__(256, 5) raycast_batch_kernel(const RaycastArgs* __restrict__ A,
                                                             const int* __restrict__ off, int n) {
     const int s = batch_find(off, n, blockIdx.x);
     const RaycastArgs& a = A[s];
@@ -1125,7 +1125,7 @@ int volume_batch_raycast(azu_volume_batch* b, cudaStream_t s) {
 // Many model images at once (the relocaliser's candidate renders): one launch,
 // blockIdx.z = pose; every image is the single raycast's bit for bit.
 template <bool kHalf>
-__global__ void __launch_bounds__(256) raycast_many_kernel(VolView v, const float* __restrict__ d_poses, float fx,
+__global__ void __launch_bounds__(256, 5) raycast_many_kernel(VolView v, const float* __restrict__ d_poses, float fx,
                                                           float fy, float cx, float cy, int W, int H, float trunc,
                                                           float min_depth, float max_depth, float* __restrict__ vout,
                                                           float* __restrict__ nout,
