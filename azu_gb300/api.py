@@ -446,6 +446,10 @@ class Pipeline:
         return dict(pose=np.array(r.pose, np.float32).reshape(4, 4), icp=result_dict(r.icp), quality=r.quality,
                     integrated=bool(r.integrated), frame_index=r.frame_index)
 
+    def reset(self):
+        """Empty volume, first-frame state (PipelineController's reset)."""
+        check(self.lib.azu_pipeline_reset(self.h), "azu_pipeline_reset")
+
     def process_frame(self, depth: np.ndarray, rgb: np.ndarray | None = None) -> dict:
         """One frame from host buffers (H2D, whole frame on the device, D2H)."""
         r = _abi.FrameResult()

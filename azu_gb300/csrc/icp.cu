@@ -119,6 +119,8 @@ __device__ void grid_sync(unsigned* bar, unsigned* err, unsigned nblocks, unsign
 // one solve per iteration instead of one per block). Waits are bounded like
 // grid_sync; with the error word set nobody waits and every block proceeds
 // on its own (the result is then reported as a timeout).
+// The last block resets the arrival count at once: no block arrives again
+// before release_all, which it reaches after this reset.
 __device__ bool arrive_last(unsigned* bar, unsigned* err, unsigned nblocks, int* s_flag) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -126,6 +128,7 @@ __device__ bool arrive_last(unsigned* bar, unsigned* err, unsigned nblocks, int*
         if (ld_acquire(err) == 0) {
             __threadfence();
             last = (atomicAdd(&bar[0], 1u) == nblocks - 1) ? 1 : 0;
+            if (last) atomicExch(&bar[0], 0u);
             __threadfence();
         }
         *s_flag = last;
@@ -134,14 +137,11 @@ __device__ bool arrive_last(unsigned* bar, unsigned* err, unsigned nblocks, int*
     return *s_flag != 0;
 }
 
+// Callers fence their published writes before it.
 __device__ void release_all(unsigned* bar, unsigned* err, unsigned& gen) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        if (ld_acquire(err) == 0) {
-            atomicExch(&bar[0], 0u);
-            __threadfence();
-            atomicAdd(&bar[1], 1u);
-        }
+        if (ld_acquire(err) == 0) atomicAdd(&bar[1], 1u);
         gen += 1;
     }
     __syncthreads();

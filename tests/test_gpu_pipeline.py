@@ -97,3 +97,27 @@ def test_overlapped_schedule_equals_sequential(cuda_lib, seq, input_is_mm):
         assert np.array_equal(w, vols[0][1])
     for p in (seqp, fast, queued):
         p.close()
+
+
+def test_reset_replays_the_sequence(cuda_lib, seq):
+    """After a reset in the middle of a run (frames still in flight on both
+    streams), the pipeline gives exactly what a fresh one gives."""
+    from azu_gb300 import api
+    fresh = _pipeline(seq, True)
+    ref = [fresh.process_frame(seq.depth_mm[k]) for k in range(6)]
+    pl = _pipeline(seq, True)
+    for k in range(3):
+        pl.process_frame(seq.depth_mm[9 - k])
+    pl.reset()
+    got = [pl.process_frame(seq.depth_mm[k]) for k in range(6)]
+    for a, b in zip(ref, got):
+        assert np.array_equal(a["pose"].view(np.uint32), b["pose"].view(np.uint32))
+        assert (a["quality"], a["frame_index"]) == (b["quality"], b["frame_index"])
+    vp = api.volume_params(seq.volume["resolution"], seq.volume["voxel_size"], seq.volume["truncation"],
+                           seq.volume["max_weight"], seq.volume["origin"], seq.min_depth, seq.max_depth,
+                           seq.volume["format"])
+    ta, wa = api.TSDFVolume.borrowed(fresh.volume_handle(), vp).download()
+    tb, wb = api.TSDFVolume.borrowed(pl.volume_handle(), vp).download()
+    assert np.array_equal(ta.view(np.uint32), tb.view(np.uint32)) and np.array_equal(wa, wb)
+    fresh.close()
+    pl.close()
