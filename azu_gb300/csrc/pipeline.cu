@@ -107,6 +107,7 @@ struct azu_pipeline {
     cudaGraphExec_t exec = nullptr;
     // two-stream schedule (standalone pipelines)
     cudaStream_t s2 = nullptr;                    // inputs, preprocessing, frame maps
+    cudaStream_t s3 = nullptr;                    // result read-back beside the fusion
     cudaEvent_t ev_front = nullptr, ev_track = nullptr, ev_result = nullptr;
     float* d_depth2[2] = {nullptr, nullptr};      // the frame's depth (metres), alternating
     float* d_tiles2[2] = {nullptr, nullptr};      // its depth tile pyramid
@@ -281,9 +282,16 @@ static int run_frame(azu_pipeline* pl, bool stage_result = false) {
         if (rc) return rc;
         AZU_TRY_CUDA(cudaEventRecord(pl->ev_track, s));
         if (stage_result) {
-            AZU_TRY_CUDA(cudaMemcpyAsync(pl->h_st, pl->d_st, sizeof(PoseState), cudaMemcpyDeviceToHost, s));
-            AZU_TRY_CUDA(cudaMemcpyAsync(pl->h_icp, pl->d_icp, sizeof(azu_icp_result), cudaMemcpyDeviceToHost, s));
-            AZU_TRY_CUDA(cudaEventRecord(pl->ev_result, s));
+            // on a third stream, so the fusion does not wait for the copies; only
+            // what the tracking wrote and the fusion does not touch is read
+            cudaStream_t s3 = pl->s3;
+            AZU_TRY_CUDA(cudaStreamWaitEvent(s3, pl->ev_track, 0));
+            AZU_TRY_CUDA(cudaMemcpyAsync(pl->h_st->cur, pl->d_st->cur, sizeof(pl->h_st->cur), cudaMemcpyDeviceToHost,
+                                         s3));
+            AZU_TRY_CUDA(cudaMemcpyAsync(&pl->h_st->quality, &pl->d_st->quality, 2 * sizeof(int),
+                                         cudaMemcpyDeviceToHost, s3));  // quality, gate
+            AZU_TRY_CUDA(cudaMemcpyAsync(pl->h_icp, pl->d_icp, sizeof(azu_icp_result), cudaMemcpyDeviceToHost, s3));
+            AZU_TRY_CUDA(cudaEventRecord(pl->ev_result, s3));
         }
         rc = first ? enqueue_tail(pl, s)
                    : run_part(pl, pl->g_part[3 + b], pl->x_part[3 + b], s, [&] { return enqueue_tail(pl, s); });
@@ -326,7 +334,7 @@ static int read_staged_result(azu_pipeline* pl, azu_frame_result* out) {
     out->icp = *pl->h_icp;
     out->quality = st.quality;
     out->integrated = st.gate;
-    out->frame_index = st.frame_index;
+    out->frame_index = pl->frames - 1;  // run_frame has counted this frame
     if (st.quality == -1) std::memset(&out->icp, 0, sizeof(out->icp));
     if (out->icp.status == AZU_E_TIMEOUT) {
         set_error("ICP grid barrier timed out");
@@ -394,6 +402,7 @@ extern "C" int azu_pipeline_destroy(azu_pipeline* pl) {
     if (!pl) return AZU_OK;
     cudaSetDevice(pl->device);
     if (pl->s2) cudaStreamSynchronize(pl->s2);
+    if (pl->s3) cudaStreamSynchronize(pl->s3);
     if (pl->s) cudaStreamSynchronize(pl->s);
     drop_graphs(pl);
     azu_preprocessor_destroy(pl->pre);
@@ -408,6 +417,7 @@ extern "C" int azu_pipeline_destroy(azu_pipeline* pl) {
     for (cudaEvent_t e : pl->ev) if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : {pl->ev_front, pl->ev_track, pl->ev_result}) if (e) cudaEventDestroy(e);
     if (pl->s2) cudaStreamDestroy(pl->s2);
+    if (pl->s3) cudaStreamDestroy(pl->s3);
     if (pl->s && pl->own_stream) cudaStreamDestroy(pl->s);
     delete pl;
     return AZU_OK;
@@ -453,6 +463,7 @@ int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t st
         if (!e && pl->own_stream) {
             // the second stream of the two-stream schedule
             e = cudaStreamCreateWithFlags(&pl->s2, cudaStreamNonBlocking);
+            if (!e) e = cudaStreamCreateWithFlags(&pl->s3, cudaStreamNonBlocking);
             for (cudaEvent_t* ev : {&pl->ev_front, &pl->ev_track, &pl->ev_result})
                 if (!e) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
             for (int k = 0; !e && k < 2; ++k) e = cudaMalloc(&pl->d_depth2[k], n * 4);
@@ -477,6 +488,7 @@ extern "C" int azu_pipeline_reset(azu_pipeline* pl) {
     AZU_CHECK_ARG(pl != nullptr, "null handle");
     AZU_TRY_CUDA(cudaSetDevice(pl->device));
     if (pl->s2) AZU_TRY_CUDA(cudaStreamSynchronize(pl->s2));
+    if (pl->s3) AZU_TRY_CUDA(cudaStreamSynchronize(pl->s3));
     AZU_TRY_CUDA(cudaStreamSynchronize(pl->s));
     if (int rc = azu_volume_reset(pl->vol)) return rc;
     if (pl->pre) if (int rc = azu_preprocessor_reset(pl->pre)) return rc;
@@ -542,6 +554,7 @@ extern "C" int azu_pipeline_set_profiling(azu_pipeline* pl, int on) {
     if ((on != 0) != pl->profiling) {
         // Event records are part of the captured graphs: recapture.
         if (pl->s2) AZU_TRY_CUDA(cudaStreamSynchronize(pl->s2));
+        if (pl->s3) AZU_TRY_CUDA(cudaStreamSynchronize(pl->s3));
         AZU_TRY_CUDA(cudaStreamSynchronize(pl->s));
         drop_graphs(pl);
     }
