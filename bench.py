@@ -49,6 +49,18 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(vals, ws: int, device: str):
+    """Element-wise max of per-rank times over the process group (the job ends
+    when its slowest replica does); the identity for a single rank."""
+    if ws <= 1:
+        return [float(v) for v in vals]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in vals], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 50 ms (nvidia-smi's
     own loop, in a child process) during a timed region."""
@@ -522,11 +534,7 @@ def run_gpu(args):
     # max over ranks
     t_run = ms / 1000.0
     t_e2e = e2e_ms / 1000.0
-    if ws > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_run, t_e2e], device=f"cuda:{dev}", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_run, t_e2e = tt.tolist()
+    t_run, t_e2e = max_over_ranks([t_run, t_e2e], ws, f"cuda:{dev}")
     if rank != 0:
         _release(torch, dev, mc, pl)
         if ws > 1:
