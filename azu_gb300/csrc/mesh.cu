@@ -234,8 +234,16 @@ __device__ int cube_valid_edges(const MeshVol& v, int x, int y, int z, int& cube
     return ok;
 }
 
-__device__ __forceinline__ int count_tris(int cube_idx, int ok) {
-    const uint64_t row = c_tri_rows[cube_idx];
+// Threads of a warp index the triangle table by their own cube, so the
+// kernels that read it stage it in shared memory (constant memory serialises
+// divergent indices).
+__device__ __forceinline__ void stage_tri_rows(uint64_t* s_rows) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_rows[i] = c_tri_rows[i];
+    __syncthreads();
+}
+
+__device__ __forceinline__ int count_tris(const uint64_t* rows, int cube_idx, int ok) {
+    const uint64_t row = rows[cube_idx];
     int n = 0;
     for (int t = 0; ((row >> (4 * t)) & 0xF) != 0xF; t += 3) {
         const int a = (row >> (4 * t)) & 0xF, b = (row >> (4 * (t + 1))) & 0xF, c = (row >> (4 * (t + 2))) & 0xF;
@@ -389,6 +397,8 @@ __global__ void __launch_bounds__(256) mc_validate_kernel(MeshVol v, const unsig
                                                           const unsigned* __restrict__ n_active, unsigned cap,
                                                           uint32_t* __restrict__ meta, uint8_t* __restrict__ counts,
                                                           unsigned* __restrict__ block_sums) {
+    __shared__ uint64_t s_rows[256];
+    stage_tri_rows(s_rows);
     const unsigned n = min(*n_active, cap);
     const unsigned cr = static_cast<unsigned>(v.res - 1);
     for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -396,7 +406,7 @@ __global__ void __launch_bounds__(256) mc_validate_kernel(MeshVol v, const unsig
         int x, y, z, ci;
         cube_of(i, cr, x, y, z);
         const int ok = cube_valid_edges(v, x, y, z, ci);
-        const int nt = ok ? count_tris(ci, ok) : 0;
+        const int nt = ok ? count_tris(s_rows, ci, ok) : 0;
         meta[k] = static_cast<uint32_t>(ok) | (static_cast<uint32_t>(ci) << 12) | (static_cast<uint32_t>(nt) << 20);
         if (nt) {
             counts[i] = static_cast<uint8_t>(nt);
@@ -417,6 +427,8 @@ __global__ void __launch_bounds__(256) mc_emit_kernel(MeshVol v, const unsigned 
                                                       const uint8_t* __restrict__ counts,
                                                       const unsigned* __restrict__ block_offsets, unsigned cap,
                                                       uint64_t* __restrict__ slot_key) {
+    __shared__ uint64_t s_rows[256];
+    stage_tri_rows(s_rows);
     const unsigned cr = static_cast<unsigned>(v.res - 1);
     const uint64_t R = static_cast<uint64_t>(v.res);
     for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -446,7 +458,7 @@ __global__ void __launch_bounds__(256) mc_emit_kernel(MeshVol v, const unsigned 
         int x, y, z;
         cube_of(i, cr, x, y, z);
         const int ok = static_cast<int>(m & 0xFFF), ci = static_cast<int>((m >> 12) & 0xFF);
-        const uint64_t row = c_tri_rows[ci];
+        const uint64_t row = s_rows[ci];
         unsigned tri = first;
         for (int t = 0; ((row >> (4 * t)) & 0xF) != 0xF && tri < cap; t += 3) {
             const int e0 = int((row >> (4 * t)) & 0xF), e1 = int((row >> (4 * (t + 1))) & 0xF),

@@ -38,7 +38,7 @@ METRIC = "frames/s @512³ TSDF, 640×480 (FP32 vs FP16-TSDF form, CPU ref); inte
 SEQ_FRAMES = 300
 MESH_EVERY = 30
 W, H = 640, 480
-KERNELS_PER_FRAME_RAW = 19  # 7 preprocess + 2 frame + predict + ICP + 3 integrate + 3 brick distance + raycast + commit
+KERNELS_PER_FRAME_RAW = 19  # 7 preprocess + 2 frame maps + 2 depth tiles + ICP + 2 integrate + 3 brick distance + raycast + commit
 D2H_RESULT_BYTES = 336 + 264  # device pose state + azu_icp_result read back per frame
 
 
@@ -523,8 +523,11 @@ def run_gpu(args):
     # then completes before the call returns)
     pl.set_profiling(True)
     statsp0 = pl.volume_stats()
+    icp_pix_iters = []
     for k in range(min(Ke, 30)):
-        pl.process_frame(h_raw_np[frame % SEQ_FRAMES], h_rgb_np)
+        r = pl.process_frame(h_raw_np[frame % SEQ_FRAMES], h_rgb_np)
+        # association passes of the solve: (W_l - 2)(H_l - 2) pixels per iteration at level l
+        icp_pix_iters.append(sum(it * ((W >> l) - 2) * ((H >> l) - 2) for l, it in enumerate(r["icp"]["iterations"])))
         frame += 1
     stage_ms, prof_frames = pl.stage_times()
     statsp1 = pl.volume_stats()
@@ -571,6 +574,13 @@ def run_gpu(args):
                      "algorithmic_bytes_per_launch": bytes_per_frame, "launch_ms": int_ms,
                      "updated_voxels_per_frame": upd / max(prof_frames, 1)},
         "stage_ms_per_frame": {k: v2 / max(prof_frames, 1) for k, v2 in stage_ms.items()},
+        "icp": {"pixel_iterations_per_frame": float(np.mean(icp_pix_iters)),
+                "bytes_per_frame": 48.0 * float(np.mean(icp_pix_iters)),
+                "achieved_gbs": 48.0 * float(np.mean(icp_pix_iters)) / (stage_ms["track"] / max(prof_frames, 1) * 1e-3)
+                / 1e9 if stage_ms["track"] > 0 else None,
+                "peak_gbs": peak,
+                "note": "48 B per pixel-iteration (live vertex and normal, model vertex and normal), L2-resident; "
+                        "the bound is the serial reduction + solve per iteration, not bandwidth"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "wall_frames_per_s": K / wall,
