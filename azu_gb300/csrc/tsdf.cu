@@ -64,6 +64,7 @@ constexpr int kIntWarps = 4;
 constexpr int kTileShift = 3;  // level-0 depth tiles are 8x8 pixels
 constexpr int kCullSeg = 16;   // voxels per culling piece of a 32-voxel chunk
 constexpr int kIntParts = 2;   // x-parts per 32-row item of the persistent kernel (shorter items, shorter tail)
+constexpr int kUpdGroup = 4;   // rows per software-pipelined update group (6 and 8 were slower)
 
 // Deepest in-band depth of every 8x8 pixel tile (-inf when the tile has none),
 // level 0 of the tile pyramid. Eight lanes share a tile, one pixel row each.
@@ -392,44 +393,56 @@ __device__ __forceinline__ void integrate_item(
         }
         if (!live_rows) continue;
         __syncwarp();
-        // update (lane = x), live rows in batches of 8 so their loads overlap
+        // update (lane = x): live rows in groups of kUpdGroup, software
+        // pipelined: the projection and depth gather of the next group are
+        // issued before the voxel read-modify-write of this one, so the two
+        // dependent load latencies overlap.
         const int x = xc + lane;
         const bool x_on = x >= x0 && x <= x1;
         unsigned rem = live_rows;
-#pragma unroll 1
-        while (rem) {
-            int rsel[8];
+        int ra[kUpdGroup], pa[kUpdGroup];
+        float za[kUpdGroup], da[kUpdGroup];
+        auto gather = [&]() {  // next group: rows, pixels (-1: none), camera z, depth
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                rsel[j] = rem ? __ffs(rem) - 1 : -1;
+            for (int j = 0; j < kUpdGroup; ++j) {
+                ra[j] = rem ? __ffs(rem) - 1 : -1;
                 rem &= rem - 1;
             }
-            int pix[8];
-            float cz[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                pix[j] = -1;
-                cz[j] = 0.0f;
-                if (rsel[j] >= 0 && x_on) {
-                    const F3 cv = mk3(s_c[warp][0][rsel[j]][lane], s_c[warp][1][rsel[j]][lane],
-                                      s_c[warp][2][rsel[j]][lane]);
+            for (int j = 0; j < kUpdGroup; ++j) {
+                pa[j] = -1;
+                za[j] = 0.0f;
+                if (ra[j] >= 0 && x_on) {
+                    const F3 cv = mk3(s_c[warp][0][ra[j]][lane], s_c[warp][1][ra[j]][lane], s_c[warp][2][ra[j]][lane]);
                     if (cv.z > 0.0f) {
                         const float inv_z = __frcp_rn(cv.z);  // == 1.0f / c.z, correctly rounded
                         const float uf = floorf(fa(fa(fm(fm(fx, cv.x), inv_z), cx), 0.5f));
                         const float vf = floorf(fa(fa(fm(fm(fy, cv.y), inv_z), cy), 0.5f));
                         if (uf >= 0.0f && uf < fW && vf >= 0.0f && vf < fH) {
-                            const int ui = static_cast<int>(uf), vi = static_cast<int>(vf);
-                            pix[j] = vi * W + ui;
-                            cz[j] = cv.z;
+                            pa[j] = static_cast<int>(vf) * W + static_cast<int>(uf);
+                            za[j] = cv.z;
                         }
                     }
                 }
             }
-            float sdf[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) sdf[j] = pix[j] >= 0 ? __ldg(depth + pix[j]) : 0.0f;
+            for (int j = 0; j < kUpdGroup; ++j) da[j] = pa[j] >= 0 ? __ldg(depth + pa[j]) : 0.0f;
+        };
+        gather();
+#pragma unroll 1
+        while (ra[0] >= 0) {
+            int rsel[kUpdGroup], pix[kUpdGroup];
+            float cz[kUpdGroup], sdf[kUpdGroup];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
+            for (int j = 0; j < kUpdGroup; ++j) {
+                rsel[j] = ra[j];
+                pix[j] = pa[j];
+                cz[j] = za[j];
+                sdf[j] = da[j];
+            }
+            gather();  // the next group's loads are in flight during this group's update
+#pragma unroll
+            for (int j = 0; j < kUpdGroup; ++j) {
                 const float d = sdf[j];
                 bool ok = false;
                 if (pix[j] >= 0 && d >= min_d && d <= max_d) {
@@ -438,14 +451,14 @@ __device__ __forceinline__ void integrate_item(
                 }
                 if (!ok) pix[j] = -1;
             }
-            float2 old[8];
+            float2 old[kUpdGroup];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
+            for (int j = 0; j < kUpdGroup; ++j) {
                 const size_t v = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
                 if (pix[j] >= 0) old[j] = kResid ? VoxR::load_fold(vox, v) : Vox<kHalf>::load_rw(vox, v);
             }
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
+            for (int j = 0; j < kUpdGroup; ++j) {
                 if (pix[j] < 0) continue;
                 const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
                 const float tsdf_new = fminf(1.0f, fd(sdf[j], trunc));
