@@ -444,7 +444,11 @@ int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t st
         pl->s = stream;
         pl->own_stream = false;
     } else {
-        e = cudaStreamCreateWithFlags(&pl->s, cudaStreamNonBlocking);
+        // the frame's critical path (tracking, fusion) gets the highest
+        // priority; the next frame's input stage (second stream) fills the gaps
+        int least = 0, greatest = 0;
+        e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (!e) e = cudaStreamCreateWithPriority(&pl->s, cudaStreamNonBlocking, greatest);
     }
     if (e) { set_error("stream: %s", cudaGetErrorString(e)); rc = AZU_E_CUDA; }
     if (!rc) rc = azu_volume_create(device, &p->volume, pl->s, &pl->vol);
@@ -462,7 +466,9 @@ int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t st
         for (int k = 0; !e && k < 6; ++k) e = cudaEventCreate(&pl->ev[k]);
         if (!e && pl->own_stream) {
             // the second stream of the two-stream schedule
-            e = cudaStreamCreateWithFlags(&pl->s2, cudaStreamNonBlocking);
+            int least = 0, greatest = 0;
+            e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+            if (!e) e = cudaStreamCreateWithPriority(&pl->s2, cudaStreamNonBlocking, least);
             if (!e) e = cudaStreamCreateWithFlags(&pl->s3, cudaStreamNonBlocking);
             for (cudaEvent_t* ev : {&pl->ev_front, &pl->ev_track, &pl->ev_result})
                 if (!e) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
