@@ -14,11 +14,12 @@
 //   integrate  only when the grade is Good (a device flag gates the kernels)
 //   raycast    the new model at cur (same gate)
 // A pipeline made by azu_pipeline_create runs the input and frame stages on a
-// second stream: frame k+1's upload, preprocessing and frame maps overlap
-// frame k's integrate and raycast (they only wait for frame k's tracking, and
-// the depth map alternates between two buffers), and a call that returns the
-// result returns once the pose is known, with the fusion of the frame still
-// running on the pipeline's stream. Each part replays its own captured CUDA
+// second stream: frame k+1's upload, preprocessing, frame maps and depth tiles
+// overlap frame k's integrate and raycast (they only wait for frame k's
+// tracking, and the depth map and its tiles alternate between two buffers),
+// and a call that returns the result returns once the pose is known (read back
+// on a third stream), with the fusion of the frame still running on the
+// pipeline's stream. Each part replays its own captured CUDA
 // graph (frames k > 0); host inputs and the result are copied outside them.
 // Results are those of the strictly sequential schedule: every stage reads
 // what it read there.
@@ -171,7 +172,8 @@ static int enqueue_input(azu_pipeline* pl, cudaStream_t s) {
     return mark(pl, 2, s);
 }
 
-// Prediction and tracking (or the first-frame pose).
+// Tracking (or the first-frame pose); the prediction it starts from was made
+// by the previous frame's commit.
 static int enqueue_track(azu_pipeline* pl, bool first, cudaStream_t s) {
     PoseState* st = pl->d_st;
     if (first) {
