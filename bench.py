@@ -125,6 +125,16 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def committed_hit_rates():
+    """L1 / L2 hit rates of the raycast kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "raycast_c2_512.md")
+    try:
+        m = re.search(r"L1 hit / L2 hit \| ([0-9.]+)% / ([0-9.]+)%", open(path).read())
+        return (float(m.group(1)) / 100.0, float(m.group(2)) / 100.0) if m else (None, None)
+    except OSError:
+        return None, None
+
+
 def committed_traffic():
     """Per-launch DRAM bytes of the integrate kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "integrate_c2_512.md")
@@ -532,6 +542,13 @@ def run_gpu(args):
     stage_ms, prof_frames = pl.stage_times()
     statsp1 = pl.volume_stats()
     pl.set_profiling(False)
+    # one marching-cubes extraction of the final volume, device time
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    mesh_last = mc.extract_counts(vol)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    mesh_ms = e0.elapsed_time(e1)
     n_int = sum(1 for q in qual if q == 0)
 
     # max over ranks
@@ -587,6 +604,19 @@ def run_gpu(args):
         "tracking": {"good_frames_e2e": n_int, "frames_e2e": Ke,
                      "final_pose_err_m": float(np.linalg.norm(pl.last_result()["pose"][:3, 3] - gt[:3, 3]))},
         "meshes": [{"vertices": m["n_vertices"], "triangles": m["n_indices"] // 3} for m in meshes[:3]],
+        "marching_cubes": {"extract_ms": mesh_ms, "mvoxels_per_s": 512 ** 3 / (mesh_ms * 1e-3) / 1e6,
+                           "classify_bytes": 8 * 512 ** 3, "triangles": mesh_last["n_indices"] // 3,
+                           "vertices": mesh_last["n_vertices"], "truncated": bool(mesh_last["truncated"])},
+        "raycast": {"rays_per_s": W * H / (stage_ms["raycast"] / max(prof_frames, 1) * 1e-3)
+                    if stage_ms["raycast"] > 0 else None,
+                    "output_bytes_per_frame": 24 * W * H,
+                    "l1_hit": committed_hit_rates()[0], "l2_hit": committed_hit_rates()[1],
+                    "note": "stage time includes the three brick-distance passes; hit rates from the committed "
+                            "ncu summary"},
+        "preprocess": {"ms": stage_ms["input"] / max(prof_frames, 1),
+                       "gbs": 9.7e6 / (stage_ms["input"] / max(prof_frames, 1) * 1e-3) / 1e9
+                       if stage_ms["input"] > 0 else None,
+                       "bytes_per_frame": 9.7e6, "note": "second stream, beside the previous frame's fusion"},
     }
     if cpu:
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
