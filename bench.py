@@ -403,6 +403,50 @@ def run_batch_form(dev, n_scenes: int, frames_scale: float):
                       "single pipeline's frames"}
 
 
+def run_ingest(pl, raw, rgb, frames: int):
+    """Frames/s of the sensor-ingest path: a fakenect recording (INDEX.txt, PGM
+    depth, PPM RGB, RGB 60 ticks before its depth) written to a temporary
+    directory, read ahead into pinned slots by the ingest thread, one
+    host-to-device copy per frame (azu_pipeline_process_frame_packed)."""
+    import shutil
+    import tempfile
+    from azu_gb300 import api
+    d = tempfile.mkdtemp(prefix="azu_ingest_")
+    try:
+        lines = []
+        for k in range(frames):
+            dn, rn = f"d-{k:.3f}-{k * 33 * 60000 + 60}-0.pgm", f"r-{k:.3f}-{k * 33 * 60000}-0.ppm"
+            with open(os.path.join(d, rn), "wb") as f:
+                f.write(b"P6 640 480 255\n" + rgb.tobytes())
+            with open(os.path.join(d, dn), "wb") as f:
+                f.write(b"P5 640 480 65535\n" + raw[k % len(raw)].astype("<u2").tobytes())
+            lines += [rn, dn]
+        with open(os.path.join(d, "INDEX.txt"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+        rec = api.Recording(d)
+        ing = api.Ingest(rec, slots=4)
+        warm = 3
+        t0 = None
+        n = 0
+        while True:
+            got = ing.next()
+            if got is None:
+                break
+            pl.process_frame_packed(got[0])
+            ing.release()
+            n += 1
+            if n == warm:
+                t0 = time.perf_counter()
+        dt = time.perf_counter() - t0 if t0 is not None else None
+        ing.close()
+        rec.close()
+        return {"frames_per_s": (n - warm) / dt if dt else None, "frames": n - warm, "slots": 4,
+                "source": "fakenect recording in the page cache (written by the bench), read ahead on the ingest "
+                          "thread; host wall clock"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -621,6 +665,8 @@ def run_gpu(args):
     if cpu:
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         line["cpu_stage_s_per_frame"] = cpu["stage_s_per_frame"]
+    if args.ingest_frames > 0:
+        line["ingest"] = run_ingest(pl, raw, rgb, args.ingest_frames)
     _release(torch, dev, mc, pl)
     if args.form_frames > 0:
         line["forms"] = run_forms(seq, raw, rgb, dev, args.form_frames, args.form_err_frames)
@@ -651,6 +697,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-frames", type=int, default=12)
     ap.add_argument("--form-frames", type=int, default=60, help="frames per precision-form run (0: skip)")
+    ap.add_argument("--ingest-frames", type=int, default=60, help="frames through the recording ingest (0: skip)")
     ap.add_argument("--form-err-frames", type=int, default=20, help="frames of the FP64 error sample (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
