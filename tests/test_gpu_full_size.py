@@ -1,0 +1,116 @@
+"""Parity at the size the frame rate is measured on: the c2 workload (512^3 FP32
+volume over a 2 m cube, 640x480 frames of the 360-degree orbit with 40 extra
+spheres), GPU against the oracle.
+
+  integration   values, weights and per-frame counts bit for bit
+  raycast       vertices and normals bit for bit, at an integrated pose and at
+                a pose the volume has not seen
+  mesh          marching cubes of the 512^3 volume bit for bit (positions,
+                normals, welded indices)
+  pipeline      the whole GPU frame (raw codes -> preprocess -> pyramid -> ICP
+                -> integrate -> raycast) against the oracle's lockstep CPU
+                pipeline: same grades and integration decisions, poses within
+                5e-4 rad / 5e-4 m
+"""
+import numpy as np
+import pytest
+
+import fixtures as F
+
+pytestmark = pytest.mark.gpu
+
+FUSED_FRAMES = 4
+
+
+@pytest.fixture(scope="module")
+def c2():
+    from azu_gb300 import synth
+    return synth.sequence("c2", frames=8)
+
+
+@pytest.fixture(scope="module")
+def fused(cuda_lib, orc, c2):
+    """GPU and oracle volumes after the first frames at their true poses."""
+    from azu_gb300 import api, synth
+    s = c2
+    v = s.volume
+    assert v["resolution"] == 512 and (s.width, s.height) == (640, 480)
+    g = api.TSDFVolume(api.volume_params(v["resolution"], v["voxel_size"], v["truncation"], v["max_weight"],
+                                         v["origin"], s.min_depth, s.max_depth))
+    o = orc.Volume(orc.tsdf_params(resolution=v["resolution"], voxel_size=v["voxel_size"],
+                                   truncation=v["truncation"], max_weight=v["max_weight"],
+                                   origin=tuple(v["origin"]), min_depth=s.min_depth, max_depth=s.max_depth))
+    K = (s.fx, s.fy, s.cx, s.cy)
+    counts = []
+    for k in range(FUSED_FRAMES):
+        dm = synth.mm_to_meters(s.depth_mm[k])
+        g.integrate(dm, s.poses[k], K, s.width, s.height, s.min_depth, s.max_depth)
+        st = o.integrate(dm, s.poses[k], orc.intr(*K), s.width, s.height, s.min_depth, s.max_depth)
+        counts.append((g.stats()["last_voxels_updated"], st["voxels_updated"], st["newly_observed"]))
+    return s, g, o, counts
+
+
+def test_c2_integration_bit_exact(fused):
+    s, g, o, counts = fused
+    for k, (gu, ou, _) in enumerate(counts):
+        assert gu == ou, k
+        assert ou > 5_000_000, k  # a full-size frame: millions of voxels per update
+    assert g.stats()["observed_voxels"] == sum(c[2] for c in counts)
+    t, w = g.download()
+    assert t.size == 512 ** 3
+    assert np.array_equal(w, o.weight)
+    assert np.array_equal(t.view(np.uint32), o.tsdf.view(np.uint32))
+
+
+@pytest.mark.parametrize("frame", [FUSED_FRAMES - 1, 7])
+def test_c2_raycast_bit_exact(fused, orc, frame):
+    s, g, o, _ = fused
+    K = (s.fx, s.fy, s.cx, s.cy)
+    rg = g.raycast(s.poses[frame], K, s.width, s.height)
+    ro = o.raycast(s.poses[frame], orc.intr(*K), s.width, s.height)
+    assert (ro["vertices"] != 0).any(-1).sum() > 20000
+    assert np.array_equal(rg["vertices"].view(np.uint32), ro["vertices"].view(np.uint32))
+    assert np.array_equal(rg["normals"].view(np.uint32), ro["normals"].view(np.uint32))
+
+
+def test_c2_mesh_bit_exact(fused):
+    from azu_gb300 import api
+    _, g, o, _ = fused
+    gm = api.MarchingCubes().extract(g)
+    om = o.extract_mesh()
+    assert len(om["indices"]) > 100_000 and not om["truncated"]
+    assert gm["truncated"] == om["truncated"]
+    assert np.array_equal(gm["indices"], om["indices"])
+    assert np.array_equal(gm["positions"].view(np.uint32), om["positions"].view(np.uint32))
+    assert np.array_equal(gm["normals"].view(np.uint32), om["normals"].view(np.uint32))
+
+
+def test_c2_pipeline_matches_lockstep_oracle(cuda_lib, orc, c2):
+    from azu_gb300 import api, synth
+    s = c2
+    v = s.volume
+    vp = api.volume_params(v["resolution"], v["voxel_size"], v["truncation"], v["max_weight"], v["origin"],
+                           s.min_depth, s.max_depth, v["format"])
+    tp = api.tracker_params(min_depth=s.min_depth, max_depth=s.max_depth)
+    pl = api.Pipeline(api.pipeline_params(vp, tp, 0, s.min_depth, s.max_depth, False, True))
+    L = orc.Lockstep(s.volume, input_is_mm=False, fold_threads=0)
+    rgb = synth.grey_rgb()
+    for k in range(len(s.poses)):
+        d = synth.encode_raw(s.depth_mm[k])
+        gr = pl.process_frame(d, rgb)
+        orr = L.process(d, rgb)
+        assert gr["frame_index"] == k
+        assert gr["quality"] == orr["quality"], k
+        assert gr["integrated"] == orr["integrated"], k
+        rot, trans = F.rel_pose_error(gr["pose"], orr["pose"])
+        assert rot <= 5e-4 and trans <= 5e-4, (k, rot, trans)
+        if k:
+            assert gr["icp"]["status"] == 0
+            assert abs(gr["icp"]["inliers"] - orr["icp"]["inliers"]) <= max(5, 1e-2 * orr["icp"]["inliers"])
+            # tracking sanity only (the oracle itself is this far from the
+            # generator's poses on the first frames of the orbit)
+            rot_gt, trans_gt = F.rel_pose_error(gr["pose"], s.poses[k])
+            assert rot_gt < 2e-2 and trans_gt < 2e-2, (k, rot_gt, trans_gt)
+            rot_o, trans_o = F.rel_pose_error(orr["pose"], s.poses[k])
+            assert abs(rot_gt - rot_o) <= 5e-4 and abs(trans_gt - trans_o) <= 5e-4
+    pl.close()
