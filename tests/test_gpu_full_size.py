@@ -11,6 +11,8 @@ spheres), GPU against the oracle.
                 -> integrate -> raycast) against the oracle's lockstep CPU
                 pipeline: same grades and integration decisions, poses within
                 5e-4 rad / 5e-4 m
+  precision     the FP16R form at its own size (c3: 1024^3 over a 4 m cube)
+                against the oracle's storage emulation bit for bit
 """
 import numpy as np
 import pytest
@@ -114,3 +116,45 @@ def test_c2_pipeline_matches_lockstep_oracle(cuda_lib, orc, c2):
             rot_o, trans_o = F.rel_pose_error(orr["pose"], s.poses[k])
             assert abs(rot_gt - rot_o) <= 5e-4 and abs(trans_gt - trans_o) <= 5e-4
     pl.close()
+
+
+def _mem_available_gb():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) / 2 ** 20
+    except OSError:
+        pass
+    return 0.0
+
+
+def test_c3_fp16r_integration_bit_exact_at_1024(cuda_lib, orc):
+    """The precision form at its own size: 1024^3 FP16R (half + 9-bit residual)
+    over a 4 m cube, against the oracle's emulation of the same storage (bit for
+    bit) and its FP64 running average (the bounds of test_gpu_precision)."""
+    if _mem_available_gb() < 64:
+        pytest.skip("needs ~30 GB of host memory for the 1024^3 oracle volumes")
+    from azu_gb300 import api, synth
+    s = synth.sequence("c3", frames=3)
+    v = s.volume
+    assert v["resolution"] == 1024 and v["format"] == 2
+    g = api.TSDFVolume(api.volume_params(v["resolution"], v["voxel_size"], v["truncation"], v["max_weight"],
+                                         v["origin"], s.min_depth, s.max_depth, v["format"]))
+    o = orc.PrecisionVolume(orc.tsdf_params(resolution=v["resolution"], voxel_size=v["voxel_size"],
+                                            truncation=v["truncation"], max_weight=v["max_weight"],
+                                            origin=tuple(v["origin"]), min_depth=s.min_depth,
+                                            max_depth=s.max_depth), half_storage=2)
+    K = (s.fx, s.fy, s.cx, s.cy)
+    for k in range(len(s.poses)):
+        dm = synth.mm_to_meters(s.depth_mm[k])
+        g.integrate(dm, s.poses[k], K, s.width, s.height, s.min_depth, s.max_depth)
+        o.integrate(dm, s.poses[k], orc.intr(*K), s.width, s.height, s.min_depth, s.max_depth)
+    t, w = g.download()
+    assert np.array_equal(w, o.weight)
+    assert np.array_equal(t.view(np.uint32), o.tsdf.view(np.uint32))
+    m = np.flatnonzero(w > 0)
+    assert m.size > 1_000_000
+    ref = o.tsdf64[m]
+    assert np.abs(t[m].astype(np.float64) - ref).max() <= 1e-4
+    assert np.abs(t[m].astype(np.float16).astype(np.float64) - ref).max() <= 2e-3
