@@ -71,3 +71,29 @@ def test_batch_rejects_bad_scenes(cuda_lib, scenes):
     lib = _abi.load()
     h = C.c_void_p()
     assert lib.azu_batch_create(0, 0, None, C.byref(h)) == _abi.AZU_E_INVALID
+
+
+def test_c4_scene_set_equals_single_pipelines(cuda_lib):
+    """The batching form's own scene set (16 scenes, volumes 128^3..384^3,
+    320x240 and 640x480 frames), each cut to its first frames: one batch step
+    per frame index gives every scene its single pipeline's poses and volume."""
+    from azu_gb300 import api, synth
+    scenes = synth.batch_scenes(n_scenes=16, frames_scale=0.04)
+    assert len({s.volume["resolution"] for s in scenes}) >= 3 and len({s.width for s in scenes}) == 2
+    ref = [_single(sc) for sc in scenes]
+    b = api.Batch(scenes)
+    n = max(len(sc.depth_mm) for sc in scenes)
+    poses = [[] for _ in scenes]
+    for k in range(n):
+        res = b.process([sc.depth_mm[k] if k < len(sc.depth_mm) else None for sc in scenes])
+        for i, r in enumerate(res):
+            if r is not None:
+                poses[i].append(r["pose"])
+    for i in range(len(scenes)):
+        assert len(poses[i]) == len(ref[i][0])
+        for a, c in zip(poses[i], ref[i][0]):
+            assert np.array_equal(a.view(np.uint32), c.view(np.uint32)), i
+        t, w = b.volume(i).download()
+        assert np.array_equal(w, ref[i][2]), i
+        assert np.array_equal(t.view(np.uint32), ref[i][1].view(np.uint32)), i
+    b.close()
