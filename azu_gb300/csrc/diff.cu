@@ -13,7 +13,8 @@
 // f-dependent step back to the sample that set it, and t_near through the box
 // entry. Sample positions are recomputed, not stored: one pass marches and
 // keeps only the parameters of the f-dependent steps (a short ring), then the
-// reverse sweep re-samples those positions for the trilinear gradients.
+// reverse sweep re-samples those positions for the trilinear gradients; a
+// chain longer than the ring is taken in windows by marching the ray again.
 //
 // One thread per pixel. Per-block sums of the loss, its pose gradient and the
 // Gauss-Newton terms (J^T W J, J^T W r with IRLS Huber weights) are written as
@@ -75,7 +76,7 @@ struct DiffArgs {
     float* jac_out;     // dD/dxi per pixel (6) or null
     float* grad_tsdf;   // dL/dtsdf (res^3, accumulated) or null
     double* partials;   // [blocks][kDiffValues]
-    unsigned* overflow; // pixels whose f-dependent chain exceeded kMaxDep
+    unsigned* overflow; // pixels whose f-dependent chain outgrew the ring (taken by re-marching)
 };
 
 // Adjoint contribution of one sample: a_f * dF/d(everything) at t.
@@ -110,6 +111,77 @@ __device__ __forceinline__ void sample_adjoint(const DiffArgs& a, F3 co, F3 dir,
         atomicAdd(a.grad_tsdf + base + r * r + r, s * ux * ty * tz);
         atomicAdd(a.grad_tsdf + base + r * r + r + 1, s * tx * ty * tz);
     }
+}
+
+// Outcome of the forward march of one ray: the bracketing samples of the hit
+// (a before, b after the crossing) and the number of f-dependent steps (steps
+// whose length 0.8 f trunc exceeded the minimum) taken before it.
+struct MarchHit {
+    bool hit = false, dep_a = false, clip_b = false;
+    float t_a = 0.0f, f_a = 0.0f, t_b = 0.0f, f_b = 0.0f, t_hit = 0.0f;
+    int ndep = 0;
+};
+
+// The forward march (TSDFVolume.cpp:372-475) from t_near. The start time of
+// f-dependent step k is kept in dep_t: with lo < 0 in a ring (dep_t[k %
+// kMaxDep], the newest kMaxDep survive), else dep_t[k - lo] for k in [lo, hi),
+// hi - lo <= kMaxDep. The march is deterministic, so a second run with a
+// window recovers steps the ring overwrote.
+template <bool kHalf>
+__device__ MarchHit march_ray(const VolView& v, F3 co, F3 dir, float t_near, float t_far, float min_step,
+                              float far_step, float trunc, float* dep_t, int lo, int hi) {
+    MarchHit m;
+    if (!(t_near < t_far)) return m;
+    float t_prev = t_near, f_prev = 1.0f;
+    bool prev_valid = sample_tsdf<kHalf>(v, add3(co, mul3(dir, t_prev)), f_prev);
+    if (prev_valid && !isfinite(f_prev)) return m;
+    if (prev_valid && f_prev < 0.0f) return m;
+    while (t_prev < t_far) {
+        float step;
+        bool dep = false;
+        if (!prev_valid || f_prev >= 0.999f) {
+            step = far_step;
+        } else {
+            const float s = fm(fm(0.8f, f_prev), trunc);
+            dep = min_step < s;
+            step = min_step < s ? s : min_step;
+        }
+        const float tn = fa(t_prev, step);
+        const bool clip = !(tn < t_far) && tn != t_far;
+        const float t = (t_far < tn) ? t_far : tn;
+        if (!(t > t_prev)) break;
+        const F3 p = add3(co, mul3(dir, t));
+        float f = 1.0f;
+        const bool valid = sample_tsdf<kHalf>(v, p, f);
+        if (valid && !isfinite(f)) break;
+        if (valid && prev_valid) {
+            if (f_prev > 0.0f && f <= 0.0f) {
+                m.t_hit = fa(t_prev, fm(fs(t, t_prev), fd(f_prev, fs(f_prev, f))));
+                const F3 hp = add3(co, mul3(dir, m.t_hit));
+                F3 nrm;
+                if (compute_normal<kHalf>(v, hp, nrm) && finite3(hp)) {
+                    m.hit = true;
+                    m.t_a = t_prev; m.f_a = f_prev; m.t_b = t; m.f_b = f;
+                    m.dep_a = dep;
+                    m.clip_b = clip;
+                }
+                break;
+            }
+            if (f_prev < 0.0f && f >= 0.0f) break;
+        } else if (valid && f < 0.0f) {
+            break;
+        }
+        if (dep) {
+            if (lo < 0) dep_t[m.ndep % kMaxDep] = t_prev;
+            else if (m.ndep >= lo && m.ndep < hi) dep_t[m.ndep - lo] = t_prev;
+            ++m.ndep;
+        }
+        t_prev = t;
+        f_prev = f;
+        prev_valid = valid;
+        if (t >= t_far) break;
+    }
+    return m;
 }
 
 template <bool kHalf>
@@ -159,59 +231,13 @@ __global__ void __launch_bounds__(256) depth_adjoint_kernel(DiffArgs a) {
             t_far = (t1 < t_far) ? t1 : t_far;
         }
 
-        // forward march (TSDFVolume.cpp:372-475), keeping the f-dependent steps
+        // forward march, keeping the newest f-dependent steps in a ring
         float dep_t[kMaxDep];
-        int ndep = 0;
-        bool hit = false, dep_a = false, clip_b = false;
-        float t_a = 0.0f, f_a = 0.0f, t_b = 0.0f, f_b = 0.0f, t_hit = 0.0f;
-        do {
-            if (!(t_near < t_far)) break;
-            float t_prev = t_near, f_prev = 1.0f;
-            bool prev_valid = sample_tsdf<kHalf>(v, add3(co, mul3(dir, t_prev)), f_prev);
-            if (prev_valid && !isfinite(f_prev)) break;
-            if (prev_valid && f_prev < 0.0f) break;
-            while (t_prev < t_far) {
-                float step;
-                bool dep = false;
-                if (!prev_valid || f_prev >= 0.999f) {
-                    step = far_step;
-                } else {
-                    const float s = fm(fm(0.8f, f_prev), a.trunc);
-                    dep = min_step < s;
-                    step = min_step < s ? s : min_step;
-                }
-                const float tn = fa(t_prev, step);
-                const bool clip = !(tn < t_far) && tn != t_far;
-                const float t = (t_far < tn) ? t_far : tn;
-                if (!(t > t_prev)) break;
-                const F3 p = add3(co, mul3(dir, t));
-                float f = 1.0f;
-                const bool valid = sample_tsdf<kHalf>(v, p, f);
-                if (valid && !isfinite(f)) break;
-                if (valid && prev_valid) {
-                    if (f_prev > 0.0f && f <= 0.0f) {
-                        t_hit = fa(t_prev, fm(fs(t, t_prev), fd(f_prev, fs(f_prev, f))));
-                        const F3 hp = add3(co, mul3(dir, t_hit));
-                        F3 nrm;
-                        if (compute_normal<kHalf>(v, hp, nrm) && finite3(hp)) {
-                            hit = true;
-                            t_a = t_prev; f_a = f_prev; t_b = t; f_b = f;
-                            dep_a = dep;
-                            clip_b = clip;
-                        }
-                        break;
-                    }
-                    if (f_prev < 0.0f && f >= 0.0f) break;
-                } else if (valid && f < 0.0f) {
-                    break;
-                }
-                if (dep) dep_t[ndep++ % kMaxDep] = t_prev;
-                t_prev = t;
-                f_prev = f;
-                prev_valid = valid;
-                if (t >= t_far) break;
-            }
-        } while (false);
+        const MarchHit mh = march_ray<kHalf>(v, co, dir, t_near, t_far, min_step, far_step, a.trunc, dep_t, -1, 0);
+        const bool hit = mh.hit;
+        const int ndep = mh.ndep;
+        const float t_a = mh.t_a, f_a = mh.f_a, t_b = mh.t_b, f_b = mh.f_b, t_hit = mh.t_hit;
+        const bool dep_a = mh.dep_a, clip_b = mh.clip_b;
 
         const float D = hit ? t_hit / ray_norm : 0.0f;
         if (a.depth_out) a.depth_out[o] = D;
@@ -238,10 +264,18 @@ __global__ void __launch_bounds__(256) depth_adjoint_kernel(DiffArgs a) {
             at += (1.0f - f_a / den) * inv_rn;
             sample_adjoint<kHalf>(a, co, dir, rn, R0, t_a, af, dr, at, J);
             const int kept = ndep < kMaxDep ? ndep : kMaxDep;
-            if (ndep > kMaxDep) atomicAdd(a.overflow, 1u);
             for (int i = 0; i < kept; ++i) {
                 const float tk = dep_t[(ndep - 1 - i) % kMaxDep];
                 sample_adjoint<kHalf>(a, co, dir, rn, R0, tk, at * 0.8f * a.trunc, dr, at, J);
+            }
+            // older steps the ring overwrote: march again and take them
+            // kMaxDep at a time, newest window first
+            if (ndep > kMaxDep) atomicAdd(a.overflow, 1u);
+            for (int hi = ndep - kMaxDep; hi > 0; hi -= kMaxDep) {
+                const int lo = hi > kMaxDep ? hi - kMaxDep : 0;
+                march_ray<kHalf>(v, co, dir, t_near, t_far, min_step, far_step, a.trunc, dep_t, lo, hi);
+                for (int k = hi - 1; k >= lo; --k)
+                    sample_adjoint<kHalf>(a, co, dir, rn, R0, dep_t[k - lo], at * 0.8f * a.trunc, dr, at, J);
             }
             if (near_axis >= 0) {
                 const float da = comp(dir, near_axis);

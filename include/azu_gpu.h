@@ -163,8 +163,9 @@ int azu_volume_render_depth(azu_volume* v, const float pose[16], float fx, float
  * dD/dxi and IRLS weights w = min(1, delta/|r|). Optional device outputs:
  * d_depth (float[W*H]), d_jacobian (float[6*W*H], dD/dxi per pixel),
  * d_grad_tsdf (float[res^3], dL/dtsdf ADDED to its contents). chain_overflow
- * (host, optional) counts pixels whose chain of f-dependent steps exceeded the
- * 24 kept for the reverse sweep (their oldest terms are dropped). */
+ * (host, optional) counts pixels whose chain of f-dependent steps was longer
+ * than the 24 the reverse sweep keeps at a time (their older steps are
+ * recovered by marching the ray again; every term is kept). */
 int azu_volume_depth_backward(azu_volume* v, const float pose[16], float fx, float fy, float cx, float cy,
                               int width, int height, const float* d_depth_obs, float huber_delta, float* d_depth,
                               float* d_jacobian, float* d_grad_tsdf, double sums[35], unsigned* chain_overflow);

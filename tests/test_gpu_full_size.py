@@ -13,6 +13,9 @@ spheres), GPU against the oracle.
                 5e-4 rad / 5e-4 m
   precision     the FP16R form at its own size (c3: 1024^3 over a 4 m cube)
                 against the oracle's storage emulation bit for bit
+  adjoint       the differentiation form at its own size (c5: 512^3 from 100
+                frames, 640x480) against the FP64 CPU adjoint and FP64 central
+                differences
 """
 import numpy as np
 import pytest
@@ -158,3 +161,62 @@ def test_c3_fp16r_integration_bit_exact_at_1024(cuda_lib, orc):
     ref = o.tsdf64[m]
     assert np.abs(t[m].astype(np.float64) - ref).max() <= 1e-4
     assert np.abs(t[m].astype(np.float16).astype(np.float64) - ref).max() <= 2e-3
+
+
+def test_c5_adjoint_at_512(cuda_lib, orc):
+    """The differentiation form at its own size (c5): 512^3 from 100 c2 frames,
+    640x480 depth at a pose perturbed by N(0, 2 deg) rotation and N(0, 2 cm)
+    translation per axis (seed 2024), Huber 1 cm against frame 100. The GPU
+    backward against the FP64 CPU adjoint of the same float march (the
+    tolerances of test_gpu_diff), and its per-pixel dD/dxi against FP64 central
+    differences of the rendered depth (step 1e-6; 99% of the rays within 1e-3 +
+    1e-2 relative, the rest change branch inside the step)."""
+    from azu_gb300 import api, synth
+    s = synth.sequence("c2", frames=101)
+    v = s.volume
+    g = api.TSDFVolume(api.volume_params(v["resolution"], v["voxel_size"], v["truncation"], v["max_weight"],
+                                         v["origin"], s.min_depth, s.max_depth))
+    K = (s.fx, s.fy, s.cx, s.cy)
+    for k in range(100):
+        g.integrate(synth.mm_to_meters(s.depth_mm[k]), s.poses[k], K, s.width, s.height, s.min_depth, s.max_depth)
+    obs = synth.mm_to_meters(s.depth_mm[100]).astype(np.float32)
+    rng = np.random.default_rng(2024)
+    w = rng.normal(0.0, np.radians(2.0), 3)
+    th = np.linalg.norm(w)
+    Wx = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+    R = np.eye(3) + np.sin(th) / th * Wx + (1 - np.cos(th)) / th ** 2 * (Wx @ Wx)
+    start = s.poses[100].astype(np.float64).copy()
+    start[:3, :3] = start[:3, :3] @ R
+    start[:3, 3] += rng.normal(0.0, 0.02, 3)
+    start = start.astype(np.float32)
+    r = g.depth_backward(start, K, s.width, s.height, obs, 0.01, jacobian=True)
+    t, wt = g.download()
+    prm = orc.tsdf_params(resolution=v["resolution"], voxel_size=v["voxel_size"], truncation=v["truncation"],
+                          max_weight=v["max_weight"], origin=tuple(v["origin"]), min_depth=s.min_depth,
+                          max_depth=s.max_depth)
+    Ko = orc.intr(*K)
+    o = orc.depth_adjoint_f(prm, t, wt, start, Ko, s.width, s.height, depth_obs=obs, huber_delta=0.01, jac=True)
+    assert np.array_equal(r["depth"] > 0, o["depth"] > 0)
+    hit = o["depth"] > 0
+    assert hit.sum() > 50_000 and r["n_valid"] == o["n_valid"]
+    assert np.max(np.abs(r["depth"][hit] - o["depth"][hit])) <= 2e-6
+    Jg, Jo = r["jacobian"][hit], o["jac"][hit]
+    assert np.all(np.abs(Jg - Jo) <= 1e-5 + 1e-3 * np.abs(Jo))
+    assert abs(r["loss"] - o["loss"]) <= 1e-4 * o["loss"]
+    assert np.allclose(r["grad_xi"], o["grad_xi"], rtol=1e-3, atol=1e-5)
+    # per-pixel dD/dxi against FP64 central differences of the rendered depth
+    # (step 1e-6): the whole-image loss jumps where a ray changes surface inside
+    # the step, so the check is per ray, on rays that hit on both sides
+    t64 = t.astype(np.float64)
+    P = start.astype(np.float64)
+    for j in range(6):
+        xi = np.zeros(6)
+        xi[j] = 1e-6
+        dp = orc.depth_loss_d(prm, t64, wt, P, xi, Ko, s.width, s.height)["depth"]
+        dm = orc.depth_loss_d(prm, t64, wt, P, -xi, Ko, s.width, s.height)["depth"]
+        both = hit & (dp > 0) & (dm > 0)
+        fd = (dp[both] - dm[both]) / 2e-6
+        jg = r["jacobian"][..., j][both].astype(np.float64)
+        ok = np.abs(jg - fd) <= 1e-3 + 1e-2 * np.abs(fd)
+        assert both.sum() > 0.99 * hit.sum(), j
+        assert ok.mean() >= 0.99, (j, ok.mean(), np.median(np.abs(jg - fd)))
