@@ -413,48 +413,61 @@ __device__ __forceinline__ void reduce_grid_t(const IcpArgs& a, int slot, double
     __syncthreads();
 }
 
-// FP32 path: a warp takes two values per round with all their loads in flight
-// (one L2 round trip per two values); per value the same order as above.
-template <>
-__device__ __forceinline__ void reduce_grid_t<float>(const IcpArgs& a, int slot, double* s_sum_raw, int* s_isum) {
-    float* s_sum = reinterpret_cast<float*>(s_sum_raw);
+// FP32 path: a warp takes kVals values per round with all their loads in
+// flight (one L2 round trip per round), lane l loading slots l + 32 j for
+// j < kPL; per value the same order as above (the slots beyond the grid would
+// only add +0, which leaves a float sum that started at +0 unchanged), so every
+// instantiation gives the same bits.
+template <int kPL, int kVals>
+__device__ __forceinline__ void reduce_grid_f(const IcpArgs& a, int slot, float* s_sum, int* s_isum) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
     const int nb = a.vblocks;
-    for (int k0 = warp; k0 < kNF + kNI; k0 += 2 * nw) {
-        unsigned w[2][kPerLane];
+    for (int k0 = warp; k0 < kNF + kNI; k0 += kVals * nw) {
+        unsigned w[kVals][kPL];
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
+        for (int r = 0; r < kVals; ++r) {
             const int k = k0 + r * nw;
             const unsigned* src =
                 k < kNF ? reinterpret_cast<const unsigned*>(a.partials) + (static_cast<size_t>(slot) * kNF + k) * nb
                         : reinterpret_cast<const unsigned*>(a.ipartials) +
                               (static_cast<size_t>(slot) * kNI + (k - kNF)) * nb;
 #pragma unroll
-            for (int j = 0; j < kPerLane; ++j) {
+            for (int j = 0; j < kPL; ++j) {
                 const int b = lane + 32 * j;
                 w[r][j] = (b < nb && k < kNF + kNI) ? __ldcg(src + b) : 0u;
             }
         }
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
+        for (int r = 0; r < kVals; ++r) {
             const int k = k0 + r * nw;
             if (k < kNF) {
                 float sum = 0.0f;
 #pragma unroll
-                for (int j = 0; j < kPerLane; ++j) sum += __uint_as_float(w[r][j]);
+                for (int j = 0; j < kPL; ++j) sum += __uint_as_float(w[r][j]);
                 for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
                 if (lane == 0) s_sum[k] = sum;
             } else if (k < kNF + kNI) {
                 int sum = 0;
 #pragma unroll
-                for (int j = 0; j < kPerLane; ++j) sum += static_cast<int>(w[r][j]);
+                for (int j = 0; j < kPL; ++j) sum += static_cast<int>(w[r][j]);
                 for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
                 if (lane == 0) s_isum[k - kNF] = sum;
             }
         }
     }
     __syncthreads();
+}
+
+// Up to 160 partial slots (one block per SM) and 16 warps: all 34 values in one
+// round; otherwise two values per warp and round over up to kMaxGridBlocks.
+template <>
+__device__ __forceinline__ void reduce_grid_t<float>(const IcpArgs& a, int slot, double* s_sum_raw, int* s_isum) {
+    float* s_sum = reinterpret_cast<float*>(s_sum_raw);
+    if (a.vblocks <= 5 * 32 && 3 * static_cast<int>(blockDim.x >> 5) >= kNF + kNI)
+        reduce_grid_f<5, 3>(a, slot, s_sum, s_isum);
+    else
+        reduce_grid_f<kPerLane, 2>(a, slot, s_sum, s_isum);
 }
 
 __device__ void reduce_grid(const IcpArgs& a, int slot, double* s_sum, int* s_isum) {
