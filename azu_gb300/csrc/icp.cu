@@ -1087,8 +1087,8 @@ struct azu_tracker {
     float* d_est = nullptr;   // 16 estimate, 16 ref, 16 prev
     azu_icp_result* d_result = nullptr;
     float* d_build = nullptr;
-    void* d_many = nullptr;   // track_many: estimates, refs and results
-    size_t many_cap = 0;
+    void* d_many = nullptr;   // track_many: per-candidate scratch, estimates, refs, results, launch table
+    size_t many_cap = 0;      // candidates d_many is laid out for
 };
 
 namespace azu {
@@ -1373,38 +1373,96 @@ extern "C" int azu_tracker_track_many(azu_tracker* t, int width, int height, con
     AZU_TRY_CUDA(cudaSetDevice(t->device));
     const azu_tracker_params p = params ? sanitize(*params) : t->p;
     cudaStream_t s = t->stream.s;
+    // Layout of d_many for cap candidates (each part 256-byte aligned): the
+    // candidates' own partial slots and barrier words, then estimates,
+    // reference poses, results, launch arguments and block table. The scratch
+    // sits first so that its barrier words keep their place between calls.
+    auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
+    const size_t nb = static_cast<size_t>(t->nblocks);
+    constexpr size_t kBarWords = 4 + sizeof(LevelState) / 4 + 1;
+    const size_t sz_p = up(sizeof(double) * 2 * kNF * nb), sz_i = up(sizeof(int) * 2 * kNI * nb);
+    const size_t sz_b = up(sizeof(unsigned) * kBarWords), per = sz_p + sz_i + sz_b;
     if (static_cast<size_t>(count) > t->many_cap) {
         AZU_TRY_CUDA(cudaStreamSynchronize(s));
         if (t->d_many) cudaFree(t->d_many);
         t->d_many = nullptr;
         t->many_cap = 0;
-        AZU_TRY_CUDA(cudaMalloc(&t->d_many, count * (32 * sizeof(float) + sizeof(azu_icp_result))));
-        t->many_cap = count;
+        const size_t c = static_cast<size_t>(count);
+        const size_t bytes = per * c + up(32 * sizeof(float) * c) + up(sizeof(azu_icp_result) * c) +
+                             up(sizeof(IcpArgs) * c) + up(sizeof(int) * (c + 1));
+        AZU_TRY_CUDA(cudaMalloc(&t->d_many, bytes));
+        AZU_TRY_CUDA(cudaMemsetAsync(t->d_many, 0, bytes, s));  // barrier words start at zero
+        t->many_cap = c;
     }
-    float* d_est = reinterpret_cast<float*>(t->d_many);
-    float* d_ref = d_est + 16 * count;
-    azu_icp_result* d_res = reinterpret_cast<azu_icp_result*>(d_est + 32 * count);
+    const size_t cap = t->many_cap;
+    char* base = static_cast<char*>(t->d_many);
+    float* d_est = reinterpret_cast<float*>(base + per * cap);
+    float* d_ref = d_est + 16 * cap;
+    azu_icp_result* d_res = reinterpret_cast<azu_icp_result*>(base + per * cap + up(32 * sizeof(float) * cap));
+    IcpArgs* d_args = reinterpret_cast<IcpArgs*>(reinterpret_cast<char*>(d_res) + up(sizeof(azu_icp_result) * cap));
+    int* d_first = reinterpret_cast<int*>(reinterpret_cast<char*>(d_args) + up(sizeof(IcpArgs) * cap));
+    auto bar_of = [&](int k) { return reinterpret_cast<unsigned*>(base + per * k + sz_p + sz_i); };
     AZU_TRY_CUDA(cudaMemcpyAsync(d_est, estimates, 16 * count * sizeof(float), cudaMemcpyHostToDevice, s));
     AZU_TRY_CUDA(cudaMemcpyAsync(d_ref, ref_poses ? ref_poses : estimates, 16 * count * sizeof(float),
                                  cudaMemcpyHostToDevice, s));
     const size_t img = static_cast<size_t>(model_w) * model_h * 3;
+    // Candidates side by side in one cooperative launch, each on an equal share
+    // of the resident blocks with its own slots and barrier words. The slot
+    // count is the tracker's, so every solve equals track_prepared's; more
+    // candidates than resident blocks run one launch after another.
+    int sms = 0, occ = 0;
+    AZU_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->device));
+    AZU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, icp_batch_kernel, kIcpThreads, 0));
+    const int grid = sms * std::min(occ, 2);
+    const bool side_by_side = count > 1 && count <= grid;
+    std::vector<IcpArgs> args(side_by_side ? count : 0);
+    std::vector<int> first(side_by_side ? count + 1 : 0, 0);
     for (int k = 0; k < count; ++k) {
         IcpArgs a;
         fill_args_p(t, p, a, d_model_vertices + img * k, d_model_normals + img * k, model_w, model_h);
         a.d_estimate = d_est + 16 * k;
         a.d_ref = d_ref + 16 * k;
         a.d_result = d_res + k;
-        if (int rc = icp_launch(t, a, s)) return rc;
+        if (side_by_side) {
+            a.partials = reinterpret_cast<double*>(base + per * k);
+            a.ipartials = reinterpret_cast<int*>(base + per * k + sz_p);
+            a.bar = bar_of(k);
+            a.err = a.bar + 2;
+            a.state = a.bar + 4;
+            args[k] = a;
+            first[k + 1] = first[k] + grid / count;
+        } else if (int rc = icp_launch(t, a, s)) {
+            return rc;
+        }
+    }
+    if (side_by_side) {
+        AZU_TRY_CUDA(cudaMemcpyAsync(d_args, args.data(), count * sizeof(IcpArgs), cudaMemcpyHostToDevice, s));
+        AZU_TRY_CUDA(cudaMemcpyAsync(d_first, first.data(), (count + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(first[count]);
+        cfg.blockDim = dim3(kIcpThreads);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        AZU_TRY_CUDA(cudaLaunchKernelEx(&cfg, icp_batch_kernel, static_cast<const IcpArgs*>(d_args),
+                                        static_cast<const int*>(d_first), count));
     }
     AZU_TRY_CUDA(cudaMemcpyAsync(out, d_res, count * sizeof(azu_icp_result), cudaMemcpyDeviceToHost, s));
     AZU_TRY_CUDA(cudaStreamSynchronize(s));
+    bool timed_out = false;
     for (int k = 0; k < count; ++k)
         if (out[k].status == AZU_E_TIMEOUT) {
-            unsigned z = 0;
-            cudaMemcpy(t->bar + 2, &z, sizeof(z), cudaMemcpyHostToDevice);
-            set_error("ICP grid barrier timed out");
-            return AZU_E_TIMEOUT;
+            timed_out = true;
+            const unsigned z = 0;
+            cudaMemcpy(side_by_side ? bar_of(k) + 2 : t->bar + 2, &z, sizeof(z), cudaMemcpyHostToDevice);
         }
+    if (timed_out) {
+        set_error("ICP grid barrier timed out");
+        return AZU_E_TIMEOUT;
+    }
     return AZU_OK;
 }
 
