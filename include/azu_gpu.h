@@ -229,8 +229,10 @@ int azu_tracker_track_prepared(azu_tracker* t, int width, int height, const floa
  * model image k (model_w * model_h * 3 floats apart in d_model_vertices /
  * d_model_normals) from estimates[k] with reference pose ref_poses[k] (NULL:
  * the estimates), with `params` (NULL: the tracker's) — e.g. the coarse
- * stage's level-2-only iterations and wider gates. Launched back to back on
- * the tracker's stream; results (count, host) are read back once. */
+ * stage's level-2-only iterations and wider gates. The solves run side by side
+ * in one cooperative launch on the tracker's stream (one after another when
+ * count exceeds the GPU's resident ICP blocks), each bit-identical to
+ * track_prepared; results (count, host) are read back once. */
 int azu_tracker_track_many(azu_tracker* t, int width, int height, const float* d_model_vertices,
                            const float* d_model_normals, int model_w, int model_h, int count, const float* estimates,
                            const float* ref_poses, const azu_tracker_params* params, azu_icp_result* out);
