@@ -1,6 +1,7 @@
 """Oracle (test infrastructure only): ctypes binding of oracle/_build/liborc.so,
 the CPU restatement of Azu's KinectFusion hot path. Imported by tests/,
-__graft_entry__.smoke() and bench.py's CPU-baseline leg only, as the checker.
+__graft_entry__.smoke() and bench.py's CPU-baseline leg only, to compare results
+against and to time the CPU path.
 
 Arrays are numpy; poses are row-major (4, 4) float32 world-from-camera.
 """

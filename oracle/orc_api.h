@@ -1,7 +1,7 @@
 /* Oracle (test infrastructure only): C entry points of the CPU restatement of
  * Azu's per-frame KinectFusion hot path. Only tests, __graft_entry__.smoke()
- * and bench.py's CPU-baseline leg load this library, as the checker; the
- * product never links it.
+ * and bench.py's CPU-baseline leg load this library, to compare results
+ * against and to time the CPU path; the product never links it.
  *
  * Conventions: poses are row-major float[16] (element (r, c) at 4 r + c),
  * world-from-camera. Vertex/normal maps are float[3 * W * H] (x, y, z per pixel,
