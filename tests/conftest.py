@@ -21,7 +21,7 @@ def orc():
 
 @pytest.fixture(scope="session")
 def cuda_lib():
-    """The built CUDA backend on a GPU machine; builds it when missing."""
+    """The built CUDA backend on a machine with a GPU; builds it when missing."""
     from azu_gb300 import _abi, build
     if not os.path.exists(_abi.LIB_PATH):
         build.build()
