@@ -263,10 +263,16 @@ __device__ __forceinline__ void associate_range(const IcpArgs& a, const Rel& r, 
 // Partials are stored value-major, [slot][value][block], so the grid reduction
 // reads them coalesced; the partial buffers and the shared staging are sized
 // for double and reinterpreted for float.
+// FP32 values take half of the staging, so consecutive slots alternate halves
+// (buf) and the block needs no barrier after the partial stores: a half is
+// written again two slots later, after the next slot's barrier, which every
+// thread reaches only when its reads of this slot are done.
 template <typename T>
-__device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc, int slot, int vb, double* s_red_raw) {
+__device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc, int slot, int vb, double* s_red_raw,
+                                               int buf) {
+    static_assert(sizeof(T) == 4, "two staging halves hold FP32 values only");
     constexpr int kNV = kNF + kNI;  // 34
-    T* s_red = reinterpret_cast<T*>(s_red_raw);
+    T* s_red = reinterpret_cast<T*>(s_red_raw) + buf * (kIcpThreads / 32) * kNV;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
     T v[32];
@@ -293,7 +299,6 @@ __device__ __forceinline__ void reduce_block_t(const IcpArgs& a, const Acc& acc,
         for (int w = 0; w < nw; ++w) sum += s_red[w * kNV + k];
         a.ipartials[(static_cast<size_t>(slot) * kNI + (k - kNF)) * nb + vb] = static_cast<int>(sum);
     }
-    __syncthreads();
 }
 
 // Error-free sum: s + e == a + b exactly (Knuth's TwoSum).
@@ -344,9 +349,9 @@ __device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, in
     __syncthreads();
 }
 
-__device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, int vb, double* s_red) {
+__device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, int vb, double* s_red, int buf) {
     if (a.precision) reduce_block_comp(a, acc, slot, vb, s_red);
-    else reduce_block_t<float>(a, acc, slot, vb, s_red);
+    else reduce_block_t<float>(a, acc, slot, vb, s_red, buf);
 }
 
 // One association pass over the pixels of every partial slot this block owns
@@ -355,14 +360,15 @@ __device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, int vb, doubl
 // so a smaller grid (several scenes tracked side by side) gives the same sums.
 __device__ __forceinline__ void associate_all(const IcpArgs& a, const Rel& rel, const IcpLevel& L, int n, int slot,
                                               double* s_red, int gb, int gn) {
-    for (int vb = gb; vb < a.vblocks; vb += gn) {
+    int buf = 0;
+    for (int vb = gb; vb < a.vblocks; vb += gn, buf ^= 1) {
         Acc acc;
 #pragma unroll
         for (int k = 0; k < kNF; ++k) acc.f[k] = 0.0f;
 #pragma unroll
         for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
         associate_range(a, rel, L, vb * blockDim.x + threadIdx.x, a.vblocks * blockDim.x, n, acc);
-        reduce_block(a, acc, slot, vb, s_red);
+        reduce_block(a, acc, slot, vb, s_red, buf);
     }
 }
 
