@@ -123,6 +123,7 @@ SIGNATURES = {
                                                C.POINTER(TrackerParams), fp, fp, vp, fp, fp, fp,
                                                C.POINTER(C.c_int)]),
     "azu_tracker_live_maps": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "azu_testing_set_icp_wait": (C.c_int, [C.c_uint, C.c_uint]),
     # preprocessor
     "azu_preprocessor_create": (C.c_int, [C.c_int, C.c_int, vp, C.POINTER(vp)]),
     "azu_preprocessor_destroy": (C.c_int, [vp]),

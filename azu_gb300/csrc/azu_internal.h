@@ -175,6 +175,8 @@ int pipeline_enqueue_input_on(azu_pipeline* pl, cudaStream_t s);
 int pipeline_enqueue_track_on(azu_pipeline* pl, bool first, cudaStream_t s);
 int pipeline_enqueue_commit(azu_pipeline* pl);
 int pipeline_read_result(azu_pipeline* pl, azu_frame_result* out);
+// Resets the tracker's barrier words on stream s (after a wait ran out).
+int tracker_clear_barrier(azu_tracker* t, cudaStream_t s);
 PipelineFrameView pipeline_frame_view(azu_pipeline* pl);
 }  // namespace azu
 

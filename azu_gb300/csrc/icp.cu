@@ -87,20 +87,32 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     return v;
 }
 
-__device__ void grid_sync(unsigned* bar, unsigned* err, unsigned nblocks, unsigned& gen) {
+// The wait limits of every barrier: the spin limit and the arrival count that
+// releases a barrier (the group's block count). A testing hook may lower the
+// limit and raise the count by extra arrivals that never come, so that a wait
+// runs out by design; the kernel then finishes with the error word set.
+__device__ unsigned g_icp_spin_limit = kSpinLimit;
+__device__ unsigned g_icp_extra_arrivals = 0;
+
+struct WaitLimits {
+    unsigned spins;     // iterations before a wait gives up
+    unsigned arrivals;  // arrivals that complete a barrier
+};
+
+__device__ void grid_sync(unsigned* bar, unsigned* err, WaitLimits wl, unsigned& gen) {
     __syncthreads();
     if (threadIdx.x == 0) {
         if (ld_acquire(err) == 0) {
             __threadfence();
             const unsigned arrived = atomicAdd(&bar[0], 1u);
-            if (arrived == nblocks - 1) {
+            if (arrived == wl.arrivals - 1) {
                 atomicExch(&bar[0], 0u);
                 __threadfence();
                 atomicAdd(&bar[1], 1u);
             } else {
                 unsigned spins = 0;
                 while (ld_acquire(&bar[1]) == gen) {
-                    if (++spins > kSpinLimit) {
+                    if (++spins > wl.spins) {
                         atomicExch(err, kDevErrBarrierTimeout);
                         break;
                     }
@@ -121,13 +133,13 @@ __device__ void grid_sync(unsigned* bar, unsigned* err, unsigned nblocks, unsign
 // on its own (the result is then reported as a timeout).
 // The last block resets the arrival count at once: no block arrives again
 // before release_all, which it reaches after this reset.
-__device__ bool arrive_last(unsigned* bar, unsigned* err, unsigned nblocks, int* s_flag) {
+__device__ bool arrive_last(unsigned* bar, unsigned* err, WaitLimits wl, int* s_flag) {
     __syncthreads();
     if (threadIdx.x == 0) {
         int last = 1;
         if (ld_acquire(err) == 0) {
             __threadfence();
-            last = (atomicAdd(&bar[0], 1u) == nblocks - 1) ? 1 : 0;
+            last = (atomicAdd(&bar[0], 1u) == wl.arrivals - 1) ? 1 : 0;
             if (last) atomicExch(&bar[0], 0u);
             __threadfence();
         }
@@ -147,11 +159,11 @@ __device__ void release_all(unsigned* bar, unsigned* err, unsigned& gen) {
     __syncthreads();
 }
 
-__device__ void wait_release(unsigned* bar, unsigned* err, unsigned& gen) {
+__device__ void wait_release(unsigned* bar, unsigned* err, WaitLimits wl, unsigned& gen) {
     if (threadIdx.x == 0) {
         unsigned spins = 0;
         while (ld_acquire(err) == 0 && ld_acquire(&bar[1]) == gen) {
-            if (++spins > kSpinLimit) {
+            if (++spins > wl.spins) {
                 atomicExch(err, kDevErrBarrierTimeout);
                 break;
             }
@@ -917,9 +929,12 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
     __shared__ azu_icp_result s_res;
     __shared__ int s_retry;
     __shared__ int s_last;
+    __shared__ WaitLimits s_wl;
 
     if (threadIdx.x == 0) {
         s_gen = ld_acquire(&a.bar[1]);
+        s_wl.spins = g_icp_spin_limit;
+        s_wl.arrivals = static_cast<unsigned>(gn) + g_icp_extra_arrivals;
         float ref[16];
         for (int i = 0; i < 16; ++i) ref[i] = a.d_ref[i];
         inverse4(ref, s_refinv);
@@ -927,6 +942,7 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
     }
     __syncthreads();
     unsigned gen = s_gen;
+    const WaitLimits wl = s_wl;
     int slot = 0;
 
     if (a.build_level >= 0) {  // single association pass (parity probe)
@@ -937,7 +953,7 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
         const int iw = L.W - 2, ih = L.H - 2;
         const int n = iw > 0 && ih > 0 ? iw * ih : 0;
         associate_all(a, rel, L, n, 0, s_red, gb, gn);
-        grid_sync(a.bar, a.err, gn, gen);
+        grid_sync(a.bar, a.err, wl, gen);
         reduce_grid(a, 0, sm.sum, sm.isum);
         if (gb == 0 && threadIdx.x == 0) {
             int k = 0;
@@ -990,7 +1006,7 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
                 associate_all(a, rel, L, n, slot, s_red, gb, gn);
                 constexpr int kWords = static_cast<int>(sizeof(LevelState) / 4);
                 unsigned* st_words = reinterpret_cast<unsigned*>(&st);
-                if (arrive_last(a.bar, a.err, gn, &s_last)) {
+                if (arrive_last(a.bar, a.err, wl, &s_last)) {
                     reduce_grid(a, slot, sm.sum, sm.isum);
                     if (threadIdx.x < 32) solve_step(a, level, sm, st);
                     __syncthreads();
@@ -999,7 +1015,7 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
                     __threadfence();
                     release_all(a.bar, a.err, gen);
                 } else {
-                    wait_release(a.bar, a.err, gen);
+                    wait_release(a.bar, a.err, wl, gen);
                     for (int i = threadIdx.x; i <= kWords; i += blockDim.x) {
                         const unsigned w = __ldcg(a.state + i);
                         if (i < kWords) st_words[i] = w;
@@ -1043,10 +1059,13 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
 
     if (gb == 0 && threadIdx.x == 0) {
         azu_icp_result res = s_res;
-        res.status = ld_acquire(a.err) ? AZU_E_TIMEOUT : AZU_OK;
+        const bool timed_out = ld_acquire(a.err) != 0;
+        res.status = timed_out ? AZU_E_TIMEOUT : AZU_OK;
         *a.d_result = res;
         if (a.d_prev) {
-            const int q = classify(res, a.d_prev);
+            // a track whose wait ran out is graded Failed: the pose stays at
+            // prev and nothing is fused from this frame
+            const int q = timed_out ? 2 : classify(res, a.d_prev);
             if (a.d_quality) *a.d_quality = q;
             if (a.d_gate) *a.d_gate = (q == 0) ? 1 : 0;
             if (a.d_pose_out) {
@@ -1263,6 +1282,17 @@ int tracker_prepare_dev(azu_tracker* t, const float* d_depth, int W, int H, cuda
     return launch_prepare_live(d_depth, W, H, t->p.fx, t->p.fy, t->p.cx, t->p.cy, t->V, t->N, t->D, s);
 }
 
+// Barrier words back to their initial state (arrivals, generation, error),
+// ordered on stream s after the launch that used them. After a wait ran out,
+// blocks that arrived before the error was set leave the arrival count
+// nonzero; the next launch would then release a barrier early.
+int clear_barrier_words(unsigned* bar, cudaStream_t s) {
+    AZU_TRY_CUDA(cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), s));
+    return AZU_OK;
+}
+
+int tracker_clear_barrier(azu_tracker* t, cudaStream_t s) { return clear_barrier_words(t->bar, s); }
+
 }  // namespace azu
 
 using namespace azu;
@@ -1356,8 +1386,8 @@ extern "C" int azu_tracker_track_prepared(azu_tracker* t, int width, int height,
     AZU_TRY_CUDA(cudaMemcpyAsync(out, t->d_result, sizeof(azu_icp_result), cudaMemcpyDeviceToHost, t->stream.s));
     AZU_TRY_CUDA(cudaStreamSynchronize(t->stream.s));
     if (out->status == AZU_E_TIMEOUT) {
-        unsigned z = 0;
-        cudaMemcpy(t->bar + 2, &z, sizeof(z), cudaMemcpyHostToDevice);
+        if (int rc = clear_barrier_words(t->bar, t->stream.s)) return rc;
+        AZU_TRY_CUDA(cudaStreamSynchronize(t->stream.s));
         set_error("ICP grid barrier timed out");
         return AZU_E_TIMEOUT;
     }
@@ -1462,10 +1492,10 @@ extern "C" int azu_tracker_track_many(azu_tracker* t, int width, int height, con
     for (int k = 0; k < count; ++k)
         if (out[k].status == AZU_E_TIMEOUT) {
             timed_out = true;
-            const unsigned z = 0;
-            cudaMemcpy(side_by_side ? bar_of(k) + 2 : t->bar + 2, &z, sizeof(z), cudaMemcpyHostToDevice);
+            if (int rc = clear_barrier_words(side_by_side ? bar_of(k) : t->bar, s)) return rc;
         }
     if (timed_out) {
+        AZU_TRY_CUDA(cudaStreamSynchronize(s));
         set_error("ICP grid barrier timed out");
         return AZU_E_TIMEOUT;
     }
@@ -1505,8 +1535,8 @@ extern "C" int azu_tracker_build_system(azu_tracker* t, int level, const float* 
     AZU_TRY_CUDA(cudaMemcpyAsync(&err, t->bar + 2, sizeof(err), cudaMemcpyDeviceToHost, t->stream.s));
     AZU_TRY_CUDA(cudaStreamSynchronize(t->stream.s));
     if (err) {
-        unsigned z = 0;
-        cudaMemcpy(t->bar + 2, &z, sizeof(z), cudaMemcpyHostToDevice);
+        if (int rc = clear_barrier_words(t->bar, t->stream.s)) return rc;
+        AZU_TRY_CUDA(cudaStreamSynchronize(t->stream.s));
         set_error("ICP grid barrier timed out");
         return AZU_E_TIMEOUT;
     }
@@ -1693,5 +1723,17 @@ extern "C" int azu_icp_build_system_noalloc(const float* d_live_vertices, const 
     std::memcpy(b, out + 36, 6 * sizeof(float));
     *residual = out[42];
     std::memcpy(counts, out + 43, 6 * sizeof(int));
+    return AZU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Testing hook: the wait limits every ICP launch on the current device reads
+// at its start (see WaitLimits). Lets a test make a barrier wait run out on
+// purpose, through the bounded path only: no wait is left unbounded.
+extern "C" int azu_testing_set_icp_wait(unsigned spin_limit, unsigned extra_arrivals) {
+    AZU_CHECK_ARG(extra_arrivals <= 1024, "extra_arrivals");
+    const unsigned spins = spin_limit ? spin_limit : azu::kSpinLimit;
+    AZU_TRY_CUDA(cudaMemcpyToSymbol(azu::g_icp_spin_limit, &spins, sizeof(spins)));
+    AZU_TRY_CUDA(cudaMemcpyToSymbol(azu::g_icp_extra_arrivals, &extra_arrivals, sizeof(extra_arrivals)));
     return AZU_OK;
 }

@@ -339,6 +339,9 @@ static int read_staged_result(azu_pipeline* pl, azu_frame_result* out) {
     out->frame_index = pl->frames - 1;  // run_frame has counted this frame
     if (st.quality == -1) std::memset(&out->icp, 0, sizeof(out->icp));
     if (out->icp.status == AZU_E_TIMEOUT) {
+        // the frame was graded Failed on the device; the next frame's tracking
+        // (after this on the pipeline's stream) starts from clean barrier words
+        if (int rc = tracker_clear_barrier(pl->trk, pl->s)) return rc;
         set_error("ICP grid barrier timed out");
         return AZU_E_TIMEOUT;
     }
@@ -377,6 +380,7 @@ int pipeline_read_result(azu_pipeline* pl, azu_frame_result* out) {
     out->frame_index = st.frame_index - 1;
     if (st.quality == -1) std::memset(&out->icp, 0, sizeof(out->icp));
     if (out->icp.status == AZU_E_TIMEOUT) {
+        if (int rc = tracker_clear_barrier(pl->trk, pl->s)) return rc;
         set_error("ICP grid barrier timed out");
         return AZU_E_TIMEOUT;
     }
@@ -500,6 +504,8 @@ extern "C" int azu_pipeline_reset(azu_pipeline* pl) {
     AZU_TRY_CUDA(cudaStreamSynchronize(pl->s));
     if (int rc = azu_volume_reset(pl->vol)) return rc;
     if (pl->pre) if (int rc = azu_preprocessor_reset(pl->pre)) return rc;
+    if (int rc = tracker_clear_barrier(pl->trk, pl->s)) return rc;
+    AZU_TRY_CUDA(cudaStreamSynchronize(pl->s));
     pl->frames = 0;
     pl->buf = 0;
     pl->vol->integrated_frames = 0;

@@ -493,6 +493,19 @@ void* azu_batch_stream(azu_batch* b);
 int azu_batch_uses_graph(azu_batch* b);
 int azu_batch_synchronize(azu_batch* b);
 
+/* ------------------------------------------------------------------------ */
+/* Testing hooks (no counterpart in the reference).                          */
+/* ------------------------------------------------------------------------ */
+
+/* Wait limits of every later ICP launch on the current device: each barrier
+ * wait gives up after spin_limit polls (0 = the default, about a quarter of a
+ * second), and a barrier completes only after extra_arrivals more arrivals
+ * than the launch has blocks (0 = normal). extra_arrivals > 0 makes every
+ * wait run out on purpose, so a test can check that the call reports
+ * AZU_E_TIMEOUT, that the frame is graded Failed and fuses nothing, and that
+ * the next call works. Synchronous; not for use while ICP work is in flight. */
+int azu_testing_set_icp_wait(unsigned spin_limit, unsigned extra_arrivals);
+
 #ifdef __cplusplus
 }
 #endif
