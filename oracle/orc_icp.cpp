@@ -16,6 +16,7 @@
 // rounding; decisions can differ only at a threshold's exact edge.
 #include "orc_api.h"
 #include "orc_math.h"
+#include "orc_linalg.h"
 
 #include <vector>
 
@@ -36,48 +37,8 @@ inline float huberLoss(float a) { return (a <= kHuberK) ? a * a : 2.0f * kHuberK
 inline bool modelVertexValid(V3 v) { return finite3(v) && sqnorm(v) > kModelVertexNormSqMin; }
 inline bool normalValid(V3 n) { return finite3(n) && sqnorm(n) > kNormalNormSqMin; }
 
-// Symmetric eigenvalues by cyclic Jacobi (double), ascending.
-void jacobiEigen(int n, double* a /* n*n row-major, destroyed */, double* ev, double* vec /* n*n or null */) {
-    if (vec) for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) vec[i * n + j] = (i == j);
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        double off = 0.0;
-        for (int i = 0; i < n; ++i) for (int j = i + 1; j < n; ++j) off += a[i * n + j] * a[i * n + j];
-        if (off < 1e-300) break;
-        for (int p = 0; p < n; ++p) {
-            for (int q = p + 1; q < n; ++q) {
-                const double apq = a[p * n + q];
-                if (apq == 0.0) continue;
-                const double theta = (a[q * n + q] - a[p * n + p]) / (2.0 * apq);
-                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < n; ++k) {
-                    const double akp = a[k * n + p], akq = a[k * n + q];
-                    a[k * n + p] = c * akp - s * akq;
-                    a[k * n + q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < n; ++k) {
-                    const double apk = a[p * n + k], aqk = a[q * n + k];
-                    a[p * n + k] = c * apk - s * aqk;
-                    a[q * n + k] = s * apk + c * aqk;
-                }
-                if (vec)
-                    for (int k = 0; k < n; ++k) {
-                        const double vkp = vec[k * n + p], vkq = vec[k * n + q];
-                        vec[k * n + p] = c * vkp - s * vkq;
-                        vec[k * n + q] = s * vkp + c * vkq;
-                    }
-            }
-        }
-    }
-    for (int i = 0; i < n; ++i) ev[i] = a[i * n + i];
-    // ascending sort (with vectors)
-    for (int i = 0; i < n; ++i)
-        for (int j = i + 1; j < n; ++j)
-            if (ev[j] < ev[i]) {
-                std::swap(ev[i], ev[j]);
-                if (vec) for (int k = 0; k < n; ++k) std::swap(vec[k * n + i], vec[k * n + j]);
-            }
-}
+// Symmetric eigenvalues by cyclic Jacobi (double), ascending (orc_linalg.h).
+inline void jacobiEigen(int n, double* a, double* ev, double* vec) { linalg::jacobi_eigen(n, a, ev, vec); }
 
 // dampingForHessian (include/tracking/ICPShared.h:86-100).
 float dampingForHessian(const float A[36], int level) {
@@ -90,46 +51,8 @@ float dampingForHessian(const float A[36], int level) {
     return level == 0 ? kDampingLevel0 : kDampingDefault;
 }
 
-// A x = b by LDL^T with symmetric diagonal pivoting (float).
-void ldltSolve(const float A_in[36], const float b[6], float x[6]) {
-    float A[36];
-    std::memcpy(A, A_in, sizeof(A));
-    int perm[6] = {0, 1, 2, 3, 4, 5};
-    float L[36] = {0}, D[6];
-    for (int k = 0; k < 6; ++k) {
-        int p = k;
-        for (int i = k + 1; i < 6; ++i) if (std::fabs(A[i * 6 + i]) > std::fabs(A[p * 6 + p])) p = i;
-        if (p != k) {
-            for (int j = 0; j < 6; ++j) std::swap(A[k * 6 + j], A[p * 6 + j]);
-            for (int i = 0; i < 6; ++i) std::swap(A[i * 6 + k], A[i * 6 + p]);
-            for (int j = 0; j < k; ++j) std::swap(L[k * 6 + j], L[p * 6 + j]);
-            std::swap(perm[k], perm[p]);
-        }
-        D[k] = A[k * 6 + k];
-        L[k * 6 + k] = 1.0f;
-        for (int i = k + 1; i < 6; ++i) L[i * 6 + k] = A[i * 6 + k] / D[k];
-        for (int i = k + 1; i < 6; ++i)
-            for (int j = k + 1; j <= i; ++j) {
-                A[i * 6 + j] -= L[i * 6 + k] * A[j * 6 + k];
-                A[j * 6 + i] = A[i * 6 + j];
-            }
-        for (int i = k + 1; i < 6; ++i) A[i * 6 + k] = A[k * 6 + i] = 0.0f;
-    }
-    float y[6];
-    for (int i = 0; i < 6; ++i) {
-        float s = b[perm[i]];
-        for (int j = 0; j < i; ++j) s -= L[i * 6 + j] * y[j];
-        y[i] = s;
-    }
-    for (int i = 0; i < 6; ++i) y[i] /= D[i];
-    float z[6];
-    for (int i = 5; i >= 0; --i) {
-        float s = y[i];
-        for (int j = i + 1; j < 6; ++j) s -= L[j * 6 + i] * z[j];
-        z[i] = s;
-    }
-    for (int i = 0; i < 6; ++i) x[perm[i]] = z[i];
-}
+// A x = b by LDL^T with symmetric diagonal pivoting (float, orc_linalg.h).
+inline void ldltSolve(const float A_in[36], const float b[6], float x[6]) { linalg::ldlt_solve6(A_in, b, x); }
 
 // projectToSO3 (include/tracking/ICPShared.h:102-110): U V^T with the sign fix.
 M3 projectToSO3(const M3& M) {

@@ -1,0 +1,172 @@
+"""The CPU restatement (oracle/) pinned to the reference's OWN code.
+
+oracle/ref.mk compiles the reference's hot-path sources unmodified — TSDFVolume,
+ICPTracker, FrameData, MarchingCubes, SignalConditioner, SuperResolution,
+KinectSensor, PLYExporter, GLBExporter — against the project's Eigen-API shim
+(Eigen is not installed here) into oracle/_ref/. Two kinds of checks:
+
+  contracts   the reference's own contract programs of the path (its
+              tests/*.cpp, hand-derived expectations) linked against that
+              build: every check passes, except the two writer checks that a
+              write into a read-only directory fails, which cannot fail for the
+              root user these tests run as (reported, not hidden)
+  pinning     the restatement and the reference build run the same c1 inputs:
+              integration (values, weights, newly observed counts), raycast,
+              marching cubes (positions, normals, welded indices), point cloud,
+              vertex/normal maps and pyramid, the ICP linear system (one fold
+              thread: the reference's float sums in its own order), the
+              preprocessor chain, all bit for bit; ICP poses within 1e-6
+
+These need the reference checkout (the build reads its sources in place);
+where it is absent they skip. The GPU path is compared with the restatement
+(tests/test_gpu_*), so these close the chain GPU == restatement == reference.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import refimpl as R
+
+pytestmark = pytest.mark.skipif(not R.available(), reason="the reference checkout is not present")
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CONTRACTS = ["tsdf_integration_race_contract", "tsdf_integration_min_depth_contract", "fusion_bias_contract",
+             "tsdf_raycast_contract", "tsdf_subvoxel_thin_feature_contract", "raycast_accuracy_contract",
+             "tsdf_reset_contract", "coordinate_rounding_contract", "icp_weighting_contract",
+             "icp_numeric_policy_contract", "icp_refpose_contract", "icp_lowres_model_contract",
+             "tracking_policy_contract", "depth_consistency_contract", "marching_cubes_table_contract",
+             "mesh_welding_contract", "marching_cubes_winding_contract", "marching_cubes_frontier_contract",
+             "mesh_truncation_progress_contract", "marching_cubes_sphere_contract", "mesh_color_invariant_contract",
+             "mesh_validation_contract", "depth_domain_contract", "depth_ema_determinism_contract",
+             "cas_border_contract", "ply_writer_contract", "glb_writer_contract", "glb_linear_color_contract",
+             "kinect_pairing_contract"]
+# Checks that a write into a read-only directory fails: root writes anyway.
+ROOT_ONLY_FAILS = ("unwritable", "G3:")
+
+
+@pytest.fixture(scope="module")
+def contracts_built():
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "-f", "ref.mk",
+                    "REF=" + R.reference_dir(), "contracts"], check=True)
+    return os.path.join(ROOT, "oracle", "_ref", "contracts")
+
+
+@pytest.mark.parametrize("name", CONTRACTS)
+def test_reference_contract_passes(contracts_built, name, tmp_path):
+    out = subprocess.run([os.path.join(contracts_built, name)], cwd=tmp_path, capture_output=True, text=True,
+                         errors="replace", timeout=900)
+    fails = [l for l in out.stdout.splitlines() if l.startswith("FAIL:")]
+    if out.returncode != 0 and os.geteuid() == 0:
+        assert fails and all(any(k in l for k in ROOT_ONLY_FAILS) for l in fails), out.stdout[-3000:]
+        return
+    assert out.returncode == 0, out.stdout[-3000:] + out.stderr[-2000:]
+
+
+@pytest.fixture(scope="module")
+def c1(orc):
+    from azu_gb300 import synth
+    s = synth.sequence("c1", frames=10)
+    prm = dict(s.volume)
+    prm.pop("format")
+    P = orc.tsdf_params(**prm, min_depth=s.min_depth, max_depth=s.max_depth)
+    K = orc.intr(s.fx, s.fy, s.cx, s.cy)
+    return s, P, K
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def test_volume_integrate_raycast_mesh_point_cloud(orc, c1):
+    from azu_gb300 import synth
+    s, P, K = c1
+    o, r = orc.Volume(P), R.Volume(P)
+    for k in range(8):
+        dm = synth.mm_to_meters(s.depth_mm[k])
+        so = o.integrate(dm, s.poses[k], K, 640, 480, s.min_depth, s.max_depth)
+        sr = r.integrate(dm, s.poses[k], K, 640, 480, s.min_depth, s.max_depth)
+        assert so["newly_observed"] == sr["newly_observed"], k
+        t, w = r.arrays()
+        assert np.array_equal(_bits(t), _bits(o.tsdf)) and np.array_equal(w, o.weight), k
+    for k in (3, 7, 9):
+        ro, rr = o.raycast(s.poses[k], K, 640, 480), r.raycast(s.poses[k], K, 640, 480)
+        assert (ro["vertices"] != 0).any(-1).sum() > 20000
+        assert np.array_equal(_bits(ro["vertices"]), _bits(rr["vertices"])), k
+        assert np.array_equal(_bits(ro["normals"]), _bits(rr["normals"])), k
+    mo, mr = o.extract_mesh(), r.mesh()
+    assert len(mr["indices"]) > 100000
+    assert np.array_equal(_bits(mo["positions"]), _bits(mr["positions"]))
+    assert np.array_equal(_bits(mo["normals"]), _bits(mr["normals"]))
+    assert np.array_equal(np.asarray(mo["indices"]).reshape(-1), mr["indices"])
+    assert np.array_equal(np.asarray(mo["colors"]).reshape(-1, 3), mr["colors"])
+    po, co = o.point_cloud()
+    n = orc.get_threads()
+    R.set_threads(1)  # the reference appends per OpenMP thread: one thread gives index order
+    try:
+        pr, cr = r.point_cloud()
+    finally:
+        R.set_threads(n)
+    assert len(pr) > 10000 and np.array_equal(_bits(po), _bits(pr)) and np.array_equal(co, cr)
+
+
+def test_frame_maps_and_pyramid(orc, c1):
+    from azu_gb300 import synth
+    s, P, K = c1
+    raw = synth.encode_raw(s.depth_mm[4])
+    d, v, n = R.build_frame(raw, K, s.min_depth, s.max_depth)
+    od, ov = orc.build_frame_raw(raw, K, s.min_depth, s.max_depth)
+    assert (d > 0).sum() > 100000
+    assert np.array_equal(_bits(d), _bits(od)) and np.array_equal(_bits(v), _bits(ov))
+    lv = R.frame_pyramid(d, v, K)
+    op = orc.frame_pyramid_from_depth(d, K)
+    for l in range(3):
+        for j in range(3):  # depth, vertices, normals
+            assert np.array_equal(_bits(lv[l][j]), _bits(op[l][j])), (l, j)
+    assert (lv[0][2] != 0).any(-1).sum() > 100000
+
+
+def test_icp_system_and_track(orc, c1):
+    from azu_gb300 import synth
+    s, P, K = c1
+    o = orc.Volume(P)
+    for k in range(6):
+        o.integrate(synth.mm_to_meters(s.depth_mm[k]), s.poses[k], K, 640, 480, s.min_depth, s.max_depth)
+    model = o.raycast(s.poses[5], K, 640, 480)
+    pyr = orc.frame_pyramid_from_depth(synth.mm_to_meters(s.depth_mm[6]), K)
+    prm = orc.icp_params(fold_threads=1)
+    for level in range(3):
+        H, W = pyr[level][0].shape
+        ro = R.icp_build_system(prm, K, pyr[level][1], pyr[level][2], W, H, model["vertices"], model["normals"],
+                                640, 480, s.poses[5], s.poses[5])
+        oo = orc.icp_build_system(prm, K, pyr[level][1], pyr[level][2], model["vertices"], model["normals"],
+                                  s.poses[5], s.poses[5])
+        oc = [oo[k] for k in ("inliers", "valid_live", "valid_model", "projected", "dist_filtered",
+                              "angle_filtered")]
+        assert oc[0] > 500, level
+        assert list(ro["counts"]) == oc, level
+        assert np.array_equal(_bits(ro["A"]), _bits(oo["A"])) and np.array_equal(_bits(ro["b"]), _bits(oo["b"]))
+        assert _bits(np.float32(ro["residual"])) == _bits(np.float32(oo["residual"]))
+    rr = R.icp_track(prm, K, [(lv[1], lv[2]) for lv in pyr], model["vertices"], model["normals"], 640, 480,
+                     s.poses[5], s.poses[5])
+    oi = orc.icp_track(prm, K, pyr, model["vertices"], model["normals"], s.poses[5], s.poses[5])
+    assert rr.tracking_ok and oi.tracking_ok and rr.inliers == oi.inliers
+    assert np.abs(np.array(rr.pose) - np.array(oi.pose)).max() <= 1e-6
+    assert R.classify_tracking(rr, s.poses[5]) == orc.classify_tracking(oi, s.poses[5])
+
+
+def test_preprocessor_chain(orc, c1):
+    from azu_gb300 import synth
+    s, P, K = c1
+    rng = np.random.default_rng(3)
+    rgb_tex = rng.integers(0, 256, (480, 640, 3), dtype=np.uint8)
+    cond = R.Conditioner()
+    op = orc.Preprocessor()
+    for k in range(4):
+        raw = synth.encode_raw(s.depth_mm[k])
+        rgb = synth.grey_rgb() if k % 2 == 0 else rgb_tex
+        dr, cr = cond.process(raw, rgb, s.min_depth, s.max_depth)
+        do, co, _ = op.process(raw, rgb, s.min_depth, s.max_depth)
+        assert np.array_equal(dr.reshape(480, 640), do), k
+        assert np.array_equal(cr.reshape(480, 640, 3), co), k
