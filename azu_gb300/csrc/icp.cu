@@ -596,6 +596,87 @@ __device__ bool chol_solve_d(const double* Ain, const double* b, double* x) {
     return true;
 }
 
+// Nearest proper rotation of a general 3x3 matrix M (row-major, double): U V^T
+// of its SVD with the direction of the smallest singular value flipped when
+// det(U V^T) < 0 (projectToSO3, include/tracking/ICPShared.h:102-110). V holds
+// the eigenvectors of M^T M (cyclic Jacobi), U = M V / sigma. This is the
+// exact path for matrices the Newton-Schulz steps below cannot bring to a
+// rotation (reflections, large scale errors); near-rotations never reach it.
+__device__ __noinline__ void nearest_rotation_d(const double* M, double* R) {
+    double a[9], V[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) a[3 * i + j] = M[i] * M[j] + M[3 + i] * M[3 + j] + M[6 + i] * M[6 + j];
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        const double off = a[1] * a[1] + a[2] * a[2] + a[5] * a[5];
+        if (!(off > 1e-300)) break;
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            const double apq = a[3 * p + q];
+            if (apq == 0.0) continue;
+            const double theta = (a[3 * q + q] - a[3 * p + p]) / (2.0 * apq);
+            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+            for (int k = 0; k < 3; ++k) {
+                const double akp = a[3 * k + p], akq = a[3 * k + q];
+                a[3 * k + p] = c * akp - sn * akq;
+                a[3 * k + q] = sn * akp + c * akq;
+            }
+            for (int k = 0; k < 3; ++k) {
+                const double apk = a[3 * p + k], aqk = a[3 * q + k];
+                a[3 * p + k] = c * apk - sn * aqk;
+                a[3 * q + k] = sn * apk + c * aqk;
+            }
+            for (int k = 0; k < 3; ++k) {
+                const double vkp = V[3 * k + p], vkq = V[3 * k + q];
+                V[3 * k + p] = c * vkp - sn * vkq;
+                V[3 * k + q] = sn * vkp + c * vkq;
+            }
+        }
+    }
+    double ev[3] = {a[0], a[4], a[8]};
+    int ord[3] = {0, 1, 2};  // ascending eigenvalues: ord[0] is the smallest singular value
+    for (int i = 0; i < 3; ++i)
+        for (int j = i + 1; j < 3; ++j)
+            if (ev[ord[j]] < ev[ord[i]]) { const int t = ord[i]; ord[i] = ord[j]; ord[j] = t; }
+    double U[9], Vs[9];
+    for (int c = 0; c < 3; ++c) {
+        const int e = ord[c];
+        const double sig = sqrt(fmax(ev[e], 1e-300));
+        for (int i = 0; i < 3; ++i) {
+            Vs[3 * i + c] = V[3 * i + e];
+            U[3 * i + c] = (M[3 * i] * V[e] + M[3 * i + 1] * V[3 + e] + M[3 * i + 2] * V[6 + e]) / sig;
+        }
+    }
+    if (!(ev[ord[0]] > 1e-24 * ev[ord[2]])) {  // rank-deficient: complete the frame
+        U[0] = U[4] * U[8] - U[7] * U[5];
+        U[3] = U[7] * U[2] - U[1] * U[8];
+        U[6] = U[1] * U[5] - U[4] * U[2];
+    }
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                R[3 * i + j] = U[3 * i] * Vs[3 * j] + U[3 * i + 1] * Vs[3 * j + 1] + U[3 * i + 2] * Vs[3 * j + 2];
+        const double det = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                           R[2] * (R[3] * R[7] - R[4] * R[6]);
+        if (det >= 0.0) break;
+        for (int i = 0; i < 3; ++i) U[3 * i] = -U[3 * i];
+    }
+}
+
+// True when X (row-major 3x3) is a rotation to tolerance: X^T X = I within
+// tol and det > 0.
+template <typename T>
+__device__ __forceinline__ bool is_rotation(const T* X, T tol) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const T g = X[i] * X[j] + X[3 + i] * X[3 + j] + X[6 + i] * X[6 + j];
+            if (!(fabs(g - (i == j ? T(1) : T(0))) <= tol)) return false;
+        }
+    const T det = X[0] * (X[4] * X[8] - X[5] * X[7]) - X[1] * (X[3] * X[8] - X[5] * X[6]) +
+                  X[2] * (X[3] * X[7] - X[4] * X[6]);
+    return det > T(0);
+}
+
 // Precision form: SE(3) exponential of the step and pose composition in FP64,
 // then the nearest rotation (orthogonal polar factor, = U V^T of the SVD for
 // det > 0) by two Newton-Schulz steps X <- X (3 I - X^T X) / 2 in FP64.
@@ -641,6 +722,10 @@ __device__ void compose_precise(float* pose, const double* x) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) X[k] = N[k];
     }
+    if (!is_rotation(X, 1e-9)) {
+        const double M[9] = {P[0], P[1], P[2], P[4], P[5], P[6], P[8], P[9], P[10]};
+        nearest_rotation_d(M, X);
+    }
     for (int i = 0; i < 3; ++i) {
         for (int j = 0; j < 3; ++j) pose[4 * i + j] = static_cast<float>(X[3 * i + j]);
         pose[4 * i + 3] = static_cast<float>(P[4 * i + 3]);
@@ -650,7 +735,8 @@ __device__ void compose_precise(float* pose, const double* x) {
 // The same projection in float by the Newton-Schulz iteration
 // X <- X (3 I - X^T X) / 2, which converges quadratically to the orthogonal
 // polar factor from a near-rotation (no division); two steps reach float
-// precision from the composed pose.
+// precision from the composed pose. A result that is not a rotation (the
+// input was a reflection or far from orthogonal) takes the exact SVD path.
 __device__ void project_so3_f(float* P) {
     float X[9];
     for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) X[3 * i + j] = P[4 * i + j];
@@ -672,6 +758,12 @@ __device__ void project_so3_f(float* P) {
                 N[3 * i + j] = 0.5f * (X[3 * i] * G[j] + X[3 * i + 1] * G[3 + j] + X[3 * i + 2] * G[6 + j]);
 #pragma unroll
         for (int k = 0; k < 9; ++k) X[k] = N[k];
+    }
+    if (!is_rotation(X, 1e-5f)) {
+        double M[9], Rd[9];
+        for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) M[3 * i + j] = P[4 * i + j];
+        nearest_rotation_d(M, Rd);
+        for (int k = 0; k < 9; ++k) X[k] = static_cast<float>(Rd[k]);
     }
     for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) P[4 * i + j] = X[3 * i + j];
 }

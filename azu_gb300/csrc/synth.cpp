@@ -117,3 +117,61 @@ extern "C" int azu_synth_render(const azu_synth_scene* sc, const double P[16], d
     }
     return 0;
 }
+
+// ---------------------------------------------------------------------------
+// The reference contract tests' room scene (tests/support/SyntheticScene.h of
+// the reference): the inside of a room box (centre (0, -0.05, 1.15), half
+// extents (1.2, 0.95, 1.25)), a box (centre (0.35, 0.55, 1.5), half extents
+// (0.3, 0.35, 0.25)) and a sphere (centre (-0.5, 0.2, 1.7), radius 0.3), as a
+// signed distance, sphere-traced per pixel in float: t from 0.05 m, at most 256
+// steps, below 8 m, a hit when the distance drops below 1e-5; Z-depth in metres
+// (0 on a miss). Used as a fixture for the parity tests of those contracts.
+namespace {
+
+struct F3s {
+    float x, y, z;
+};
+
+inline float len3(F3s a) { return std::sqrt(a.x * a.x + (a.y * a.y + a.z * a.z)); }
+
+inline float box_sdf(F3s p, F3s c, F3s h) {
+    const F3s q{std::fabs(p.x - c.x) - h.x, std::fabs(p.y - c.y) - h.y, std::fabs(p.z - c.z) - h.z};
+    const F3s qp{std::fmax(q.x, 0.0f), std::fmax(q.y, 0.0f), std::fmax(q.z, 0.0f)};
+    return len3(qp) + std::fmin(std::fmax(q.x, std::fmax(q.y, q.z)), 0.0f);
+}
+
+inline float room_sdf(F3s p) {
+    const float room = -box_sdf(p, F3s{0.0f, -0.05f, 1.15f}, F3s{1.2f, 0.95f, 1.25f});
+    const float box = box_sdf(p, F3s{0.35f, 0.55f, 1.5f}, F3s{0.3f, 0.35f, 0.25f});
+    const float sph = len3(F3s{p.x + 0.5f, p.y - 0.2f, p.z - 1.7f}) - 0.3f;
+    return std::fmin(room, std::fmin(box, sph));
+}
+
+}  // namespace
+
+extern "C" int azu_synth_room_depth(const float pose_wc[16], float fx, float fy, float cx, float cy, int W, int H,
+                                    float* depth_m) {
+    if (!pose_wc || !depth_m || W <= 0 || H <= 0) return -1;
+    const float* P = pose_wc;  // row-major world-from-camera
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int v = 0; v < H; ++v) {
+        for (int u = 0; u < W; ++u) {
+            const F3s rc{(static_cast<float>(u) - cx) / fx, (static_cast<float>(v) - cy) / fy, 1.0f};
+            const float nrm = len3(rc);
+            const F3s d{(P[0] * rc.x + (P[1] * rc.y + P[2] * rc.z)) / nrm, (P[4] * rc.x + (P[5] * rc.y + P[6] * rc.z)) / nrm,
+                        (P[8] * rc.x + (P[9] * rc.y + P[10] * rc.z)) / nrm};
+            const F3s o{P[3], P[7], P[11]};
+            float t = 0.05f, out = 0.0f;
+            for (int i = 0; i < 256 && t < 8.0f; ++i) {
+                const float s = room_sdf(F3s{o.x + d.x * t, o.y + d.y * t, o.z + d.z * t});
+                if (s < 1e-5f) {
+                    out = t / nrm;
+                    break;
+                }
+                t += s;
+            }
+            depth_m[static_cast<size_t>(v) * W + u] = out;
+        }
+    }
+    return 0;
+}

@@ -221,3 +221,33 @@ def encode_raw(depth_mm: np.ndarray, min_depth=MIN_DEPTH, max_depth=MAX_DEPTH) -
 
 def grey_rgb(w=W, h=H) -> np.ndarray:
     return np.full((h, w, 3), GREY, np.uint8)
+
+
+def room_depth(pose, w=W, h=H, fx=FX, fy=FY, cx=CX, cy=CY) -> np.ndarray:
+    """Depth in metres (0 = miss) of the room scene of the reference's contract
+    tests (a room interior with a box and a sphere, sphere-traced), for the
+    parity tests of those contracts."""
+    P = np.ascontiguousarray(np.asarray(pose, np.float32).reshape(16))
+    out = np.zeros((h, w), np.float32)
+    lib = _lib()
+    lib.azu_synth_room_depth.argtypes = [C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                         C.c_int, C.POINTER(C.c_float)]
+    rc = lib.azu_synth_room_depth(P.ctypes.data_as(C.POINTER(C.c_float)), fx, fy, cx, cy, w, h,
+                                  out.ctypes.data_as(C.POINTER(C.c_float)))
+    if rc != 0:
+        raise RuntimeError("azu_synth_room_depth failed")
+    return out
+
+
+def axis_angle_pose(axis_angle, t) -> np.ndarray:
+    """World-from-camera pose from a rotation vector (rad) and a translation,
+    float32 (the contract tests' makePose)."""
+    a = np.asarray(axis_angle, np.float64)
+    T = np.eye(4)
+    ang = float(np.linalg.norm(a))
+    if ang > 0:
+        k = a / ang
+        Kx = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+        T[:3, :3] = np.eye(3) + math.sin(ang) * Kx + (1 - math.cos(ang)) * Kx @ Kx
+    T[:3, 3] = t
+    return T.astype(np.float32)

@@ -33,6 +33,15 @@ constexpr float kConvergenceStep = 5e-5f, kAcceptableFinalStep = 1e-3f;
 constexpr int kMinInliersForIteration = 10, kMinInliersForOk = 100;
 
 inline V3 ld(const float* a, size_t i) { return V3(a[3 * i], a[3 * i + 1], a[3 * i + 2]); }
+
+// ICPTracker::sanitizeParams (src/tracking/ICPTracker.cpp:24-34): a non-finite
+// angle threshold falls back to 30 degrees, others are clamped to [0, 85].
+inline float sanitizeAngle(float a) {
+    if (!std::isfinite(a)) return 30.0f;
+    if (a < 0.0f) return 0.0f;
+    if (a > 85.0f) return 85.0f;
+    return a;
+}
 inline float huberLoss(float a) { return (a <= kHuberK) ? a * a : 2.0f * kHuberK * a - kHuberK * kHuberK; }
 inline bool modelVertexValid(V3 v) { return finite3(v) && sqnorm(v) > kModelVertexNormSqMin; }
 inline bool normalValid(V3 n) { return finite3(n) && sqnorm(n) > kNormalNormSqMin; }
@@ -172,7 +181,7 @@ int build_system_impl(const orc_icp_params* prm, orc_intrinsics camK, const floa
         const float sx = static_cast<float>(MW) / 640.0f, sy = static_cast<float>(MH) / 480.0f;
         K = orc_intrinsics{camK.fx * sx, camK.fy * sy, (camK.cx + 0.5f) * sx - 0.5f, (camK.cy + 0.5f) * sy - 0.5f};
     }
-    const float angle_cos = static_cast<float>(std::cos(prm->angle_threshold * M_PI / 180.0f));
+    const float angle_cos = static_cast<float>(std::cos(sanitizeAngle(prm->angle_threshold) * M_PI / 180.0f));
     const float dist2 = prm->dist_threshold * prm->dist_threshold;
     const M4 pose = M4::from(pose_rm);
     const M3 R_cw = pose.R();

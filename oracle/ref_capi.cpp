@@ -98,6 +98,11 @@ extern "C" {
 void* ref_volume_create(const orc_tsdf_params* p) { return new tsdf::TSDFVolume(tsdf_params_of(p)); }
 void ref_volume_destroy(void* h) { delete static_cast<tsdf::TSDFVolume*>(h); }
 
+// TSDFVolume::setParams: any difference clears the volume.
+void ref_volume_set_params(void* h, const orc_tsdf_params* p) {
+    static_cast<tsdf::TSDFVolume*>(h)->setParams(tsdf_params_of(p));
+}
+
 // Voxel contents in and out (tsdf, weight, colour[3 n] or NULL), z-major.
 void ref_volume_load(void* h, const float* tsdf, const float* weight, const float* color) {
     auto* v = static_cast<tsdf::TSDFVolume*>(h);

@@ -68,7 +68,7 @@ def lib():
         _lib.ref_volume_create.restype = C.c_void_p
         _lib.ref_conditioner_create.restype = C.c_void_p
         _lib.ref_volume_point_cloud.restype = C.c_int64
-        for f in ("ref_volume_destroy", "ref_volume_load", "ref_volume_store", "ref_volume_integrate",
+        for f in ("ref_volume_destroy", "ref_volume_set_params", "ref_volume_load", "ref_volume_store", "ref_volume_integrate",
                   "ref_volume_raycast", "ref_volume_point_cloud", "ref_volume_mesh", "ref_conditioner_destroy",
                   "ref_conditioner_process"):
             getattr(_lib, f).argtypes = None
@@ -102,6 +102,11 @@ class Volume:
             self.close()
         except Exception:
             pass
+
+    def set_params(self, p: O.TsdfParams):
+        lib().ref_volume_set_params(self.h, C.byref(p))
+        self.p = p
+        self.n = p.res ** 3
 
     def load(self, tsdf, weight, color=None):
         lib().ref_volume_load(self.h, _p(np.ascontiguousarray(tsdf, np.float32)),

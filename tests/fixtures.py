@@ -192,3 +192,137 @@ def rel_pose_error(a, b):
     d = np.linalg.inv(np.asarray(a, np.float64)) @ np.asarray(b, np.float64)
     c = max(-1.0, min(1.0, (np.trace(d[:3, :3]) - 1.0) * 0.5))
     return math.acos(c), float(np.linalg.norm(d[:3, 3]))
+
+
+# ---- tests/icp_numeric_policy_contract.cpp:97-140, 226-239 (fixture plumbing) --
+# One correspondence = a live level-0 pixel (vertex, normal) and the model pixel
+# its vertex projects onto at identity poses; float32 arithmetic in the
+# contract's order.
+def _f(x):
+    return np.float32(x)
+
+
+def back_project(px, py, z):
+    z = _f(z)
+    return np.array([(_f(px) - _f(CX)) / _f(FX) * z, (_f(py) - _f(CY)) / _f(FY) * z, z], np.float32)
+
+
+def projected_pixel(v):
+    inv_z = _f(1.0) / _f(v[2])
+    mx = int(math.floor(_f(_f(_f(FX) * _f(v[0])) * inv_z + _f(CX)) + _f(0.5)))
+    my = int(math.floor(_f(_f(_f(FY) * _f(v[1])) * inv_z + _f(CY)) + _f(0.5)))
+    return mx, my
+
+
+def make_corr(px, py, z, n, axis, offset):
+    lv = back_project(px, py, z)
+    mv = lv.copy()
+    mv[axis] = lv[axis] - _f(offset)
+    n = np.asarray(n, np.float32)
+    mpx, mpy = projected_pixel(lv)
+    return dict(lp=(px, py), mp=(mpx, mpy), lv=lv, ln=n.copy(), mv=mv, mn=n.copy())
+
+
+def corr_maps(cs):
+    """Live level-0 vertex/normal maps and model vertex/normal maps (640x480)."""
+    lv = np.zeros((H0, W0, 3), np.float32)
+    ln = np.zeros((H0, W0, 3), np.float32)
+    mv = np.zeros((H0, W0, 3), np.float32)
+    mn = np.zeros((H0, W0, 3), np.float32)
+    for c in cs:
+        (px, py), (mx, my) = c["lp"], c["mp"]
+        lv[py, px], ln[py, px] = c["lv"], c["ln"]
+        mv[my, mx], mn[my, mx] = c["mv"], c["mn"]
+    return lv, ln, mv, mn
+
+
+def grid_fixture(x0, x1, y0, y1, z, offset, n=(0.0, 0.0, 1.0)):
+    return [make_corr(x, y, z, n, 2, offset) for y in range(y0, y1 + 1) for x in range(x0, x1 + 1)]
+
+
+# :315-325 two point-symmetric rows, opposite 1 m residuals (rotation cap)
+def rotation_leak_fixture(per_row):
+    x0 = 320 - per_row // 2
+    cs = [make_corr(x0 + i, 450, 2.0, (0, 0, 1), 2, 1.0) for i in range(per_row)]
+    cs += [make_corr(x0 + i, 29, 2.0, (0, 0, 1), 2, -1.0) for i in range(per_row)]
+    return cs
+
+
+# :455-461 escalation: six symmetric pairs at 0.01 and one outlier at 0.08
+def escalation_fixture():
+    cs = []
+    for k in range(6):
+        cs.append(make_corr(319 - k, 239 - k, 1.0, (0, 0, 1), 2, 0.01))
+        cs.append(make_corr(320 + k, 240 + k, 1.0, (0, 0, 1), 2, 0.01))
+    cs.append(make_corr(320, 239, 1.0, (0, 0, 1), 2, 0.08))
+    return cs
+
+
+# :476-494 well-conditioned three walls (no escalation)
+def three_wall_fixture():
+    cs = []
+    for x in range(314, 326):
+        cs.append(make_corr(x, 150, 1.0, (0, 0, 1), 2, 0.01))
+        cs.append(make_corr(x, 329, 1.0, (0, 0, 1), 2, 0.01))
+    depths = (1.0, 1.5, 2.0, 2.5)
+    for x in range(300, 340):
+        for y in range(200, 240):
+            cs.append(make_corr(x, y, depths[(x + y) & 3], (1, 0, 0), 0, 0.0))
+        for y in range(240, 280):
+            cs.append(make_corr(x, y, depths[(2 * x + y) & 3], (0, 1, 0), 0, 0.0))
+    return cs
+
+
+# :541-552 ten clean +z pairs, plus one pixel (340, 260) with a chosen model normal
+def model_normal_fixture(extra_normal=None):
+    cs = []
+    for k in range(5):
+        cs.append(make_corr(319 - k, 239 - k, 1.0, (0, 0, 1), 2, 0.01))
+        cs.append(make_corr(320 + k, 240 + k, 1.0, (0, 0, 1), 2, 0.01))
+    if extra_normal is not None:
+        c = make_corr(340, 260, 1.0, (0, 0, 1), 2, 0.01)
+        c["mn"] = np.asarray(extra_normal, np.float32)
+        cs.append(c)
+    return cs
+
+
+# :637-651 a tangent wall (model normals (1,0,0)) with a chosen live normal
+def live_normal_fixture(live_n, offset=0.01, dist_offset=0.0):
+    cs = []
+    for k in range(5):
+        for i in range(2):
+            px, py = (320 + k, 240 + k) if i else (319 - k, 239 - k)
+            c = make_corr(px, py, 1.0, (1, 0, 0), 0, offset)
+            c["ln"] = np.asarray(live_n, np.float32)
+            if dist_offset:
+                c["mv"][2] = _f(c["mv"][2] + _f(dist_offset))
+            cs.append(c)
+    return cs
+
+
+# :731-742 live normals (1,0,0) against model normals (0,0,1): |dot| = 0
+def orthogonal_fixture():
+    cs = []
+    for k in range(5):
+        for i in range(2):
+            px, py = (320 + k, 240 + k) if i else (319 - k, 239 - k)
+            c = make_corr(px, py, 1.0, (0, 0, 1), 2, 0.01)
+            c["ln"] = np.array([1, 0, 0], np.float32)
+            cs.append(c)
+    return cs
+
+
+# :781-806 a reflected, non-orthonormal estimate and a zero residual
+REFLECTED_ESTIMATE = np.diag([-2.0, 1.0, 2.0, 1.0]).astype(np.float32)
+
+
+def reflection_fixture():
+    v_ref = np.array([0, 0, 2], np.float32)
+    mp = projected_pixel(v_ref)
+    return [dict(lp=(300 + i, 200), mp=mp, lv=np.array([0, 0, 1], np.float32), ln=np.array([0, 0, 1], np.float32),
+                 mv=v_ref.copy(), mn=np.array([0, 0, 1], np.float32)) for i in range(12)]
+
+
+ICP_TOL_MATCH = 1e-7     # the contract's kTolMatch
+ICP_HUBER_K = 0.02
+ICP_ROW_VY = (450.0 - CY) * 2.0 / FY
