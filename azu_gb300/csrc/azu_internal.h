@@ -98,6 +98,7 @@ struct azu_volume {
     unsigned long long* d_counters = nullptr;  // [0] newly observed (cumulative), [1] updated (last), [2] colour (last),
                                                // [3] updated (cumulative), [4] integrate work counter
     int int_blocks = 0;                        // resident blocks of the persistent integrate kernel
+    const void* int_kernel = nullptr;          // the kernel variant int_blocks was sized for
     float* d_depth_stage = nullptr;            // host-depth staging (integrate_host)
     uint8_t* d_rgb_stage = nullptr;
     size_t stage_pixels = 0;

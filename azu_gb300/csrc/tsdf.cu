@@ -20,6 +20,7 @@
 #include "azu_internal.h"
 #include "kf_math.cuh"
 #include "tsdf_sample.cuh"
+#include "fstep.cuh"
 
 namespace azu {
 
@@ -65,6 +66,7 @@ constexpr int kTileShift = 3;  // level-0 depth tiles are 8x8 pixels
 constexpr int kCullSeg = 16;   // voxels per culling piece of a 32-voxel chunk
 constexpr int kIntParts = 2;   // x-parts per 32-row item of the persistent kernel (shorter items, shorter tail)
 constexpr int kUpdGroup = 4;   // rows per software-pipelined update group (6 and 8 were slower)
+constexpr int kFineSide = 4;   // level-0 depth tiles a culling box may span a side before a coarser level is used
 
 // Deepest in-band depth of every 8x8 pixel tile (-inf when the tile has none),
 // level 0 of the tile pyramid. Eight lanes share a tile, one pixel row each.
@@ -223,6 +225,9 @@ __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res
                          pyramid != 0);
 }
 
+// fs_walk kept out of line (it runs once per item, not per voxel).
+__device__ __noinline__ float fs_walk_far(float v, float s, int n) { return fs_walk(v, s, n); }
+
 // Voxel-projective integration (TSDFVolume.cpp:282-329).
 //
 // The CPU steps the camera coordinate of a voxel row incrementally along x
@@ -325,8 +330,12 @@ __device__ __forceinline__ void integrate_item(
     wxe = min(wxe, (part + 1) * span - 1);
     if (wxs > wxe) return;  // no row of this warp reaches the image in this part
     const int xfirst = wxs & ~31;
-    if (row_on)
-        for (int x = x0; x < xfirst; ++x) c = add3(c, step);
+    if (row_on && xfirst > x0) {
+        // the sequential steps from x0 to the first chunk, replayed exactly
+        // by the closed form of the running float sum (fstep.cuh)
+        const int n0 = xfirst - x0;
+        c = mk3(fs_walk_far(c.x, step.x, n0), fs_walk_far(c.y, step.y, n0), fs_walk_far(c.z, step.z, n0));
+    }
 
     for (int xc = xfirst; xc <= wxe; xc += 32) {
         // cull (lane = row), per kCullSeg-voxel piece of the chunk so each
@@ -350,13 +359,33 @@ __device__ __forceinline__ void integrate_item(
                 const int iu1 = static_cast<int>(fminf(uhi, fW - 1.0f));
                 const int iv0 = static_cast<int>(fmaxf(vlo, 0.0f));
                 const int iv1 = static_cast<int>(fminf(vhi, fH - 1.0f));
-                const int ext = max(iu1 - iu0, iv1 - iv0) >> kTileShift;
-                const int l = min(ext ? 32 - __clz(ext) : 0, mip.levels - 1);
-                const int sh = kTileShift + l, w = mip.w[l];
-                const float* tl = tiles + mip.off[l];
-                const int a0 = (iv0 >> sh) * w, a1 = (iv1 >> sh) * w, b0 = iu0 >> sh, b1 = iu1 >> sh;
-                const float tm = fmaxf(fmaxf(__ldg(tl + a0 + b0), __ldg(tl + a0 + b1)),
-                                       fmaxf(__ldg(tl + a1 + b0), __ldg(tl + a1 + b1)));
+                const int tu0 = iu0 >> kTileShift, tu1 = iu1 >> kTileShift;
+                const int tv0 = iv0 >> kTileShift, tv1 = iv1 >> kTileShift;
+                float tm;
+                if (tu1 - tu0 < kFineSide && tv1 - tv0 < kFineSide) {
+                    // every level-0 tile of the box, all loads in flight together
+                    const int w0 = mip.w[0];
+                    float t[kFineSide * kFineSide];
+#pragma unroll
+                    for (int a = 0; a < kFineSide; ++a)
+#pragma unroll
+                        for (int b = 0; b < kFineSide; ++b)
+                            t[a * kFineSide + b] = (tv0 + a <= tv1 && tu0 + b <= tu1)
+                                                       ? __ldg(tiles + (tv0 + a) * w0 + tu0 + b)
+                                                       : -__int_as_float(0x7f800000);
+                    tm = t[0];
+#pragma unroll
+                    for (int i = 1; i < kFineSide * kFineSide; ++i) tm = fmaxf(tm, t[i]);
+                } else {
+                    // two tiles a side at the level that fits
+                    const int ext = max(iu1 - iu0, iv1 - iv0) >> kTileShift;
+                    const int l = min(ext ? 32 - __clz(ext) : 0, mip.levels - 1);
+                    const int sh = kTileShift + l, w = mip.w[l];
+                    const float* tl = tiles + mip.off[l];
+                    const int a0 = (iv0 >> sh) * w, a1 = (iv1 >> sh) * w, b0 = iu0 >> sh, b1 = iu1 >> sh;
+                    tm = fmaxf(fmaxf(__ldg(tl + a0 + b0), __ldg(tl + a0 + b1)),
+                               fmaxf(__ldg(tl + a1 + b0), __ldg(tl + a1 + b1)));
+                }
                 return !(fminf(ca.z, cb.z) > tm + cull_off);
             };
             for (int pa = xa; pa <= xb && !live; pa += kCullSeg) live = piece_live(pa, min(pa + kCullSeg - 1, xb));
@@ -461,12 +490,18 @@ __device__ __forceinline__ void integrate_item(
             for (int j = 0; j < kUpdGroup; ++j) {
                 if (pix[j] < 0) continue;
                 const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
-                const float tsdf_new = fminf(1.0f, fd(sdf[j], trunc));
+                // min(1, sdf / trunc) is exactly 1 for sdf >= trunc (a rounded
+                // quotient of operands in that order is >= 1): free space needs
+                // no division
+                const float tsdf_new = sdf[j] >= trunc ? 1.0f : fminf(1.0f, fd(sdf[j], trunc));
                 const float w_old = old[j].y;
                 n_new += (w_old == 0.0f);
                 ++n_upd;
                 const float wp1 = fa(w_old, 1.0f);
-                const float t = fd(fa(fm(old[j].x, w_old), tsdf_new), wp1);
+                // (1 w + 1) / (w + 1) is exactly 1 for an integer-valued weight:
+                // folding free space into free space needs no division either
+                const float t = (old[j].x == 1.0f && tsdf_new == 1.0f) ? 1.0f
+                                                                       : fd(fa(fm(old[j].x, w_old), tsdf_new), wp1);
                 const float w = fminf(wp1, max_w);
                 if (kResid) VoxR::store(vox, vi, t, w);
                 else Vox<kHalf>::store(vox, vi, t, w);

@@ -208,7 +208,12 @@ def encode_raw(depth_mm: np.ndarray, min_depth=MIN_DEPTH, max_depth=MAX_DEPTH) -
     """Kinect raw codes of mm depth via the reference's band-rejecting encoder
     (cpuDepthMetersToRaw, include/sensor/DepthValidity.h:100-109), float32
     arithmetic, std::lround rounding."""
-    m = mm_to_meters(depth_mm)
+    return encode_raw_m(mm_to_meters(depth_mm), min_depth, max_depth)
+
+
+def encode_raw_m(m: np.ndarray, min_depth=MIN_DEPTH, max_depth=MAX_DEPTH) -> np.ndarray:
+    """The same encoder from depth in metres (0 or out of band -> code 0)."""
+    m = np.asarray(m, np.float32)
     lo, hi = np.float32(min_depth), np.float32(max_depth)
     ok = np.isfinite(m) & (m >= lo) & (m <= hi)
     with np.errstate(divide="ignore", invalid="ignore"):

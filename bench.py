@@ -37,6 +37,14 @@ sys.path.insert(0, ROOT)
 METRIC = "frames/s @512³ TSDF, 640×480 (FP32 vs FP16-TSDF form, CPU ref); integrate GB/s"
 SEQ_FRAMES = 300
 MESH_EVERY = 30
+
+
+def mesh_due(step: int, steps: int) -> bool:
+    """The c2 config's mesh cadence keyed to the timed step index, so every
+    timed window carries mesh work: every 30th step, and the last step of a
+    window shorter than 30 (one mesh in fewer frames: the window then carries
+    more than its share)."""
+    return (step + 1) % MESH_EVERY == 0 or (steps < MESH_EVERY and step == steps - 1)
 W, H = 640, 480
 KERNELS_PER_FRAME_RAW = 19  # 7 preprocess + 2 frame maps + 2 depth tiles + ICP + 2 integrate + 3 brick distance + raycast + commit
 D2H_RESULT_BYTES = 336 + 264  # device pose state + azu_icp_result read back per frame
@@ -512,7 +520,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     seq, raw, rgb = load_sequence()
-    frames = max(1, min(args.steps, 24))
+    frames = max(1, args.steps)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
@@ -520,24 +528,32 @@ def run_reference(args):
     O.set_threads(threads)
     L = O.Lockstep(seq.volume, input_is_mm=False, min_depth=seq.min_depth, max_depth=seq.max_depth,
                    fold_threads=threads)
-    for k in range(min(args.warmup, 2)):
-        L.process(raw[k], rgb)
+    # the same warm-up frames, timed window and mesh cadence as the GPU arm
+    warm = max(args.warmup, 3)
+    for k in range(warm):
+        L.process(raw[k % SEQ_FRAMES], rgb)
+    n_mesh = 0
     t0 = time.perf_counter()
     for k in range(frames):
-        L.process(raw[(2 + k) % SEQ_FRAMES], rgb)
-        if k % MESH_EVERY == MESH_EVERY - 1:
+        L.process(raw[(warm + k) % SEQ_FRAMES], rgb)
+        if mesh_due(k, frames):
             L.vol.extract_mesh()
+            n_mesh += 1
     dt = time.perf_counter() - t0
     v = frames / dt
     line = {"metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus, "steps": frames,
-            "warmup": min(args.warmup, 2), "ms_per_step": 1000.0 * dt / frames, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dt / frames, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "c2: 512^3 fp32 TSDF over 2 m, 640x480 Kinect raw depth, 300-frame orbit",
-                       "resolution": 512, "image": "640x480", "mesh_every": MESH_EVERY},
+            "config": {"workload": "c2: 512^3 fp32 TSDF over 2 m, 640x480 Kinect raw depth (mm -> raw codes) + "
+                                   "grey RGB, 300-frame 360 deg orbit, 40 random spheres; mesh every 30 frames",
+                       "resolution": 512, "image": "640x480", "icp_iterations": [10, 5, 4], "mesh_every": MESH_EVERY,
+                       "meshes_in_timed_region": n_mesh},
             "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
-                             "sample": f"{frames} frames of c2 after 2 warm-up frames (the reference's C++ does not "
-                                       "build here: it needs Eigen3 and Qt6; the oracle restates its CPU path)"},
+                             "sample": f"frames {warm}..{warm + frames - 1} of c2 after {warm} warm-up frames, the "
+                                       "GPU arm's window (the oracle restates the reference's CPU path, whose own "
+                                       "sources are built and compared with it where the reference checkout is; "
+                                       "that build is not available on this machine)"},
             "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -602,7 +618,7 @@ def run_gpu(args):
             pl.process_frame_device(depth_ptr(frame), d_rgb.data_ptr())
             frame += 1
             launches += KERNELS_PER_FRAME_RAW
-            if frame % MESH_EVERY == 0:
+            if mesh_due(k, K):
                 info = mc.extract_counts(vol)
                 launches += info["launches"]
                 meshes.append(info)
@@ -619,6 +635,7 @@ def run_gpu(args):
     h_rgb_np = h_rgb.numpy()
     Ke = K
     qual = []
+    n_mesh_e2e = 0
     barrier()
     with ClockSampler(dev) as clk_e2e:
         t0 = time.perf_counter()
@@ -627,8 +644,9 @@ def run_gpu(args):
             r = pl.process_frame(h_raw_np[frame % SEQ_FRAMES], h_rgb_np)
             qual.append(r["quality"])
             frame += 1
-            if frame % MESH_EVERY == 0:
+            if mesh_due(k, Ke):
                 mc.extract_counts(vol)
+                n_mesh_e2e += 1
         e1.record(stream)
         barrier()
         e2e_wall = time.perf_counter() - t0
@@ -685,9 +703,11 @@ def run_gpu(args):
                                "RGB, 300-frame 360 deg orbit, 40 random spheres; mesh every 30 frames",
                    "resolution": 512, "image": "640x480", "icp_iterations": [10, 5, 4], "mesh_every": MESH_EVERY,
                    "cache": "inputs larger than L2 (1.07 GB volume read and written each frame)",
+                   "meshes_in_timed_region": len(meshes),
                    "graph": bool(pl.lib.azu_pipeline_uses_graph(pl.h)), "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": int(raw[0].nbytes + rgb.nbytes),
                 "d2h_bytes_per_step": D2H_RESULT_BYTES, "wall_frames_per_s": Ke / e2e_wall,
+                "meshes_in_timed_region": n_mesh_e2e,
                 "clocks": clk_e2e.summary()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,

@@ -9,14 +9,14 @@ not tabulated at all: it is computed from the cube index (an edge crosses when
 its two corner bits differ), and this script checks that the reference's
 edge_table equals that computation for all 256 rows.
 
-Run once where the reference is mounted:  python oracle/gen_mc_tables.py
+Run once where the reference checkout is:
+    python oracle/gen_mc_tables.py <reference>/include/meshing/MarchingCubesTables.h
 Writes oracle/orc_mc_tables.h and azu_gb300/csrc/mc_tables.h.
 """
 import os
 import re
 import sys
 
-REF = "/root/reference/include/meshing/MarchingCubesTables.h"
 EDGE_CORNERS = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4),
                 (0, 4), (1, 5), (2, 6), (3, 7)]
 
@@ -68,8 +68,10 @@ def emit(words, guard, ns):
 
 
 def main():
+    if len(sys.argv) != 2:
+        sys.exit("usage: gen_mc_tables.py <path of the reference's include/meshing/MarchingCubesTables.h>")
     here = os.path.dirname(os.path.abspath(__file__))
-    edge, tri = parse(open(REF).read())
+    edge, tri = parse(open(sys.argv[1]).read())
     bad = [i for i in range(256) if edge[i] != crossing_mask(i)]
     if bad:
         sys.exit(f"reference edge_table differs from the crossing-edge rule at rows {bad}")
