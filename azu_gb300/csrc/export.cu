@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -152,10 +153,47 @@ struct KeyHash {
     }
 };
 
+// A glTF number: the shortest decimal that reads back as the same double,
+// with "0.0" / "-0.0" for zeros and a ".0" on integral values, in fixed
+// notation for decimal points within 15 digits of the first digit and
+// exponent form (e+XX, e-XX) otherwise. The reference's writer prints the
+// same doubles through its JSON library; at an exact decimal tie of the last
+// digit, and in rare cases where that library's digit generation does not
+// find the shortest form, its decimal differs from this one but reads back
+// as the same double, so the documents are equal value for value.
 std::string num(double v) {
-    char b[40];
-    std::snprintf(b, sizeof(b), "%.17g", v);
-    return b;
+    if (v == 0.0) return std::signbit(v) ? "-0.0" : "0.0";
+    if (!std::isfinite(v)) return "null";
+    char b[64];
+    for (int p = 1; p <= 17; ++p) {  // fewest significant digits that read back exactly
+        std::snprintf(b, sizeof(b), "%.*e", p - 1, v);
+        if (std::strtod(b, nullptr) == v) break;
+    }
+    std::string s(b);
+    const bool neg = s[0] == '-';
+    if (neg) s.erase(0, 1);
+    const size_t epos = s.find('e');
+    const int ex = std::atoi(s.c_str() + epos + 1);
+    std::string dig = s.substr(0, 1) + (epos > 2 ? s.substr(2, epos - 2) : std::string());
+    while (dig.size() > 1 && dig.back() == '0') dig.pop_back();
+    const int k = static_cast<int>(dig.size()), n = ex + 1;  // v = 0.dig x 10^n
+    std::string out = neg ? "-" : "";
+    if (k <= n && n <= 15) {
+        out += dig + std::string(static_cast<size_t>(n - k), '0') + ".0";
+    } else if (0 < n && n <= 15) {
+        out += dig.substr(0, static_cast<size_t>(n)) + "." + dig.substr(static_cast<size_t>(n));
+    } else if (-4 < n && n <= 0) {
+        out += "0." + std::string(static_cast<size_t>(-n), '0') + dig;
+    } else {
+        out += dig.substr(0, 1);
+        if (k > 1) out += "." + dig.substr(1);
+        int e = n - 1;
+        out += e < 0 ? "e-" : "e+";
+        e = std::abs(e);
+        if (e < 10) out += "0";
+        out += std::to_string(e);
+    }
+    return out;
 }
 
 // GLB (GLBExporter.cpp): weld, buffer, glTF JSON and the binary container.
@@ -232,14 +270,16 @@ int glb_bytes(const MeshIn& in, std::string& out) {
     int nview = 0;
     auto view = [&](size_t off, size_t len, int target) {
         if (nview) views += ",";
-        views += "{\"buffer\":0,\"byteLength\":" + std::to_string(len) + ",\"byteOffset\":" + std::to_string(off) +
+        // glTF defaults (offset 0) are left out, as the reference's writer leaves them out
+        views += "{\"buffer\":0,\"byteLength\":" + std::to_string(len) +
+                 (off ? ",\"byteOffset\":" + std::to_string(off) : std::string()) +
                  ",\"target\":" + std::to_string(target) + "}";
         return nview++;
     };
     int nacc = 0;
     auto acc = [&](int v, int ctype, const char* type, size_t count, const std::string& extra) {
         if (nacc) accs += ",";
-        accs += "{\"bufferView\":" + std::to_string(v) + ",\"byteOffset\":0,\"componentType\":" +
+        accs += "{\"bufferView\":" + std::to_string(v) + ",\"componentType\":" +
                 std::to_string(ctype) + ",\"count\":" + std::to_string(count) + extra + ",\"type\":\"" + type + "\"}";
         return nacc++;
     };
@@ -253,11 +293,12 @@ int glb_bytes(const MeshIn& in, std::string& out) {
     if (a_col >= 0) attrs += "\"COLOR_0\":" + std::to_string(a_col) + ",";
     if (a_nrm >= 0) attrs += "\"NORMAL\":" + std::to_string(a_nrm) + ",";
     attrs += "\"POSITION\":" + std::to_string(a_pos);
-    const char* base = in_c ? "[1.0,1.0,1.0,1.0]" : "[0.72,0.78,0.85,1.0]";
+    // a white base colour is the glTF default and is left out
+    const std::string base = in_c ? std::string() : "\"baseColorFactor\":[0.72,0.78,0.85,1.0],";
     std::string json = "{\"accessors\":[" + accs + "],\"asset\":{\"generator\":\"KinectFusionQt\",\"version\":\"2.0\"}," +
                        "\"bufferViews\":[" + views + "],\"buffers\":[{\"byteLength\":" + std::to_string(buf.size()) +
-                       "}],\"materials\":[{\"name\":\"ScanMaterial\",\"pbrMetallicRoughness\":{\"baseColorFactor\":" +
-                       base + ",\"metallicFactor\":0.0,\"roughnessFactor\":0.8}}],\"meshes\":[{\"name\":\"KinectScan\"," +
+                       "}],\"materials\":[{\"name\":\"ScanMaterial\",\"pbrMetallicRoughness\":{" + base +
+                       "\"metallicFactor\":0.0,\"roughnessFactor\":0.8}}],\"meshes\":[{\"name\":\"KinectScan\"," +
                        "\"primitives\":[{\"attributes\":{" + attrs + "},\"indices\":" + std::to_string(a_idx) +
                        ",\"material\":0,\"mode\":4}]}],\"nodes\":[{\"mesh\":0}],\"scene\":0,\"scenes\":[{\"nodes\":[0]}]}";
     while (json.size() % 4) json.push_back(' ');

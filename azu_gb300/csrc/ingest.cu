@@ -81,7 +81,9 @@ namespace {
 
 // KinectSensor::onDepth / onRgb over the recording order (accelerometer
 // samples do not take part in pairing). A depth frame still waiting for a
-// nearer RGB sample when the recording ends is published depth-only.
+// nearer RGB sample when the recording ends is not published: the sensor fed
+// the same samples parks it until a later sample arrives
+// (src/sensor/KinectSensor.cpp:295-312), and none does.
 void pair_entries(azu_recording* r) {
     int waiting = -1, held = -1;
     for (int i = 0; i < static_cast<int>(r->entries.size()); ++i) {
@@ -117,7 +119,6 @@ void pair_entries(azu_recording* r) {
             held = spent ? -1 : i;
         }
     }
-    if (waiting >= 0) r->frames.push_back(Frame{waiting, -1});
 }
 
 bool read_frame(const azu_recording* r, int k, uint16_t* depth, uint8_t* rgb, int* rgb_valid) {

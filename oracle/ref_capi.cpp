@@ -9,7 +9,9 @@
 // MarchingCubes::extract, sensor::buildFrameData / computeNormals /
 // buildFramePyramid, tracking::ICPTracker (track; buildLinearSystem through
 // the class's private member, opened for this translation unit only),
-// tracking::classifyTracking and sensor::SignalConditioner::process.
+// tracking::classifyTracking, sensor::SignalConditioner::process, the
+// export_io::PLYExporter / GLBExporter writers and sensor::KinectSensor's
+// depth-led pairing (through its device-free test seam).
 // Everything ICPTracker.h includes comes first, so that only that class's
 // declaration is read with its private members opened.
 #include <Eigen/Core>
@@ -22,6 +24,8 @@
 #include "tracking/ICPTracker.h"
 #undef private
 
+#include "export/GLBExporter.h"
+#include "export/PLYExporter.h"
 #include "meshing/MarchingCubes.h"
 #include "sensor/FrameData.h"
 #include "sensor/KinectSensor.h"
@@ -330,6 +334,60 @@ void ref_conditioner_process(void* h, uint16_t* depth, uint8_t* rgb, float min_d
     c->process(raw, nullptr, min_depth, max_depth);
     std::memcpy(depth, raw.depth.data(), n * sizeof(uint16_t));
     std::memcpy(rgb, raw.rgb.data(), n * 3);
+}
+
+// ---- export ------------------------------------------------------------------
+static meshing::MeshData mesh_of(const float* pos, const float* nrm, const uint8_t* col, int64_t nv,
+                                 const uint32_t* idx, int64_t ni) {
+    meshing::MeshData m;
+    m.positions.resize(static_cast<size_t>(nv));
+    for (int64_t i = 0; i < nv; ++i) m.positions[i] = Eigen::Vector3f(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    if (nrm) {
+        m.normals.resize(static_cast<size_t>(nv));
+        for (int64_t i = 0; i < nv; ++i) m.normals[i] = Eigen::Vector3f(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+    }
+    if (col) m.colors.assign(col, col + 3 * nv);
+    m.indices.assign(idx, idx + ni);
+    return m;
+}
+
+// PLYExporter::writeBinary (binary != 0) or writeASCII; GLBExporter::write.
+// Normals or colours may be NULL. Returns the writer's success flag.
+int ref_export_ply(const float* pos, const float* nrm, const uint8_t* col, int64_t nv, const uint32_t* idx,
+                   int64_t ni, const char* path, int binary) {
+    const meshing::MeshData m = mesh_of(pos, nrm, col, nv, idx, ni);
+    return binary ? export_io::PLYExporter::writeBinary(m, path) : export_io::PLYExporter::writeASCII(m, path);
+}
+
+int ref_export_glb(const float* pos, const float* nrm, const uint8_t* col, int64_t nv, const uint32_t* idx,
+                   int64_t ni, const char* path) {
+    return export_io::GLBExporter::write(mesh_of(pos, nrm, col, nv, idx, ni), path);
+}
+
+// ---- sensor pairing ------------------------------------------------------------
+// Feeds depth (kind 0) and RGB (kind 1) samples with their 60 MHz tick stamps,
+// in order, through KinectSensor's pairing path. Per published frame writes
+// the depth ticks and the paired RGB ticks (-1: published depth-only).
+// Returns the number of frames published (at most cap are written).
+int ref_sensor_pairing(const int* kinds, const uint32_t* ticks, int n, int64_t* depth_ticks, int64_t* rgb_ticks,
+                       int cap) {
+    static std::vector<uint16_t> depth(static_cast<size_t>(sensor::DEPTH_WIDTH) * sensor::DEPTH_HEIGHT, 0);
+    static std::vector<uint8_t> rgb(static_cast<size_t>(sensor::RGB_WIDTH) * sensor::RGB_HEIGHT * 3, 0);
+    sensor::KinectSensor s;
+    std::vector<std::pair<int64_t, int64_t>> got;
+    s.setFrameCallback([&got](std::shared_ptr<sensor::RawFrame> f) {
+        got.emplace_back(f->depth_ticks, f->rgb_valid ? static_cast<int64_t>(f->rgb_ticks) : -1);
+    });
+    for (int i = 0; i < n; ++i) {
+        if (kinds[i] == 0) s.injectDepthForTests(depth.data(), ticks[i]);
+        else s.injectRgbForTests(rgb.data(), ticks[i]);
+    }
+    s.setFrameCallback(nullptr);
+    for (size_t k = 0; k < got.size() && static_cast<int>(k) < cap; ++k) {
+        depth_ticks[k] = got[k].first;
+        rgb_ticks[k] = got[k].second;
+    }
+    return static_cast<int>(got.size());
 }
 
 void ref_set_threads(int n) {

@@ -240,3 +240,47 @@ class Conditioner:
             self.close()
         except Exception:
             pass
+
+
+def _mesh_args(positions, indices, normals, colors):
+    pos = np.ascontiguousarray(positions, np.float32)
+    idx = np.ascontiguousarray(indices, np.uint32)
+    nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+    col = None if colors is None else np.ascontiguousarray(colors, np.uint8)
+    keep = (pos, idx, nrm, col)
+    args = [_p(pos), None if nrm is None else _p(nrm), None if col is None else col.ctypes.data_as(C.c_void_p),
+            C.c_int64(len(pos)), idx.ctypes.data_as(C.c_void_p), C.c_int64(len(idx))]
+    return keep, args
+
+
+def export_ply(path, positions, indices, normals=None, colors=None, binary=True) -> bool:
+    """PLYExporter::writeBinary / writeASCII of the reference."""
+    keep, args = _mesh_args(positions, indices, normals, colors)
+    f = lib().ref_export_ply
+    f.restype = C.c_int
+    return bool(f(*args, str(path).encode(), int(binary)))
+
+
+def export_glb(path, positions, indices, normals=None, colors=None) -> bool:
+    """GLBExporter::write of the reference."""
+    keep, args = _mesh_args(positions, indices, normals, colors)
+    f = lib().ref_export_glb
+    f.restype = C.c_int
+    return bool(f(*args, str(path).encode()))
+
+
+def sensor_pairing(events):
+    """KinectSensor's depth-led pairing of (kind, ticks) samples, kind 'd' or
+    'r' (other kinds are skipped). Returns [(depth ticks, rgb ticks or None)]
+    in publication order."""
+    ev = [(0 if k == "d" else 1, int(t) % (1 << 32)) for k, t in events if k in ("d", "r")]
+    kinds = np.array([e[0] for e in ev], np.int32)
+    ticks = np.array([e[1] for e in ev], np.uint32)
+    cap = max(1, len(ev))
+    d = np.zeros(cap, np.int64)
+    r = np.zeros(cap, np.int64)
+    f = lib().ref_sensor_pairing
+    f.restype = C.c_int
+    n = f(kinds.ctypes.data_as(C.c_void_p), ticks.ctypes.data_as(C.c_void_p), len(ev), d.ctypes.data_as(C.c_void_p),
+          r.ctypes.data_as(C.c_void_p), cap)
+    return [(int(d[k]), None if r[k] < 0 else int(r[k])) for k in range(min(n, cap))]

@@ -326,3 +326,60 @@ def reflection_fixture():
 ICP_TOL_MATCH = 1e-7     # the contract's kTolMatch
 ICP_HUBER_K = 0.02
 ICP_ROW_VY = (450.0 - CY) * 2.0 / FY
+
+
+# ---- export and sensor-pairing fixtures (pinned to the reference's own writers
+# and KinectSensor pairing by tests/golden/make_golden.py) ------------------------
+def export_meshes(orc):
+    """Meshes for the PLY/GLB writers: the oracle's sphere mesh with normals and
+    colours; the same positions and indices alone; and an unwelded copy
+    (every vertex twice) with a zero normal, a -0 coordinate and a saturated
+    colour, which exercises the GLB writer's welding and normal fallback."""
+    t, w, prm = sphere_volume()
+    o = orc.Volume(orc.tsdf_params(**prm))
+    o.tsdf[:] = t
+    o.weight[:] = w
+    m = o.extract_mesh()
+    full = dict(positions=m["positions"], normals=m["normals"], colors=m["colors"], indices=m["indices"])
+    bare = dict(positions=m["positions"], normals=None, colors=None, indices=m["indices"])
+    n = len(m["positions"])
+    pos = np.concatenate([m["positions"], m["positions"]]).astype(np.float32)
+    nrm = np.concatenate([m["normals"], m["normals"]]).astype(np.float32)
+    col = np.concatenate([m["colors"], m["colors"]]).astype(np.uint8)
+    idx = np.concatenate([m["indices"], m["indices"] + n]).astype(np.uint32)
+    col[0] = (0, 10, 255)
+    nrm[int(idx[5])] = 0.0
+    pos[int(idx[7]), 1] = -0.0
+    dup = dict(positions=pos, normals=nrm, colors=col, indices=idx)
+    return {"sphere": full, "sphere_bare": bare, "sphere_unwelded": dup}
+
+
+PAIR_MS = 60000  # 60 MHz device ticks per millisecond (KinectSensor.h:85)
+
+
+def pairing_events(name):
+    """(kind, 60 MHz ticks) sample sequences for the depth-led pairing:
+    'hand'     the hand-derived sequence of tests/test_ingest.py (skew limit
+               edges, a late RGB, RGB ahead of depth, a counter wrap)
+    'jitter'   depth and RGB samples at 30 Hz with seeded phase jitter,
+               dropped samples and reordering across streams, through a wrap
+               of the 32-bit counter"""
+    ms = PAIR_MS
+    if name == "hand":
+        wrap_r = (1 << 32) - 3 * ms
+        ev = [("r", 0.0), ("d", 5.0), ("d", 38.0), ("r", 40.0), ("r", 60.0), ("d", 100.0), ("d", 133.0),
+              ("r", 140.0), ("r", 200.0), ("d", 170.0), ("d", 205.0), ("d", 300.0), ("r", wrap_r),
+              ("d", 2 * ms)]
+        return [(k, int(t * ms) % (1 << 32) if isinstance(t, float) else int(t) % (1 << 32)) for k, t in ev]
+    rng = np.random.default_rng(77)
+    t0 = (1 << 32) - 60 * 33 * ms  # the counter wraps about 60 frames in
+    ev = []
+    for i in range(150):
+        td = t0 + int((33.37 * i + rng.normal(0, 1.5)) * ms)
+        tr = t0 + int((33.37 * i + 9.0 + rng.normal(0, 6.0)) * ms)
+        if rng.random() > 0.06:
+            ev.append(("d", td % (1 << 32), td))
+        if rng.random() > 0.1:
+            ev.append(("r", tr % (1 << 32), tr + int(rng.normal(0, 4.0) * ms)))  # delivered out of order
+    ev.sort(key=lambda e: e[2])
+    return [(k, t) for k, t, _ in ev]

@@ -16,6 +16,12 @@ It drives the same scenario code the tests use, through recording backends:
   mesh/<fixture>/...    MarchingCubes::extract of every fixture volume of
                         tests/mesh_fixtures.py (positions, normals, colours,
                         indices, truncated)
+  export/<mesh>/...     PLYExporter::writeBinary / writeASCII (sha256 and size
+                        of the file) and GLBExporter::write (the JSON chunk,
+                        the BIN chunk's sha256, the file size) of the
+                        tests/fixtures.py export meshes
+  pairing/<seq>/...     KinectSensor's depth-led pairing of the tests/fixtures.py
+                        sample sequences (depth ticks, RGB ticks or -1)
 
 Run: python tests/golden/make_golden.py   (from the repository root)
 """
@@ -177,6 +183,36 @@ def record_meshes(store):
         store[f"mesh/{name}/truncated"] = np.array(m["truncated"])
 
 
+def _sha_file(path):
+    return hashlib.sha256(open(path, "rb").read()).hexdigest()
+
+
+def record_exports(store):
+    import struct
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        for name, m in F.export_meshes(O).items():
+            for binary, tag in ((True, "ply_binary"), (False, "ply_ascii")):
+                p = os.path.join(d, f"{name}.{tag}.ply")
+                assert R.export_ply(p, m["positions"], m["indices"], m["normals"], m["colors"], binary)
+                store[f"export/{name}/{tag}"] = np.array([_sha_file(p), str(os.path.getsize(p))])
+            p = os.path.join(d, f"{name}.glb")
+            assert R.export_glb(p, m["positions"], m["indices"], m["normals"], m["colors"])
+            data = open(p, "rb").read()
+            jlen = struct.unpack_from("<I", data, 12)[0]
+            blen = struct.unpack_from("<I", data, 20 + jlen)[0]
+            store[f"export/{name}/glb"] = np.array([str(len(data)),
+                                                    hashlib.sha256(data[28 + jlen:28 + jlen + blen]).hexdigest()])
+            store[f"export/{name}/glb_json"] = np.frombuffer(data[20:20 + jlen], np.uint8)
+
+
+def record_pairing(store):
+    for name in ("hand", "jitter"):
+        pairs = R.sensor_pairing(F.pairing_events(name))
+        store[f"pairing/{name}/depth"] = np.array([d for d, _ in pairs], np.int64)
+        store[f"pairing/{name}/rgb"] = np.array([-1 if r is None else r for _, r in pairs], np.int64)
+
+
 def main():
     if not R.available():
         raise SystemExit("the reference build is not available (oracle/_ref needs the reference checkout)")
@@ -186,6 +222,8 @@ def main():
     record_tsdf(store)
     record_scene(store)
     record_meshes(store)
+    record_exports(store)
+    record_pairing(store)
     np.savez_compressed(OUT, **store)
     print(f"wrote {OUT}: {len(store)} arrays, {os.path.getsize(OUT) / 1e3:.0f} kB")
 

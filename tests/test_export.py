@@ -1,7 +1,12 @@
-"""Mesh export (PLY binary/ASCII and GLB) from the CUDA library's host code
-against a plain restatement of the reference's writers: PLY byte for byte,
-GLB's binary chunk byte for byte and its glTF JSON by content; invalid meshes
-create no file. CPU only."""
+"""Mesh export (PLY binary/ASCII and GLB) from the CUDA library's host code.
+
+  reference   the files the reference's own PLYExporter / GLBExporter write
+              for the tests/fixtures.py export meshes (tests/golden, made by
+              tests/golden/make_golden.py): every file byte for byte
+  restatement a plain restatement of the writers (oracle/export_ref.py): PLY
+              byte for byte, GLB's binary chunk byte for byte and its glTF
+              JSON by content
+  invalid meshes create no file. CPU only."""
 import json
 
 import numpy as np
@@ -70,7 +75,8 @@ def test_glb_chunks(orc, tmp_path):
     assert acc[prim["indices"]]["count"] == len(idx)
     pg = np.asarray(pos, np.float32) * np.array([1, -1, -1], np.float32)
     assert acc[prim["attributes"]["POSITION"]]["min"] == [float(v) for v in pg.min(0)]
-    assert doc["materials"][0]["pbrMetallicRoughness"]["baseColorFactor"] == [1.0, 1.0, 1.0, 1.0]
+    # a white base colour is the glTF default, left out as the reference leaves it out
+    assert "baseColorFactor" not in doc["materials"][0]["pbrMetallicRoughness"]
     assert doc["buffers"][0]["byteLength"] == len(b)
 
 
@@ -89,3 +95,33 @@ def test_invalid_mesh_creates_no_file(orc, tmp_path):
             with pytest.raises(_abi.AzuError):
                 fn(p)
             assert not p.exists()
+
+
+@pytest.mark.parametrize("name", ["sphere", "sphere_bare", "sphere_unwelded"])
+def test_files_equal_the_reference_writers(orc, tmp_path, name):
+    """PLYExporter::writeBinary / writeASCII and GLBExporter::write of the
+    reference (src/export/PLYExporter.cpp, GLBExporter.cpp) wrote these files
+    for the same meshes: ours are the same bytes."""
+    _lib_ready()
+    import hashlib
+    import struct
+    from golden_check import golden
+    from azu_gb300 import api
+    g = golden()
+    m = F.export_meshes(orc)[name]
+    md = {k: v for k, v in m.items() if v is not None}
+    for binary, tag in ((True, "ply_binary"), (False, "ply_ascii")):
+        p = tmp_path / f"{tag}.ply"
+        api.write_ply(p, md, binary)
+        data = p.read_bytes()
+        sha, size = g[f"export/{name}/{tag}"]
+        assert len(data) == int(size) and hashlib.sha256(data).hexdigest() == sha, tag
+    p = tmp_path / "m.glb"
+    api.write_glb(p, md)
+    data = p.read_bytes()
+    size, bin_sha = g[f"export/{name}/glb"]
+    jlen = struct.unpack_from("<I", data, 12)[0]
+    blen = struct.unpack_from("<I", data, 20 + jlen)[0]
+    assert data[20:20 + jlen] == g[f"export/{name}/glb_json"].tobytes()
+    assert hashlib.sha256(data[28 + jlen:28 + jlen + blen]).hexdigest() == bin_sha
+    assert len(data) == int(size)

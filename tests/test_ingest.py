@@ -69,6 +69,29 @@ def test_pairing_follows_the_sensor_rules(tmp_path):
     rec.close()
 
 
+@pytest.mark.parametrize("name", ["hand", "jitter"])
+def test_pairing_equals_the_reference_sensor(tmp_path, name):
+    """The same depth / RGB samples fed to the reference's KinectSensor
+    (onDepth / onRgb through its test seam, src/sensor/KinectSensor.cpp)
+    published these frames (tests/golden, made by
+    tests/golden/make_golden.py): the recording pairs them identically, in
+    the same order."""
+    _lib_ready()
+    import fixtures as F
+    from golden_check import golden
+    from azu_gb300 import api
+    g = golden()
+    events = F.pairing_events(name)
+    _recording(str(tmp_path), events)
+    rec = api.Recording(tmp_path)
+    want_d, want_r = g[f"pairing/{name}/depth"], g[f"pairing/{name}/rgb"]
+    got = [rec.info(k) for k in range(len(rec))]
+    rec.close()
+    assert len(got) == len(want_d)
+    for k, (d, r) in enumerate(got):
+        assert d == want_d[k] and (-1 if r is None else r) == want_r[k], k
+
+
 def test_missing_index_is_an_error(tmp_path):
     _lib_ready()
     from azu_gb300 import api, _abi

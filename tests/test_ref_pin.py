@@ -170,3 +170,79 @@ def test_preprocessor_chain(orc, c1):
         do, co, _ = op.process(raw, rgb, s.min_depth, s.max_depth)
         assert np.array_equal(dr.reshape(480, 640), do), k
         assert np.array_equal(cr.reshape(480, 640, 3), co), k
+
+
+def _random_mesh(rng, scale):
+    nv = int(rng.integers(3, 400))
+    pos = (rng.standard_normal((nv, 3)) * scale).astype(np.float32)
+    nrm = rng.standard_normal((nv, 3)).astype(np.float32)
+    nrm[rng.random(nv) < 0.05] = 0.0
+    col = rng.integers(0, 256, (nv, 3), dtype=np.uint8)
+    idx = rng.integers(0, nv, 3 * int(rng.integers(1, 300))).astype(np.uint32)
+    pos[rng.random((nv, 3)) < 0.02] = -0.0
+    dup = rng.random(nv) < 0.2  # repeated positions, welded by the GLB writer
+    pos[dup] = pos[0]
+    return pos, nrm, col, idx
+
+
+def test_mesh_files_equal_reference_writers(tmp_path):
+    """Our PLY and GLB writers against the reference's PLYExporter and
+    GLBExporter on 60 seeded random meshes (metre to kilometre scales,
+    welded duplicates, zero normals, -0 coordinates, with and without normals
+    and colours): PLY byte for byte; GLB's binary chunk byte for byte and its
+    glTF JSON equal value for value (its numbers are the same doubles; the
+    reference's JSON library may print a tie's last digit differently)."""
+    import json
+    import struct
+    from azu_gb300 import api
+    rng = np.random.default_rng(11)
+    for k in range(60):
+        pos, nrm, col, idx = _random_mesh(rng, 10.0 ** rng.uniform(-3, 3))
+        with_n, with_c = k % 3 != 1, k % 3 != 2
+        n, c = (nrm if with_n else None), (col if with_c else None)
+        md = dict(positions=pos, indices=idx)
+        if with_n:
+            md["normals"] = nrm
+        if with_c:
+            md["colors"] = col
+        for binary in (True, False):
+            a, b = tmp_path / "a.ply", tmp_path / "b.ply"
+            api.write_ply(a, md, binary)
+            assert R.export_ply(b, pos, idx, n, c, binary)
+            assert a.read_bytes() == b.read_bytes(), (k, binary)
+        a, b = tmp_path / "a.glb", tmp_path / "b.glb"
+        api.write_glb(a, md)
+        assert R.export_glb(b, pos, idx, n, c)
+        da, db = a.read_bytes(), b.read_bytes()
+        ja, jb = struct.unpack_from("<I", da, 12)[0], struct.unpack_from("<I", db, 12)[0]
+        assert json.loads(da[20:20 + ja]) == json.loads(db[20:20 + jb]), k
+        assert da[20 + ja:] == db[20 + jb:], k
+
+
+def test_pairing_equals_reference_sensor(tmp_path):
+    """The recording's pairing (azu_gb300/csrc/ingest.cu) against the
+    reference's KinectSensor fed the same samples, on 20 seeded sequences with
+    jitter, drops, reordering across the two streams and counter wraps."""
+    from azu_gb300 import api
+    import test_ingest as TI
+    rng = np.random.default_rng(5)
+    ms = 60000
+    for k in range(20):
+        t = int(rng.integers(0, 1 << 32))
+        ev = []
+        for i in range(int(rng.integers(5, 40))):
+            td = t + int((33.37 * i + rng.normal(0, 3.0)) * ms)
+            tr = t + int((33.37 * i + rng.uniform(-25, 25)) * ms)
+            if rng.random() > 0.15:
+                ev.append(("d", td % (1 << 32), td))
+            if rng.random() > 0.2:
+                ev.append(("r", tr % (1 << 32), tr + int(rng.normal(0, 8.0) * ms)))
+        ev.sort(key=lambda e: e[2])
+        events = [(kind, tk) for kind, tk, _ in ev]
+        d = tmp_path / f"rec{k}"
+        d.mkdir()
+        TI._recording(str(d), events)
+        rec = api.Recording(d)
+        got = [rec.info(i) for i in range(len(rec))]
+        rec.close()
+        assert got == R.sensor_pairing(events), k
