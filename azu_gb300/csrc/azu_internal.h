@@ -69,6 +69,9 @@ struct IntegrateConsts {
     // line; cull_off = trunc + cull_eps + slack; voxels nearer than z_safe are
     // never culled
     float cull_eps, cull_off, z_safe;
+    // brick pre-cull: a stepped coordinate lies within brick_eps of the exact
+    // affine one anywhere on its row; brick_off = trunc + brick_eps + slack
+    float brick_eps, brick_off;
 };
 
 // Tile-max pyramid over the depth image: level l tiles are 8 * 2^l pixels
@@ -98,7 +101,11 @@ struct azu_volume {
     unsigned long long* d_counters = nullptr;  // [0] newly observed (cumulative), [1] updated (last), [2] colour (last),
                                                // [3] updated (cumulative), [4] integrate work counter
     int int_blocks = 0;                        // resident blocks of the persistent integrate kernel
-    const void* int_kernel = nullptr;          // the kernel variant int_blocks was sized for
+    // One bit per 8^3 brick that the frame being integrated may update, rows
+    // of nb bricks along x in 32-bit words (int_live_words per row), rows in
+    // (z, y) order: written by the brick pre-cull before every integration.
+    uint32_t* int_live = nullptr;
+    int int_live_words = 0;
     float* d_depth_stage = nullptr;            // host-depth staging (integrate_host)
     uint8_t* d_rgb_stage = nullptr;
     size_t stage_pixels = 0;

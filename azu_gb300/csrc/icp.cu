@@ -73,7 +73,6 @@ struct IcpArgs {
     int vblocks;          // partial slots: the pixel split and summation order (>= the launch's blocks)
     unsigned* bar;        // [0] arrivals, [1] generation
     unsigned* err;
-    unsigned* state;      // iteration outcome published by the last-arriving block
     float* build_out;     // build mode: A[36], b[6], residual, counts[6] (as int bits)
 };
 
@@ -119,55 +118,6 @@ __device__ void grid_sync(unsigned* bar, unsigned* err, WaitLimits wl, unsigned&
                     __nanosleep(64);
                 }
             }
-        }
-        gen += 1;
-        __threadfence();
-    }
-    __syncthreads();
-}
-
-// Split barrier: every block arrives; the one that arrives last reduces and
-// solves, publishes the outcome and releases the others (one reduction and
-// one solve per iteration instead of one per block). Waits are bounded like
-// grid_sync; with the error word set nobody waits and every block proceeds
-// on its own (the result is then reported as a timeout).
-// The last block resets the arrival count at once: no block arrives again
-// before release_all, which it reaches after this reset.
-__device__ bool arrive_last(unsigned* bar, unsigned* err, WaitLimits wl, int* s_flag) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int last = 1;
-        if (ld_acquire(err) == 0) {
-            __threadfence();
-            last = (atomicAdd(&bar[0], 1u) == wl.arrivals - 1) ? 1 : 0;
-            if (last) atomicExch(&bar[0], 0u);
-            __threadfence();
-        }
-        *s_flag = last;
-    }
-    __syncthreads();
-    return *s_flag != 0;
-}
-
-// Callers fence their published writes before it.
-__device__ void release_all(unsigned* bar, unsigned* err, unsigned& gen) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        if (ld_acquire(err) == 0) atomicAdd(&bar[1], 1u);
-        gen += 1;
-    }
-    __syncthreads();
-}
-
-__device__ void wait_release(unsigned* bar, unsigned* err, WaitLimits wl, unsigned& gen) {
-    if (threadIdx.x == 0) {
-        unsigned spins = 0;
-        while (ld_acquire(err) == 0 && ld_acquire(&bar[1]) == gen) {
-            if (++spins > wl.spins) {
-                atomicExch(err, kDevErrBarrierTimeout);
-                break;
-            }
-            __nanosleep(32);
         }
         gen += 1;
         __threadfence();
@@ -1020,7 +970,6 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
     __shared__ float s_start[16];
     __shared__ azu_icp_result s_res;
     __shared__ int s_retry;
-    __shared__ int s_last;
     __shared__ WaitLimits s_wl;
 
     if (threadIdx.x == 0) {
@@ -1096,25 +1045,15 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
                 __syncthreads();
                 const Rel rel = s_rel;
                 associate_all(a, rel, L, n, slot, s_red, gb, gn);
-                constexpr int kWords = static_cast<int>(sizeof(LevelState) / 4);
-                unsigned* st_words = reinterpret_cast<unsigned*>(&st);
-                if (arrive_last(a.bar, a.err, wl, &s_last)) {
-                    reduce_grid(a, slot, sm.sum, sm.isum);
-                    if (threadIdx.x < 32) solve_step(a, level, sm, st);
-                    __syncthreads();
-                    for (int i = threadIdx.x; i <= kWords; i += blockDim.x)
-                        __stcg(a.state + i, i < kWords ? st_words[i] : static_cast<unsigned>(sm.action));
-                    __threadfence();
-                    release_all(a.bar, a.err, gen);
-                } else {
-                    wait_release(a.bar, a.err, wl, gen);
-                    for (int i = threadIdx.x; i <= kWords; i += blockDim.x) {
-                        const unsigned w = __ldcg(a.state + i);
-                        if (i < kWords) st_words[i] = w;
-                        else sm.action = static_cast<int>(w);
-                    }
-                    __syncthreads();
-                }
+                // Every block reduces the partials and solves on its own: the
+                // same loads in the same order and the same code give every
+                // block the same bits, so no block waits for another's result
+                // after the barrier (the partial slots alternate, so the next
+                // iteration's partials never overwrite ones still being read).
+                grid_sync(a.bar, a.err, wl, gen);
+                reduce_grid(a, slot, sm.sum, sm.isum);
+                if (threadIdx.x < 32) solve_step(a, level, sm, st);
+                __syncthreads();
                 slot ^= 1;
                 if (sm.action != 0) break;
             }
@@ -1267,7 +1206,6 @@ static void fill_args_p(azu_tracker* t, const azu_tracker_params& p, IcpArgs& a,
     a.vblocks = t->nblocks;
     a.bar = t->bar;
     a.err = t->bar + 2;
-    a.state = t->bar + 4;
 }
 
 int icp_launch(azu_tracker* t, const IcpArgs& a, cudaStream_t s) {
@@ -1408,7 +1346,7 @@ extern "C" int azu_tracker_create(int device, const azu_tracker_params* p, void*
         t->nblocks = std::min(sms * std::min(occ, 2), kMaxGridBlocks);
         cudaError_t e = cudaMalloc(&t->partials, sizeof(double) * 2 * t->nblocks * kNF);
         if (e == cudaSuccess) e = cudaMalloc(&t->ipartials, sizeof(int) * 2 * t->nblocks * kNI);
-        if (e == cudaSuccess) e = cudaMalloc(&t->bar, sizeof(unsigned) * (4 + sizeof(LevelState) / 4 + 1));
+        if (e == cudaSuccess) e = cudaMalloc(&t->bar, sizeof(unsigned) * 4);
         if (e == cudaSuccess) e = cudaMemset(t->bar, 0, sizeof(unsigned) * 4);
         if (e == cudaSuccess) e = cudaMalloc(&t->d_est, sizeof(float) * 48);
         if (e == cudaSuccess) e = cudaMalloc(&t->d_result, sizeof(azu_icp_result));
@@ -1507,7 +1445,7 @@ extern "C" int azu_tracker_track_many(azu_tracker* t, int width, int height, con
     // sits first so that its barrier words keep their place between calls.
     auto up = [](size_t x) { return (x + 255) & ~static_cast<size_t>(255); };
     const size_t nb = static_cast<size_t>(t->nblocks);
-    constexpr size_t kBarWords = 4 + sizeof(LevelState) / 4 + 1;
+    constexpr size_t kBarWords = 4;
     const size_t sz_p = up(sizeof(double) * 2 * kNF * nb), sz_i = up(sizeof(int) * 2 * kNI * nb);
     const size_t sz_b = up(sizeof(unsigned) * kBarWords), per = sz_p + sz_i + sz_b;
     if (static_cast<size_t>(count) > t->many_cap) {
@@ -1556,7 +1494,6 @@ extern "C" int azu_tracker_track_many(azu_tracker* t, int width, int height, con
             a.ipartials = reinterpret_cast<int*>(base + per * k + sz_p);
             a.bar = bar_of(k);
             a.err = a.bar + 2;
-            a.state = a.bar + 4;
             args[k] = a;
             first[k + 1] = first[k] + grid / count;
         } else if (int rc = icp_launch(t, a, s)) {
@@ -1789,7 +1726,6 @@ extern "C" int azu_icp_build_system_noalloc(const float* d_live_vertices, const 
     a.vblocks = slot.nblocks;
     a.bar = d_bar;
     a.err = d_bar + 2;
-    a.state = nullptr;  // build mode publishes no iteration state
     a.build_out = d_out;
 
     cudaLaunchConfig_t cfg = {};

@@ -208,6 +208,13 @@ __device__ __forceinline__ void integrate_setup_body(const float* __restrict__ d
         const float uny = (fmaxf(fabsf(cy), fabsf(float(H) - cy)) + 3.0f) / fy;
         ic.cull_eps = eps;
         ic.cull_off = trunc + eps + 1e-5f;
+        // A row's stepped coordinate after k steps differs from the exact
+        // affine value by at most k rounding errors of ulp(cmax) / 2 each, the
+        // rounding of the step itself k times, and a few ulps of the start
+        // (and of the brick corners computed here): (res + 64) ulps, times 1.5.
+        const float eps_b = 1.5f * static_cast<float>(res + 64) * 2.0f * cmax * 1.1920929e-7f;
+        ic.brick_eps = eps_b;
+        ic.brick_off = trunc + eps_b + 1e-5f;
         ic.z_safe = fmaxf(1e-3f, 2.0f * eps * (fmaxf(fx * (1.0f + unx), fy * (1.0f + uny)) + 2.0f));
         if (!(isfinite(ic.cull_off) && isfinite(ic.z_safe))) ic.z_safe = __int_as_float(0x7f800000);
         *out = ic;
@@ -223,6 +230,102 @@ __global__ void integrate_setup_kernel(const float* __restrict__ d_pose, int res
                                        float* __restrict__ tiles, TileMip mip, int pyramid) {
     integrate_setup_body(d_pose, res, vs, ox, oy, oz, trunc, fx, fy, cx, cy, W, H, max_d, out, counters, tiles, mip,
                          pyramid != 0);
+}
+
+// Brick pre-cull: one bit per 8^3 brick, set unless no voxel of the brick can
+// take an update this frame. Every voxel's stepped camera coordinate lies
+// within brick_eps of the parallelepiped spanned by the brick's corner
+// voxels, so with every corner at least z_near in front of the camera, each
+// voxel projects inside the corners' pixel box widened by the rounding
+// margins of the exact projection (-2 / +3 pixels, as the chunk cull) and by
+// brick_eps times the projection's slope; its depth there is at most the
+// deepest in-band depth of the tiles under the box, and a voxel farther
+// than that plus trunc gets sdf < -trunc. A brick with every corner at or
+// behind the camera plane (c.z <= 0 for all its voxels) or whose box misses
+// the image takes no update either. Everything else is kept (conservative).
+// One warp per 32 consecutive bricks of a row, written with one ballot.
+constexpr float kBrickNear = 1e-2f;  // corners nearer than this: no projection bound
+constexpr int kBrickFine = 8;        // level-0 tiles a side read one by one before a coarser level is used
+__global__ void __launch_bounds__(256) integrate_bricks_kernel(
+    const IntegrateConsts* __restrict__ icp, int res, int nb, int words, float vs, float ox, float oy, float oz,
+    float fx, float fy, float cx, float cy, int W, int H, const float* __restrict__ tiles, TileMip mip,
+    const int* __restrict__ gate, uint32_t* __restrict__ live) {
+    if (gate && __ldg(gate) == 0) return;
+    const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int row = gw / words, word = gw - row * words;
+    if (row >= nb * nb) return;
+    const int bz = row / nb, by = row - bz * nb, bx = word * 32 + lane;
+    bool on = false;
+    if (__ldg(&icp->valid) && bx < nb) {
+        const int xa = bx << kBrickShift, ya = by << kBrickShift, za = bz << kBrickShift;
+        const int xb = min(xa + 7, res - 1), yb = min(ya + 7, res - 1), zb = min(za + 7, res - 1);
+        on = !(xb < __ldg(&icp->x0) || xa > __ldg(&icp->x1) || yb < __ldg(&icp->y0) || ya > __ldg(&icp->y1) ||
+               zb < __ldg(&icp->z0) || za > __ldg(&icp->z1));
+        if (on) {
+            float R[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) R[i] = __ldg(&icp->R_wc[i]);
+            const float tx = __ldg(&icp->t_wc[0]), ty = __ldg(&icp->t_wc[1]), tz = __ldg(&icp->t_wc[2]);
+            const float eps = __ldg(&icp->brick_eps);
+            float zlo = __int_as_float(0x7f800000), zhi = -zlo, ulo = zlo, uhi = -zlo, vlo = zlo, vhi = -zlo;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const float px = ox + vs * static_cast<float>((k & 1) ? xb : xa);
+                const float py = oy + vs * static_cast<float>((k & 2) ? yb : ya);
+                const float pz = oz + vs * static_cast<float>((k & 4) ? zb : za);
+                const float c0 = fmaf(R[0], px, fmaf(R[1], py, fmaf(R[2], pz, tx)));
+                const float c1 = fmaf(R[3], px, fmaf(R[4], py, fmaf(R[5], pz, ty)));
+                const float c2 = fmaf(R[6], px, fmaf(R[7], py, fmaf(R[8], pz, tz)));
+                zlo = fminf(zlo, c2);
+                zhi = fmaxf(zhi, c2);
+                const float iz = 1.0f / c2;
+                const float u = fmaf(fx * c0, iz, cx), v = fmaf(fy * c1, iz, cy);
+                ulo = fminf(ulo, u);
+                uhi = fmaxf(uhi, u);
+                vlo = fminf(vlo, v);
+                vhi = fmaxf(vhi, v);
+            }
+            zlo -= eps;
+            zhi += eps;
+            if (zhi <= 0.0f) {
+                on = false;  // every voxel has c.z <= 0
+            } else if (zlo >= kBrickNear) {
+                // the projection moves by at most eps (f + |u - c|) / z for a move of eps
+                const float du = eps * (fx + fmaxf(fabsf(ulo - cx), fabsf(uhi - cx))) / zlo + 1e-3f;
+                const float dv = eps * (fy + fmaxf(fabsf(vlo - cy), fabsf(vhi - cy))) / zlo + 1e-3f;
+                const float fW = static_cast<float>(W), fH = static_cast<float>(H);
+                ulo -= 2.0f + du;
+                uhi += 3.0f + du;
+                vlo -= 2.0f + dv;
+                vhi += 3.0f + dv;
+                if (!(uhi >= 0.0f && ulo < fW && vhi >= 0.0f && vlo < fH)) {
+                    on = false;  // the box misses the image (NaN bounds fail the other tests and keep the brick)
+                } else if (isfinite(ulo) && isfinite(uhi) && isfinite(vlo) && isfinite(vhi)) {
+                    const int tu0 = static_cast<int>(fmaxf(ulo, 0.0f)) >> kTileShift;
+                    const int tu1 = static_cast<int>(fminf(uhi, fW - 1.0f)) >> kTileShift;
+                    const int tv0 = static_cast<int>(fmaxf(vlo, 0.0f)) >> kTileShift;
+                    const int tv1 = static_cast<int>(fminf(vhi, fH - 1.0f)) >> kTileShift;
+                    float tm = -__int_as_float(0x7f800000);
+                    if (tu1 - tu0 < kBrickFine && tv1 - tv0 < kBrickFine) {
+                        const int w0 = mip.w[0];
+                        for (int a = tv0; a <= tv1; ++a)
+                            for (int b = tu0; b <= tu1; ++b) tm = fmaxf(tm, __ldg(tiles + a * w0 + b));
+                    } else {
+                        const int ext = max(tu1 - tu0, tv1 - tv0);
+                        const int l = min(32 - __clz(ext), mip.levels - 1);
+                        const int w = mip.w[l];
+                        const float* tl = tiles + mip.off[l];
+                        const int a0 = (tv0 >> l) * w, a1 = (tv1 >> l) * w, b0 = tu0 >> l, b1 = tu1 >> l;
+                        tm = fmaxf(fmaxf(__ldg(tl + a0 + b0), __ldg(tl + a0 + b1)),
+                                   fmaxf(__ldg(tl + a1 + b0), __ldg(tl + a1 + b1)));
+                    }
+                    on = !(zlo > tm + __ldg(&icp->brick_off));
+                }
+            }
+        }
+    }
+    const unsigned bits = __ballot_sync(0xffffffffu, on);
+    if (lane == 0) live[static_cast<size_t>(row) * words + word] = bits;
 }
 
 // fs_walk kept out of line (it runs once per item, not per voxel).
@@ -255,7 +358,7 @@ __device__ __forceinline__ void integrate_item(
     float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
     float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb,
     const float* __restrict__ tiles, const TileMip& mip, int item, int warp, int lane, float (*s_c)[3][32][33],
-    int nparts = 1) {
+    int nparts = 1, const uint32_t* __restrict__ live = nullptr, int live_words = 0) {
     if (gate && __ldg(gate) == 0) return;
     if (!__ldg(&icp->valid)) return;
     const int ngroups = (res + 31) >> 5;
@@ -268,6 +371,32 @@ __device__ __forceinline__ void integrate_item(
     const int ybase = (item - z * ngroups) << 5;
     const int z0 = __ldg(&icp->z0), z1 = __ldg(&icp->z1), y0 = __ldg(&icp->y0), y1 = __ldg(&icp->y1);
     if (z < z0 || z > z1 || ybase + 31 < y0 || ybase > y1) return;
+    const int y = ybase + lane;
+    const bool row_on = (y >= y0 && y <= y1);
+    // Chunks of this part (chunk j: x in [xpart + 32 j, +32)) that the brick
+    // pre-cull keeps for this row: one of the chunk's 4 bricks is kept. The
+    // item ends here when no row has one.
+    const int xpart = part * span;
+    const int nch = (min(span, res - xpart) + 31) >> 5;
+    if (nch <= 0) return;
+    const int b0 = xpart >> kBrickShift;  // a multiple of 4: chunks never straddle a mask word
+    const uint32_t* rowp = nullptr;
+    unsigned rmask = row_on ? 0xffffffffu : 0u;
+    if (live && row_on) {
+        rmask = 0;
+        rowp = live + (static_cast<size_t>(z >> kBrickShift) * nb + (y >> kBrickShift)) * live_words;
+        uint32_t word = 0;
+        int wi = -1;
+        for (int j = 0; j < nch; ++j) {
+            const int b = b0 + 4 * j;
+            if ((b >> 5) != wi) {
+                wi = b >> 5;
+                word = __ldg(rowp + wi);
+            }
+            if ((word >> (b & 31)) & 0xfu) rmask |= 1u << j;
+        }
+    }
+    if (!__reduce_or_sync(0xffffffffu, rmask)) return;
     const int x0 = __ldg(&icp->x0), x1 = __ldg(&icp->x1);
     float R[9];
 #pragma unroll
@@ -276,8 +405,6 @@ __device__ __forceinline__ void integrate_item(
     const F3 step = mk3(__ldg(&icp->step_x[0]), __ldg(&icp->step_x[1]), __ldg(&icp->step_x[2]));
     const float cull_eps = __ldg(&icp->cull_eps), cull_off = __ldg(&icp->cull_off), z_safe = __ldg(&icp->z_safe);
 
-    const int y = ybase + lane;
-    const bool row_on = (y >= y0 && y <= y1);
     F3 c = add3(mv3(R, add3(mk3(ox, oy, oz), mul3(mk3(float(x0), float(y), float(z)), vs))), t_wc);
     const float fW = static_cast<float>(W), fH = static_cast<float>(H);
     const float color_band = fm(0.5f, trunc);
@@ -329,20 +456,36 @@ __device__ __forceinline__ void integrate_item(
     wxs = max(wxs, part * span);
     wxe = min(wxe, (part + 1) * span - 1);
     if (wxs > wxe) return;  // no row of this warp reaches the image in this part
-    const int xfirst = wxs & ~31;
-    if (row_on && xfirst > x0) {
-        // the sequential steps from x0 to the first chunk, replayed exactly
-        // by the closed form of the running float sum (fstep.cuh)
-        const int n0 = xfirst - x0;
-        c = mk3(fs_walk_far(c.x, step.x, n0), fs_walk_far(c.y, step.y, n0), fs_walk_far(c.z, step.z, n0));
-    }
+    // the chunks to visit: kept by the brick pre-cull for some row and inside
+    // the warp's image interval
+    const int jfirst = (wxs - xpart) >> 5, jlast = (wxe - xpart) >> 5;
+    unsigned todo = __reduce_or_sync(0xffffffffu, rmask);
+    todo &= (jlast >= 31 ? 0xffffffffu : ((2u << jlast) - 1u)) & ~((1u << jfirst) - 1u);
+    int xat = x0;  // the x the lanes' c belongs to
 
-    for (int xc = xfirst; xc <= wxe; xc += 32) {
+    while (todo) {
+        const int j = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int xc = xpart + 32 * j;
+        {
+            // skipped chunks: the sequential steps from xat to this chunk,
+            // replayed exactly by the closed form of the running float sum
+            // (fstep.cuh)
+            const int target = max(xc, x0);
+            if (target > xat) {
+                const int n0 = target - xat;
+                if (row_on)
+                    c = mk3(fs_walk_far(c.x, step.x, n0), fs_walk_far(c.y, step.y, n0), fs_walk_far(c.z, step.z, n0));
+                xat = target;
+            }
+        }
         // cull (lane = row), per kCullSeg-voxel piece of the chunk so each
-        // piece's pixels fit a finer tile level. The lane's c belongs to
-        // x = max(xc, x0).
+        // piece's pixels fit a finer tile level, for rows whose bricks the
+        // pre-cull kept. The lane's c belongs to x = max(xc, x0).
         bool live = false;
-        if (row_on) {
+        if (row_on && ((rmask >> j) & 1u)) {
+            const uint32_t nib =
+                rowp ? (__ldg(rowp + ((b0 + 4 * j) >> 5)) >> ((b0 + 4 * j) & 31)) & 0xfu : 0xfu;
             const int xcur = max(xc, x0);
             const int xa = max(xcur, xs), xb = min(min(xc + 31, x1), xe);
             auto piece_live = [&](int pa, int pb) {
@@ -388,9 +531,14 @@ __device__ __forceinline__ void integrate_item(
                 }
                 return !(fminf(ca.z, cb.z) > tm + cull_off);
             };
-            for (int pa = xa; pa <= xb && !live; pa += kCullSeg) live = piece_live(pa, min(pa + kCullSeg - 1, xb));
+            for (int pa = xa; pa <= xb && !live; pa += kCullSeg) {
+                const int pb = min(pa + kCullSeg - 1, xb);
+                const int lo = (pa - xc) >> kBrickShift, hi = (pb - xc) >> kBrickShift;  // the piece's bricks
+                if (nib & ((2u << hi) - (1u << lo))) live = piece_live(pa, pb);
+            }
         }
         const unsigned live_rows = __ballot_sync(0xffffffffu, live);
+        if (!live_rows) continue;  // c stays at xat; the next chunk's jump covers this one
         // chain (lane = row): the sequential c-steps of the chunk
         if (row_on) {
             if (xc >= x0 && xc + 31 <= x1) {
@@ -420,7 +568,7 @@ __device__ __forceinline__ void integrate_item(
                 }
             }
         }
-        if (!live_rows) continue;
+        xat = min(max(xc + 32, x0), x1 + 1);
         __syncwarp();
         // update (lane = x): live rows in groups of kUpdGroup, software
         // pipelined: the projection and depth gather of the next group are
@@ -546,7 +694,7 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
     float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
     float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb,
-    const float* __restrict__ tiles, TileMip mip) {
+    const float* __restrict__ tiles, TileMip mip, const uint32_t* __restrict__ live, int live_words) {
     __shared__ float s_c[kIntWarps][3][32][33];
     if (gate && __ldg(gate) == 0) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -558,7 +706,7 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
         if (item >= n_items) break;
         integrate_item<kHalf, kColor, kResid>(vox, color, icp, depth, rgb, res, vs, ox, oy, oz, trunc, max_w, fx, fy,
                                               cx, cy, W, H, min_d, max_d, nullptr, counters, bricks, nb, tiles, mip,
-                                              item, warp, lane, s_c, kIntParts);
+                                              item, warp, lane, s_c, kIntParts, live, live_words);
     }
 }
 
@@ -1261,6 +1409,13 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
                                              p.origin[2], p.truncation, fx, fy, cx, cy, W, H, max_d, v->d_iconsts,
                                              v->d_counters, tiles, mip, d_tiles_built ? 0 : 1);
     AZU_LAUNCH_CHECK();
+    {
+        const int rows = v->nb * v->nb * v->int_live_words;  // warps of the pre-cull
+        integrate_bricks_kernel<<<(rows + 7) / 8, 256, 0, s>>>(
+            v->d_iconsts, p.resolution, v->nb, v->int_live_words, p.voxel_size, p.origin[0], p.origin[1],
+            p.origin[2], fx, fy, cx, cy, W, H, tiles, mip, d_gate, v->int_live);
+        AZU_LAUNCH_CHECK();
+    }
     const int ngroups = (p.resolution + 31) / 32;
     const long items = static_cast<long>(p.resolution) * ngroups;
     const bool half = p.format != AZU_TSDF_FP32;
@@ -1287,7 +1442,7 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
 #define AZU_INT_ARGS                                                                                             \
     v->vox, v->color, v->d_iconsts, d_depth_m, d_rgb, p.resolution, p.voxel_size, p.origin[0], p.origin[1],     \
         p.origin[2], p.truncation, p.max_weight, fx, fy, cx, cy, W, H, min_d, max_d, d_gate, v->d_counters,   \
-        v->bricks, v->nb, tiles, mip
+        v->bricks, v->nb, tiles, mip, v->int_live, v->int_live_words
     if (!half && !col) integrate_kernel<false, false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (!half && col) integrate_kernel<false, true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (!resid && !col) integrate_kernel<true, false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
@@ -1335,6 +1490,8 @@ static int volume_alloc(azu_volume* v) {
     AZU_TRY_CUDA(cudaMalloc(&v->bricks, static_cast<size_t>(v->nb) * v->nb * v->nb));
     AZU_TRY_CUDA(cudaMalloc(&v->brick_dist, static_cast<size_t>(v->nb) * v->nb * v->nb));
     AZU_TRY_CUDA(cudaMalloc(&v->brick_tmp, static_cast<size_t>(v->nb) * v->nb * v->nb));
+    v->int_live_words = (v->nb + 31) / 32;
+    AZU_TRY_CUDA(cudaMalloc(&v->int_live, static_cast<size_t>(v->nb) * v->nb * v->int_live_words * 4));
     if (!v->d_tiles) {
         const size_t n = static_cast<size_t>(make_tile_mip(640, 480).total);
         AZU_TRY_CUDA(cudaMalloc(&v->d_tiles, n * sizeof(float)));
@@ -1348,6 +1505,8 @@ static void volume_free_storage(azu_volume* v) {
     if (v->bricks) cudaFree(v->bricks);
     if (v->brick_dist) cudaFree(v->brick_dist);
     if (v->brick_tmp) cudaFree(v->brick_tmp);
+    if (v->int_live) cudaFree(v->int_live);
+    v->int_live = nullptr;
     v->brick_dist = nullptr;
     v->brick_tmp = nullptr;
     v->vox = nullptr;

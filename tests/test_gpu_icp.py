@@ -130,3 +130,47 @@ def test_track_without_prepare_is_a_state_error(cuda_lib):
     with pytest.raises(_abi.AzuError) as e:
         t.track_prepared(640, 480, mv, mv, 640, 480, np.eye(4), np.eye(4))
     assert e.value.code == _abi.AZU_E_STATE
+
+
+def test_counts_exact_at_the_gpu_own_poses(cuda_lib, orc, seq, model):
+    """The counters a track reports come from the association of its last
+    accepted iteration (ICPTracker.cpp:77-128: inliers, valid live/model,
+    projected, distance- and angle-filtered). Iteration j of level l runs at
+    the pose the tracker reached after j - 1 iterations, which a track whose
+    level l stops after j - 1 iterations returns bit for bit (the iterations
+    before it are the same code on the same inputs). So every counter the GPU
+    reports after iteration j must equal the oracle's association at the
+    GPU's own pose after j - 1: the counts are exact, and any difference from
+    an oracle track is in the float pose alone."""
+    from azu_gb300 import synth
+    mv, mn, ref = model
+    K = orc.intr(525, 525, 319.5, 239.5)
+    prm = orc.icp_params(fold_threads=0)
+    # GPU result key -> oracle association key
+    keys = {"inliers": "inliers", "valid_live_points": "valid_live", "valid_model_points": "valid_model",
+            "projected_points": "projected", "dist_filtered": "dist_filtered", "angle_filtered": "angle_filtered"}
+    checked = 0
+    for k in (9, 11):
+        dm = synth.mm_to_meters(seq.depth_mm[k])
+        levels = orc.frame_pyramid_from_depth(dm, K)
+        full = (10, 5, 4)
+        for lvl in (2, 1, 0):
+            # the pose iteration 1 of this level starts from: the estimate, or
+            # what a track whose finer levels run no iterations returns
+            prev = dict(pose=np.asarray(seq.poses[8], np.float32)) if lvl == 2 else None
+            for j in range(0 if lvl < 2 else 1, full[lvl] + 1):
+                iters = tuple(full[i] if i > lvl else (j if i == lvl else 0) for i in range(3))
+                t = _tracker(iters=iters)
+                t.prepare_live(_dev(dm), 640, 480)
+                g = t.track_prepared(640, 480, _dev(mv), _dev(mn), 640, 480, seq.poses[8], ref)
+                assert g["status"] == 0
+                if prev is not None:
+                    if np.array_equal(np.asarray(g["pose"]).view(np.uint32), np.asarray(prev["pose"]).view(np.uint32)):
+                        break  # iteration j made no update (converged or stopped before it): the level is done
+                    lv = levels[lvl]
+                    o = orc.icp_build_system(prm, K, lv[1], lv[2], mv, mn, prev["pose"], ref)
+                    for key, okey in keys.items():
+                        assert g[key] == o[okey], (k, lvl, j, key, g[key], o[okey])
+                    checked += 1
+                prev = g
+    assert checked >= 10
