@@ -99,13 +99,18 @@ struct azu_volume {
     float* d_pose = nullptr;    // 16 floats: pose slot for host-pose calls
     azu::IntegrateConsts* d_iconsts = nullptr;
     unsigned long long* d_counters = nullptr;  // [0] newly observed (cumulative), [1] updated (last), [2] colour (last),
-                                               // [3] updated (cumulative), [4] integrate work counter
+                                               // [3] updated (cumulative), [4] integrate work counter,
+                                               // [5 .. 5 + kIntBuckets) sizes of the integrate work buckets
     int int_blocks = 0;                        // resident blocks of the persistent integrate kernel
     // One bit per 8^3 brick that the frame being integrated may update, rows
     // of nb bricks along x in 32-bit words (int_live_words per row), rows in
     // (z, y) order: written by the brick pre-cull before every integration.
     uint32_t* int_live = nullptr;
     int int_live_words = 0;
+    // The items of the integration that the pre-cull keeps, in kIntBuckets
+    // buckets by their kept-brick count (bucket b of n_items slots at
+    // int_list + b * n_items), taken heaviest first.
+    int* int_list = nullptr;
     float* d_depth_stage = nullptr;            // host-depth staging (integrate_host)
     uint8_t* d_rgb_stage = nullptr;
     size_t stage_pixels = 0;

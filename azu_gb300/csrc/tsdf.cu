@@ -67,6 +67,8 @@ constexpr int kCullSeg = 16;   // voxels per culling piece of a 32-voxel chunk
 constexpr int kIntParts = 2;   // x-parts per 32-row item of the persistent kernel (shorter items, shorter tail)
 constexpr int kUpdGroup = 4;   // rows per software-pipelined update group (6 and 8 were slower)
 constexpr int kFineSide = 4;   // level-0 depth tiles a culling box may span a side before a coarser level is used
+constexpr int kIntBuckets = 8; // work buckets of the integration, by kept-brick count
+constexpr int kCounters = 5 + kIntBuckets;
 
 // Deepest in-band depth of every 8x8 pixel tile (-inf when the tile has none),
 // level 0 of the tile pyramid. Eight lanes share a tile, one pixel row each.
@@ -221,6 +223,7 @@ __device__ __forceinline__ void integrate_setup_body(const float* __restrict__ d
         counters[1] = 0;
         counters[2] = 0;
         counters[4] = 0;  // next warp item of the integrate kernel
+        for (int b = 0; b < kIntBuckets; ++b) counters[5 + b] = 0;
     }
     if (pyramid) build_tile_pyramid(tiles, mip);
 }
@@ -326,6 +329,51 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(
     }
     const unsigned bits = __ballot_sync(0xffffffffu, on);
     if (lane == 0) live[static_cast<size_t>(row) * words + word] = bits;
+}
+
+// Work list of the integration: every item (32 rows at one z, one x-part)
+// with a kept brick in its rows and part goes into the bucket of its
+// kept-brick count, so that the persistent kernel can take the heaviest items
+// first: an item's cost grows with its kept bricks, and items differ by two
+// orders of magnitude, so an item started last would otherwise set the end.
+// Order within a bucket is arbitrary: every item writes its own voxels and
+// the counters are integer sums, so the results do not depend on it.
+__global__ void __launch_bounds__(256) integrate_list_kernel(const IntegrateConsts* __restrict__ icp, int res,
+                                                             int nb, int words, int nparts,
+                                                             const uint32_t* __restrict__ live,
+                                                             const int* __restrict__ gate,
+                                                             unsigned long long* __restrict__ counters,
+                                                             int* __restrict__ list) {
+    if (gate && __ldg(gate) == 0) return;
+    const int ngroups = (res + 31) >> 5;
+    const int n_items = res * ngroups * nparts;
+    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= n_items || !__ldg(&icp->valid)) return;
+    const int part = item % nparts, it = item / nparts;
+    const int z = it / ngroups, ybase = (it - z * ngroups) << 5;
+    const int z0 = __ldg(&icp->z0), z1 = __ldg(&icp->z1), y0 = __ldg(&icp->y0), y1 = __ldg(&icp->y1);
+    if (z < z0 || z > z1 || ybase + 31 < y0 || ybase > y1) return;
+    const int span = (((res + nparts - 1) / nparts) + 31) & ~31;
+    const int xpart = part * span;
+    if (xpart >= res) return;
+    const int ba = xpart >> kBrickShift, bb = min((xpart + span) >> kBrickShift, nb);  // bricks [ba, bb)
+    int cost = 0;
+    for (int r = 0; r < 4; ++r) {
+        const int ya = ybase + 8 * r;
+        if (ya > y1 || ya + 7 < y0 || ya >= res) continue;
+        const uint32_t* rowp = live + (static_cast<size_t>(z >> kBrickShift) * nb + (ya >> kBrickShift)) * words;
+        for (int w = ba >> 5; w <= (bb - 1) >> 5; ++w) {
+            uint32_t m = __ldg(rowp + w);
+            const int lo = max(ba - 32 * w, 0), hi = min(bb - 32 * w, 32);  // bits [lo, hi)
+            m &= (hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+            cost += __popc(m);
+        }
+    }
+    if (!cost) return;
+    // buckets by the bit length of the count, heaviest (most bricks) first
+    const int b = max(0, kIntBuckets - (32 - __clz(cost)));
+    const unsigned long long k = atomicAdd(&counters[5 + b], 1ull);
+    list[static_cast<size_t>(b) * n_items + k] = item;
 }
 
 // fs_walk kept out of line (it runs once per item, not per voxel).
@@ -694,16 +742,28 @@ __global__ void __launch_bounds__(kIntWarps * 32) integrate_kernel(
     const float* __restrict__ depth, const uint8_t* __restrict__ rgb, int res, float vs, float ox, float oy,
     float oz, float trunc, float max_w, float fx, float fy, float cx, float cy, int W, int H, float min_d,
     float max_d, const int* __restrict__ gate, unsigned long long* __restrict__ counters, uint8_t* bricks, int nb,
-    const float* __restrict__ tiles, TileMip mip, const uint32_t* __restrict__ live, int live_words) {
+    const float* __restrict__ tiles, TileMip mip, const uint32_t* __restrict__ live, int live_words,
+    const int* __restrict__ list) {
     __shared__ float s_c[kIntWarps][3][32][33];
     if (gate && __ldg(gate) == 0) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n_items = res * ((res + 31) >> 5) * kIntParts;
+    // bucket b holds positions [s_end[b - 1], s_end[b]) of the work order
+    __shared__ int s_end[kIntBuckets];
+    if (threadIdx.x == 0) {
+        int e = 0;
+        for (int b = 0; b < kIntBuckets; ++b) s_end[b] = e += static_cast<int>(__ldcg(&counters[5 + b]));
+    }
+    __syncthreads();
+    const int total = s_end[kIntBuckets - 1];
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = static_cast<int>(atomicAdd(&counters[4], 1ull));
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= n_items) break;
+        int pos = 0;
+        if (lane == 0) pos = static_cast<int>(atomicAdd(&counters[4], 1ull));
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (pos >= total) break;
+        int b = 0;
+        while (pos >= s_end[b]) ++b;
+        const int item = __ldcg(list + static_cast<size_t>(b) * n_items + (pos - (b ? s_end[b - 1] : 0)));
         integrate_item<kHalf, kColor, kResid>(vox, color, icp, depth, rgb, res, vs, ox, oy, oz, trunc, max_w, fx, fy,
                                               cx, cy, W, H, min_d, max_d, nullptr, counters, bricks, nb, tiles, mip,
                                               item, warp, lane, s_c, kIntParts, live, live_words);
@@ -1415,6 +1475,11 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
             v->d_iconsts, p.resolution, v->nb, v->int_live_words, p.voxel_size, p.origin[0], p.origin[1],
             p.origin[2], fx, fy, cx, cy, W, H, tiles, mip, d_gate, v->int_live);
         AZU_LAUNCH_CHECK();
+        const int n_items = p.resolution * ((p.resolution + 31) / 32) * kIntParts;
+        integrate_list_kernel<<<(n_items + 255) / 256, 256, 0, s>>>(v->d_iconsts, p.resolution, v->nb,
+                                                                   v->int_live_words, kIntParts, v->int_live,
+                                                                   d_gate, v->d_counters, v->int_list);
+        AZU_LAUNCH_CHECK();
     }
     const int ngroups = (p.resolution + 31) / 32;
     const long items = static_cast<long>(p.resolution) * ngroups;
@@ -1442,7 +1507,7 @@ int volume_integrate_dev(azu_volume* v, const float* d_depth_m, const uint8_t* d
 #define AZU_INT_ARGS                                                                                             \
     v->vox, v->color, v->d_iconsts, d_depth_m, d_rgb, p.resolution, p.voxel_size, p.origin[0], p.origin[1],     \
         p.origin[2], p.truncation, p.max_weight, fx, fy, cx, cy, W, H, min_d, max_d, d_gate, v->d_counters,   \
-        v->bricks, v->nb, tiles, mip, v->int_live, v->int_live_words
+        v->bricks, v->nb, tiles, mip, v->int_live, v->int_live_words, v->int_list
     if (!half && !col) integrate_kernel<false, false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (!half && col) integrate_kernel<false, true, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
     else if (!resid && !col) integrate_kernel<true, false, false><<<blocks, kIntWarps * 32, 0, s>>>(AZU_INT_ARGS);
@@ -1492,6 +1557,10 @@ static int volume_alloc(azu_volume* v) {
     AZU_TRY_CUDA(cudaMalloc(&v->brick_tmp, static_cast<size_t>(v->nb) * v->nb * v->nb));
     v->int_live_words = (v->nb + 31) / 32;
     AZU_TRY_CUDA(cudaMalloc(&v->int_live, static_cast<size_t>(v->nb) * v->nb * v->int_live_words * 4));
+    {
+        const size_t n_items = static_cast<size_t>(v->p.resolution) * ((v->p.resolution + 31) / 32) * kIntParts;
+        AZU_TRY_CUDA(cudaMalloc(&v->int_list, n_items * kIntBuckets * sizeof(int)));
+    }
     if (!v->d_tiles) {
         const size_t n = static_cast<size_t>(make_tile_mip(640, 480).total);
         AZU_TRY_CUDA(cudaMalloc(&v->d_tiles, n * sizeof(float)));
@@ -1507,6 +1576,8 @@ static void volume_free_storage(azu_volume* v) {
     if (v->brick_tmp) cudaFree(v->brick_tmp);
     if (v->int_live) cudaFree(v->int_live);
     v->int_live = nullptr;
+    if (v->int_list) cudaFree(v->int_list);
+    v->int_list = nullptr;
     v->brick_dist = nullptr;
     v->brick_tmp = nullptr;
     v->vox = nullptr;
@@ -1544,7 +1615,7 @@ extern "C" int azu_volume_reset(azu_volume* v) {
     if (v->p.format != AZU_TSDF_FP32) reset_kernel<true><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
     else reset_kernel<false><<<blocks, 256, 0, v->stream.s>>>(v->vox, v->color, n);
     AZU_LAUNCH_CHECK();
-    AZU_TRY_CUDA(cudaMemsetAsync(v->d_counters, 0, 5 * sizeof(unsigned long long), v->stream.s));
+    AZU_TRY_CUDA(cudaMemsetAsync(v->d_counters, 0, kCounters * sizeof(unsigned long long), v->stream.s));
     AZU_TRY_CUDA(cudaMemsetAsync(v->bricks, 1, static_cast<size_t>(v->nb) * v->nb * v->nb, v->stream.s));
     v->integrated_frames = 0;
     return AZU_OK;
@@ -1562,7 +1633,7 @@ extern "C" int azu_volume_create(int device, const azu_volume_params* p, void* s
     if (!rc) rc = volume_alloc(v);
     if (!rc) { cudaError_t e = cudaMalloc(&v->d_pose, 16 * sizeof(float)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
     if (!rc) { cudaError_t e = cudaMalloc(&v->d_iconsts, sizeof(IntegrateConsts)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
-    if (!rc) { cudaError_t e = cudaMalloc(&v->d_counters, 5 * sizeof(unsigned long long)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
+    if (!rc) { cudaError_t e = cudaMalloc(&v->d_counters, kCounters * sizeof(unsigned long long)); if (e) { set_error("cudaMalloc: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; } }
     if (!rc) rc = azu_volume_reset(v);
     if (rc) {
         azu_volume_destroy(v);

@@ -143,6 +143,79 @@ def committed_hit_rates():
         return None, None
 
 
+def raycast_roofline(pl, vol, seq, dev, stream):
+    """The raycast against the L2: B_ray = 24 W H (vertex + normal out) + 64 S
+    logical gathered bytes, S the trilinear samples the reference's march
+    takes at this pose (counted by the oracle on the downloaded volume), over
+    one raycast of the same volume timed with CUDA events on the pipeline's
+    stream (the volume's). The denominator is an L2-resident copy measured here (no L2 figure
+    is in the measured peaks): torch copies of a 32 MiB buffer, read + write
+    bytes over the best time."""
+    import ctypes as C
+    import torch
+    from azu_gb300 import api
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    lib = api._abi.load()
+    W_, H_ = seq.width, seq.height
+    K = (seq.fx, seq.fy, seq.cx, seq.cy)
+    pose = np.asarray(pl.last_result()["pose"], np.float32)
+    d_v = torch.empty((H_, W_, 3), dtype=torch.float32, device=f"cuda:{dev}")
+    d_n = torch.empty_like(d_v)
+    ls = stream
+    call = lambda: api._abi.check(lib.azu_volume_raycast(vol, api._pose(pose), *map(float, K), W_, H_,  # noqa: E731
+                                                         C.c_void_p(d_v.data_ptr()), C.c_void_p(d_n.data_ptr()),
+                                                         None), "raycast")
+    for _ in range(3):
+        call()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+    for e0, e1 in ev:
+        e0.record(ls)
+        call()
+        e1.record(ls)
+    torch.cuda.synchronize(dev)
+    ms = float(np.median([e0.elapsed_time(e1) for e0, e1 in ev]))
+    n = seq.volume["resolution"] ** 3
+    t = np.empty(n, np.float32)
+    w = np.empty(n, np.float32)
+    api._abi.check(lib.azu_volume_download(vol, t.ctypes.data_as(C.c_void_p), w.ctypes.data_as(C.c_void_p), None),
+                   "download")
+    v = seq.volume
+    o = O.Volume(O.tsdf_params(resolution=v["resolution"], voxel_size=v["voxel_size"], truncation=v["truncation"],
+                               max_weight=v["max_weight"], origin=v["origin"], min_depth=seq.min_depth,
+                               max_depth=seq.max_depth))
+    o.tsdf[:] = t
+    o.weight[:] = w
+    del t, w
+    r = o.raycast(pose, O.intr(*K), W_, H_)
+    samples = int(r["samples"])
+    hits = int(np.count_nonzero(np.any(d_v.cpu().numpy() != 0, axis=-1)))
+    # L2 reference: 32 MiB copies stay in the 126 MB L2
+    a = torch.empty(8 << 20, dtype=torch.float32, device=f"cuda:{dev}")
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    best = None
+    for _ in range(20):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        t_ms = e0.elapsed_time(e1) / 10
+        best = t_ms if best is None else min(best, t_ms)
+    l2_gbs = 2 * a.numel() * 4 / (best * 1e-3) / 1e9
+    b_ray = 24.0 * W_ * H_ + 64.0 * samples
+    achieved = b_ray / (ms * 1e-3) / 1e9
+    return {"bound": "l2", "achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
+            "launch_ms": ms, "logical_samples": samples, "logical_bytes": b_ray, "hits": hits,
+            "peak_source": "measured in this run: L2-resident 32 MiB device copy (read + write bytes)",
+            "note": "B_ray = 24 W H + 64 S with S the samples of the reference's own march at the last pose "
+                    "(the oracle on the downloaded volume); the kernel takes fewer, skipping free bricks"}
+
+
 def committed_traffic():
     """Per-launch DRAM bytes of the integrate kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "integrate_c2_512.md")
@@ -755,6 +828,11 @@ def run_gpu(args):
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         line["cpu_stage_s_per_frame"] = cpu["stage_s_per_frame"]
     # before the ingest run, which feeds the pipeline other frames
+    if rank == 0:
+        try:
+            line["raycast"]["roofline"] = raycast_roofline(pl, vol, seq, dev, stream)
+        except Exception as e:  # the oracle build or the host download failed: report, do not fail the bench
+            line["raycast"]["roofline"] = {"unavailable": str(e)[:200]}
     line.update(run_beside(pl, vp, seq, frame, dev))
     if args.ingest_frames > 0:
         line["ingest"] = run_ingest(pl, raw, rgb, args.ingest_frames)
