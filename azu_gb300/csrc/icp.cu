@@ -273,7 +273,8 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // Precision form: the per-pixel terms and the warp sums stay FP32 (the same
 // recursive halving as the plain path); the sum over the block's warps is
 // compensated (each value carries the exact error of its additions), and the
-// block partial enters the FP64 cross-block sum as (double) s + (double) c.
+// block partial is stored as the float pair (s, c) for the compensated
+// cross-block sum.
 __device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, int vb, double* s_red_raw) {
     constexpr int kNV = kNF + kNI;
     float* s_red = reinterpret_cast<float*>(s_red_raw);
@@ -303,8 +304,8 @@ __device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, in
             c = __fadd_rn(c, err);
         }
         if (k < kNF)
-            a.partials[(static_cast<size_t>(slot) * kNF + k) * nb + vb] =
-                static_cast<double>(sum) + static_cast<double>(c);
+            reinterpret_cast<float2*>(a.partials)[(static_cast<size_t>(slot) * kNF + k) * nb + vb] =
+                make_float2(sum, c);
         else
             a.ipartials[(static_cast<size_t>(slot) * kNI + (k - kNF)) * nb + vb] = static_cast<int>(sum);
     }
@@ -438,9 +439,76 @@ __device__ __forceinline__ void reduce_grid_t<float>(const IcpArgs& a, int slot,
         reduce_grid_f<kPerLane, 2>(a, slot, s_sum, s_isum);
 }
 
+// (s, c) += (s2, c2): a float-float sum, s the rounded total and c the sum of
+// the exact rounding errors (TwoSum), about 48 significant bits.
+__device__ __forceinline__ void ff_add(float& s, float& c, float s2, float c2) {
+    float t, e;
+    two_sum(s, s2, t, e);
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(c2, e));
+}
+
+// Precision form: the cross-block sum of the (s, c) partials in float-float,
+// in the fixed order of reduce_grid_f (lane l takes slots l + 32 j, then a
+// shuffle tree), all of a round's loads in flight; each value lands in s_sum
+// as the double s + c. Pure FP32 instructions: GB300's FP64 rate is a small
+// fraction of its FP32 rate.
+template <int kPL, int kVals>
+__device__ __forceinline__ void reduce_grid_ff(const IcpArgs& a, int slot, double* s_sum, int* s_isum) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    const int nb = a.vblocks;
+    const float2* fp = reinterpret_cast<const float2*>(a.partials);
+    for (int k0 = warp; k0 < kNF + kNI; k0 += kVals * nw) {
+        float2 w[kVals][kPL];
+#pragma unroll
+        for (int r = 0; r < kVals; ++r) {
+            const int k = k0 + r * nw;
+#pragma unroll
+            for (int j = 0; j < kPL; ++j) {
+                const int b = lane + 32 * j;
+                w[r][j] = make_float2(0.0f, 0.0f);
+                if (b < nb && k < kNF) {
+                    w[r][j] = __ldcg(fp + (static_cast<size_t>(slot) * kNF + k) * nb + b);
+                } else if (b < nb && k < kNF + kNI) {
+                    const int* src = a.ipartials + (static_cast<size_t>(slot) * kNI + (k - kNF)) * nb;
+                    w[r][j].x = static_cast<float>(__ldcg(src + b));
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kVals; ++r) {
+            const int k = k0 + r * nw;
+            if (k < kNF) {
+                float sm = 0.0f, c = 0.0f;
+#pragma unroll
+                for (int j = 0; j < kPL; ++j) ff_add(sm, c, w[r][j].x, w[r][j].y);
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float s2 = __shfl_down_sync(0xffffffffu, sm, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
+                    ff_add(sm, c, s2, c2);
+                }
+                if (lane == 0) s_sum[k] = static_cast<double>(sm) + static_cast<double>(c);
+            } else if (k < kNF + kNI) {
+                int sum = 0;
+#pragma unroll
+                for (int j = 0; j < kPL; ++j) sum += static_cast<int>(w[r][j].x);
+                for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+                if (lane == 0) s_isum[k - kNF] = sum;
+            }
+        }
+    }
+    __syncthreads();
+}
+
 __device__ void reduce_grid(const IcpArgs& a, int slot, double* s_sum, int* s_isum) {
-    if (a.precision) reduce_grid_t<double>(a, slot, s_sum, s_isum);
-    else reduce_grid_t<float>(a, slot, s_sum, s_isum);
+    if (a.precision) {
+        if (a.vblocks <= 5 * 32 && 3 * static_cast<int>(blockDim.x >> 5) >= kNF + kNI)
+            reduce_grid_ff<5, 3>(a, slot, s_sum, s_isum);
+        else
+            reduce_grid_ff<kPerLane, 2>(a, slot, s_sum, s_isum);
+    } else {
+        reduce_grid_t<float>(a, slot, s_sum, s_isum);
+    }
 }
 
 // Reduced sum k as float (the storage holds floats unless in precision form).
@@ -516,32 +584,42 @@ __device__ void warp_eig6(float* m /* smem 36, destroyed */, float* cs /* smem 1
     mx = hi;
 }
 
-// A x = b by Cholesky in double (precision form).
-__device__ bool chol_solve_d(const double* Ain, const double* b, double* x) {
-    double L[36];
-    for (int i = 0; i < 36; ++i) L[i] = 0.0;
+// A x = b by Cholesky in double (precision form): unrolled on a packed lower
+// triangle, one reciprocal per pivot (GB300's FP64 divide and square root are
+// long sequences; this keeps six of each).
+__device__ __noinline__ bool chol_solve_d(const double* Ain, const double* b, double* x) {
+    double L[21], inv[6];  // L(i, j), j <= i, at i (i + 1) / 2 + j
+#pragma unroll
     for (int j = 0; j < 6; ++j) {
         double s = Ain[j * 6 + j];
-        for (int k = 0; k < j; ++k) s -= L[j * 6 + k] * L[j * 6 + k];
+#pragma unroll
+        for (int k = 0; k < j; ++k) s -= L[j * (j + 1) / 2 + k] * L[j * (j + 1) / 2 + k];
         if (!(s > 0.0)) return false;
         const double d = sqrt(s);
-        L[j * 6 + j] = d;
+        inv[j] = 1.0 / d;
+        L[j * (j + 1) / 2 + j] = d;
+#pragma unroll
         for (int i = j + 1; i < 6; ++i) {
             double t = Ain[i * 6 + j];
-            for (int k = 0; k < j; ++k) t -= L[i * 6 + k] * L[j * 6 + k];
-            L[i * 6 + j] = t / d;
+#pragma unroll
+            for (int k = 0; k < j; ++k) t -= L[i * (i + 1) / 2 + k] * L[j * (j + 1) / 2 + k];
+            L[i * (i + 1) / 2 + j] = t * inv[j];
         }
     }
     double y[6];
+#pragma unroll
     for (int i = 0; i < 6; ++i) {
         double s = b[i];
-        for (int k = 0; k < i; ++k) s -= L[i * 6 + k] * y[k];
-        y[i] = s / L[i * 6 + i];
+#pragma unroll
+        for (int k = 0; k < i; ++k) s -= L[i * (i + 1) / 2 + k] * y[k];
+        y[i] = s * inv[i];
     }
+#pragma unroll
     for (int i = 5; i >= 0; --i) {
         double s = y[i];
-        for (int k = i + 1; k < 6; ++k) s -= L[k * 6 + i] * x[k];
-        x[i] = s / L[i * 6 + i];
+#pragma unroll
+        for (int k = i + 1; k < 6; ++k) s -= L[k * (k + 1) / 2 + i] * x[k];
+        x[i] = s * inv[i];
     }
     return true;
 }
@@ -627,6 +705,31 @@ __device__ __forceinline__ bool is_rotation(const T* X, T tol) {
     return det > T(0);
 }
 
+// sin and cos of an angle of at most 0.5 rad (the rotation cap bounds every
+// accepted step) by their Taylor series in FP64: after the x^19 / x^18 terms
+// the remainder is below 1e-25, far under half an ulp of the results.
+__device__ __forceinline__ void sincos_small(double x, double& sn, double& cs) {
+    if (!(fabs(x) <= 0.5)) {  // outside the series' range (not reached by capped steps)
+        sincos(x, &sn, &cs);
+        return;
+    }
+    // 1 / n!, n = 0 .. 19
+    constexpr double kInvFact[20] = {
+        1.0, 1.0, 1.0 / 2.0, 1.0 / 6.0, 1.0 / 24.0, 1.0 / 120.0, 1.0 / 720.0, 1.0 / 5040.0, 1.0 / 40320.0,
+        1.0 / 362880.0, 1.0 / 3628800.0, 1.0 / 39916800.0, 1.0 / 479001600.0, 1.0 / 6227020800.0,
+        1.0 / 87178291200.0, 1.0 / 1307674368000.0, 1.0 / 20922789888000.0, 1.0 / 355687428096000.0,
+        1.0 / 6402373705728000.0, 1.0 / 121645100408832000.0};
+    const double x2 = x * x;
+    double ps = kInvFact[19], pc = kInvFact[18];
+#pragma unroll
+    for (int k = 8; k >= 0; --k) {
+        ps = kInvFact[2 * k + 1] - x2 * ps;
+        pc = kInvFact[2 * k] - x2 * pc;
+    }
+    sn = x * ps;
+    cs = pc;
+}
+
 // Precision form: SE(3) exponential of the step and pose composition in FP64,
 // then the nearest rotation (orthogonal polar factor, = U V^T of the SVD for
 // det > 0) by two Newton-Schulz steps X <- X (3 I - X^T X) / 2 in FP64.
@@ -635,8 +738,11 @@ __device__ void compose_precise(float* pose, const double* x) {
     const double angle = sqrt(rx * rx + ry * ry + rz * rz);
     double R[9];
     if (angle > 1e-4) {
-        const double ax = rx / angle, ay = ry / angle, az = rz / angle;
-        const double sn = sin(angle), cs = cos(angle), cc = 1.0 - cs;
+        const double ia = 1.0 / angle;
+        const double ax = rx * ia, ay = ry * ia, az = rz * ia;
+        double sn, cs;
+        sincos_small(angle, sn, cs);
+        const double cc = 1.0 - cs;
         R[0] = cs + cc * ax * ax;      R[1] = cc * ax * ay - sn * az; R[2] = cc * ax * az + sn * ay;
         R[3] = cc * ax * ay + sn * az; R[4] = cs + cc * ay * ay;      R[5] = cc * ay * az - sn * ax;
         R[6] = cc * ax * az - sn * ay; R[7] = cc * ay * az + sn * ax; R[8] = cs + cc * az * az;
@@ -749,9 +855,9 @@ struct SolveSmem {
     float cs[12];
     int action;    // 0 continue, 1 stop level
     int need_eig;  // the shifted-Cholesky test could not settle the damping
-    float xdef[6]; // solution with the level's default damping
-    double xdef_d[6];  // the same in FP64 (precision form)
-    int xdef_ok;
+    float spec_pose[16];  // the pose the step with the level's default damping leads to
+    float spec_step;      // that step's norm
+    int spec_ok;          // 0: that step stops the level (no solution, not finite or over a cap)
 };
 
 // Cholesky factor of A + shift I (6x6, float), fully unrolled so that the
@@ -837,68 +943,24 @@ __device__ bool damped_solve(const IcpArgs& a, const SolveSmem& sm, float damp, 
     return true;
 }
 
-// One solve from the reduced sums (ICPTracker.cpp:78-131), executed by warp 0.
-// Lane 1 solves with the level's default damping while lane 0 runs the
-// damping test; only an escalated damping needs a second solve.
-__device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelState& st) {
-    const int lane = threadIdx.x & 31;
-    const int inl = sm.isum[0];
-    const float base_damp = (level == 0) ? kDampingLevel0 : kDampingDefault;
-    if (lane == 0) {
-        for (int k = 1; k < 6; ++k) st.counts[k] = sm.isum[k];
-        sm.action = (inl <= 0 || inl < kMinInliersForIteration) ? 1 : 0;
-        if (sm.action == 0) {
-            int k = 0;
-            for (int i = 0; i < 6; ++i)
-                for (int j = i; j < 6; ++j) {
-                    const float v = sum_f(a, sm.sum, k++);
-                    st.information[i * 6 + j] = v;
-                    st.information[j * 6 + i] = v;
-                }
-            for (int i = 0; i < 36; ++i) sm.m[i] = st.information[i];
-            // dampingForHessian (ICPShared.h:86-100) escalates when min_eig < 1e-4
-            // or max_eig > 1e7 min_eig. Since max_eig <= trace, min_eig >= sigma =
-            // max(1e-4, trace / 1e7) rules both out; A - sigma' I positive definite
-            // proves it, with sigma' = 2 sigma + 32 eps trace covering the
-            // rounding of the float factorisation. Only when that test fails do
-            // the eigenvalues decide.
-            float tr = 0.0f;
-            for (int i = 0; i < 6; ++i) tr += st.information[i * 6 + i];
-            const float sigma = fmaxf(kMinEigEscalate, tr / kCondEscalate);
-            const float shift = 2.0f * sigma + 32.0f * 1.1920929e-7f * tr;
-            sm.need_eig = (isfinite(tr) && pd_after_shift(st.information, shift)) ? 0 : 1;
-        }
-    } else if (lane == 1 && !(inl <= 0 || inl < kMinInliersForIteration)) {
-        sm.xdef_ok = damped_solve(a, sm, base_damp, sm.xdef, sm.xdef_d) ? 1 : 0;
-    }
-    __syncwarp();
-    if (sm.action != 0) return;
-    float mn = 1.0f, mx = 1.0f;
-    if (sm.need_eig) warp_eig6(sm.m, sm.cs, mn, mx);
-    if (lane != 0) return;
-    float damp = base_damp;
-    if (sm.need_eig) {
-        if (!isfinite(mn) || !isfinite(mx) || mn < kMinEigEscalate) damp = kDampingEscalated;
-        else if (mx > kCondEscalate * mn) damp = kDampingEscalated;
-    }
+// The step of damping `damp` from the reduced sums and the pose it leads to
+// (ICPTracker.cpp:86-119): false when the damped system has no solution or
+// the step is not finite or exceeds a cap, which stops the level.
+__device__ __noinline__ bool step_pose(const IcpArgs& a, const SolveSmem& sm, const float* pose, float damp,
+                                       float* out, float& step_norm) {
     float x[6];
     double xd[6];
-    if (damp == base_damp) {
-        if (!sm.xdef_ok) { sm.action = 1; return; }
-        for (int i = 0; i < 6; ++i) { x[i] = sm.xdef[i]; xd[i] = sm.xdef_d[i]; }
-    } else if (!damped_solve(a, sm, damp, x, xd)) {
-        sm.action = 1;
-        return;
-    }
+    if (!damped_solve(a, sm, damp, x, xd)) return false;
     bool fin = true;
     for (int i = 0; i < 6; ++i) fin = fin && isfinite(x[i]);
     const float tn = norm3(mk3(x[0], x[1], x[2])), rn = norm3(mk3(x[3], x[4], x[5]));
-    if (!fin || tn > kTranslationCapStep || rn > kRotationCapStep) { sm.action = 1; return; }
+    if (!fin || tn > kTranslationCapStep || rn > kRotationCapStep) return false;
     float ss = 0.0f;
     for (int i = 0; i < 6; ++i) ss = fa(ss, fm(x[i], x[i]));
-    const float step_norm = fsq(ss);
+    step_norm = fsq(ss);
+    for (int i = 0; i < 16; ++i) out[i] = pose[i];
     if (a.precision) {
-        compose_precise(st.pose, xd);
+        compose_precise(out, xd);
     } else {
         const float rx = x[3], ry = x[4], rz = x[5];
         float delta[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -914,8 +976,82 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
         for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) delta[4 * i + j] = R[3 * i + j];
         delta[3] = x[0]; delta[7] = x[1]; delta[11] = x[2];
         float P[16];
-        mm4(st.pose, delta, P);
+        mm4(pose, delta, P);
         project_so3_f(P);
+        for (int i = 0; i < 16; ++i) out[i] = P[i];
+    }
+    return true;
+}
+
+// Barrier of warps 0 and 1 only (named barrier 1, 64 threads).
+__device__ __forceinline__ void sync_solve_warps() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+
+// One solve from the reduced sums (ICPTracker.cpp:78-131), executed by warps
+// 0 and 1. Lanes 2..22 of warp 0 store the information matrix; lane 0 of warp
+// 1 solves with the level's default damping and composes the pose it leads
+// to while lane 0 of warp 0 runs the damping test (two warps, so the two run
+// side by side rather than one after the other as divergent lanes of one
+// warp would), so in the usual case (no escalation) the test is off the
+// critical path; an escalated damping solves again on warp 0.
+__device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelState& st) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int inl = sm.isum[0];
+    const float base_damp = (level == 0) ? kDampingLevel0 : kDampingDefault;
+    const bool stop = (inl <= 0 || inl < kMinInliersForIteration);
+    if (warp == 1) {
+        if (lane == 0 && !stop) sm.spec_ok = step_pose(a, sm, st.pose, base_damp, sm.spec_pose, sm.spec_step) ? 1 : 0;
+        sync_solve_warps();
+        return;
+    }
+    if (!stop && lane >= 2 && lane < 23) {
+        const int k = lane - 2;  // upper-triangle entry k = (i, j), row by row
+        int i = 0, r = k;
+        while (r >= 6 - i) { r -= 6 - i; ++i; }
+        const int j = i + r;
+        const float v = sum_f(a, sm.sum, k);
+        st.information[i * 6 + j] = v;
+        st.information[j * 6 + i] = v;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        for (int k = 1; k < 6; ++k) st.counts[k] = sm.isum[k];
+        sm.action = stop ? 1 : 0;
+        if (!stop) {
+            // dampingForHessian (ICPShared.h:86-100) escalates when min_eig < 1e-4
+            // or max_eig > 1e7 min_eig. Since max_eig <= trace, min_eig >= sigma =
+            // max(1e-4, trace / 1e7) rules both out; A - sigma' I positive definite
+            // proves it, with sigma' = 2 sigma + 32 eps trace covering the
+            // rounding of the float factorisation. Only when that test fails do
+            // the eigenvalues decide.
+            float tr = 0.0f;
+            for (int i = 0; i < 6; ++i) tr += st.information[i * 6 + i];
+            const float sigma = fmaxf(kMinEigEscalate, tr / kCondEscalate);
+            const float shift = 2.0f * sigma + 32.0f * 1.1920929e-7f * tr;
+            sm.need_eig = (isfinite(tr) && pd_after_shift(st.information, shift)) ? 0 : 1;
+        }
+    }
+    sync_solve_warps();  // warp 1's step is done, and warp 0's test
+    if (sm.action != 0) return;
+    float mn = 1.0f, mx = 1.0f;
+    if (sm.need_eig) {
+        for (int i = lane; i < 36; i += 32) sm.m[i] = st.information[i];
+        __syncwarp();
+        warp_eig6(sm.m, sm.cs, mn, mx);
+    }
+    if (lane != 0) return;
+    float damp = base_damp;
+    if (sm.need_eig) {
+        if (!isfinite(mn) || !isfinite(mx) || mn < kMinEigEscalate) damp = kDampingEscalated;
+        else if (mx > kCondEscalate * mn) damp = kDampingEscalated;
+    }
+    float step_norm;
+    if (damp == base_damp) {
+        if (!sm.spec_ok) { sm.action = 1; return; }
+        for (int i = 0; i < 16; ++i) st.pose[i] = sm.spec_pose[i];
+        step_norm = sm.spec_step;
+    } else {
+        float P[16];
+        if (!step_pose(a, sm, st.pose, damp, P, step_norm)) { sm.action = 1; return; }
         for (int i = 0; i < 16; ++i) st.pose[i] = P[i];
     }
     st.final_step = step_norm;
@@ -1052,7 +1188,7 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
                 // iteration's partials never overwrite ones still being read).
                 grid_sync(a.bar, a.err, wl, gen);
                 reduce_grid(a, slot, sm.sum, sm.isum);
-                if (threadIdx.x < 32) solve_step(a, level, sm, st);
+                if (threadIdx.x < 64) solve_step(a, level, sm, st);
                 __syncthreads();
                 slot ^= 1;
                 if (sm.action != 0) break;
