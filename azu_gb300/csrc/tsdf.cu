@@ -281,8 +281,8 @@ __global__ void __launch_bounds__(256) integrate_bricks_kernel(
                 const float c2 = fmaf(R[6], px, fmaf(R[7], py, fmaf(R[8], pz, tz)));
                 zlo = fminf(zlo, c2);
                 zhi = fmaxf(zhi, c2);
-                const float iz = 1.0f / c2;
-                const float u = fmaf(fx * c0, iz, cx), v = fmaf(fy * c1, iz, cy);
+                // a bound: the approximate quotient (2 ulp) is covered by the margins below
+                const float u = __fdividef(fx * c0, c2) + cx, v = __fdividef(fy * c1, c2) + cy;
                 ulo = fminf(ulo, u);
                 uhi = fmaxf(uhi, u);
                 vlo = fminf(vlo, v);
@@ -456,7 +456,7 @@ __device__ __forceinline__ void integrate_item(
     F3 c = add3(mv3(R, add3(mk3(ox, oy, oz), mul3(mk3(float(x0), float(y), float(z)), vs))), t_wc);
     const float fW = static_cast<float>(W), fH = static_cast<float>(H);
     const float color_band = fm(0.5f, trunc);
-    unsigned long long n_new = 0, n_upd = 0, n_col = 0;
+    unsigned n_new = 0, n_upd = 0, n_col = 0;  // per lane: at most 32 rows x 32 chunks
     const size_t rr = static_cast<size_t>(res);
 
     // Conservative x-interval of this row that can land in front of the camera
@@ -624,6 +624,9 @@ __device__ __forceinline__ void integrate_item(
         // dependent load latencies overlap.
         const int x = xc + lane;
         const bool x_on = x >= x0 && x <= x1;
+        // voxel (x, ybase + r, z) = vrow + r * res
+        const size_t vrow =
+            (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase)) * rr + static_cast<size_t>(x);
         unsigned rem = live_rows;
         int ra[kUpdGroup], pa[kUpdGroup];
         float za[kUpdGroup], da[kUpdGroup];
@@ -679,13 +682,13 @@ __device__ __forceinline__ void integrate_item(
             float2 old[kUpdGroup];
 #pragma unroll
             for (int j = 0; j < kUpdGroup; ++j) {
-                const size_t v = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
+                const size_t v = vrow + static_cast<size_t>(rsel[j]) * rr;
                 if (pix[j] >= 0) old[j] = kResid ? VoxR::load_fold(vox, v) : Vox<kHalf>::load_rw(vox, v);
             }
 #pragma unroll
             for (int j = 0; j < kUpdGroup; ++j) {
                 if (pix[j] < 0) continue;
-                const size_t vi = (static_cast<size_t>(z) * rr + static_cast<size_t>(ybase + rsel[j])) * rr + x;
+                const size_t vi = vrow + static_cast<size_t>(rsel[j]) * rr;
                 // min(1, sdf / trunc) is exactly 1 for sdf >= trunc (a rounded
                 // quotient of operands in that order is >= 1): free space needs
                 // no division
@@ -724,12 +727,12 @@ __device__ __forceinline__ void integrate_item(
         n_col += __shfl_down_sync(0xffffffffu, n_col, o);
     }
     if (lane == 0) {
-        if (n_new) atomicAdd(&counters[0], n_new);
+        if (n_new) atomicAdd(&counters[0], static_cast<unsigned long long>(n_new));
         if (n_upd) {
-            atomicAdd(&counters[1], n_upd);
-            atomicAdd(&counters[3], n_upd);
+            atomicAdd(&counters[1], static_cast<unsigned long long>(n_upd));
+            atomicAdd(&counters[3], static_cast<unsigned long long>(n_upd));
         }
-        if (n_col) atomicAdd(&counters[2], n_col);
+        if (n_col) atomicAdd(&counters[2], static_cast<unsigned long long>(n_col));
     }
 }
 
@@ -793,7 +796,7 @@ __device__ __forceinline__ int brick_state(const VolView& v, const uint8_t* __re
 // in = 0 for a brick that is not free and kDistCap for a free one (the first
 // pass reads the flags) and kDistCap outside the grid. Three passes (x, y, z)
 // give the distance to the nearest non-free brick, capped.
-constexpr int kDistCap = 12;
+constexpr int kDistCap = 6;
 __device__ __forceinline__ void brick_dist_at(int x, int y, int z, const uint8_t* __restrict__ in,
                                               uint8_t* __restrict__ out, int nb, int axis, int from_flags) {
     const int b = (z * nb + y) * nb + x;  // nb <= 256: 32-bit

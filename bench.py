@@ -676,9 +676,11 @@ def run_gpu(args):
 
     launches = 0
     meshes = []
-    # warm-up (frame 0 builds the model; frame 1 captures the graph)
+    # warm-up (frame 0 builds the model; frame 1 captures the graph; one
+    # extraction sizes the mesher's buffers)
     for k in range(max(args.warmup, 3)):
         pl.process_frame_device(depth_ptr(k), d_rgb.data_ptr())
+    mc.extract_counts(vol)
     torch.cuda.synchronize(dev)
     frame = max(args.warmup, 3)
 
