@@ -9,7 +9,9 @@
 //   output         processed raw codes and band-gated metres (buildFrameData's
 //                  depth_meters) on the device
 // One kernel per stage; every stage is a stencil over the previous stage's
-// full output, so the stage boundary is the only synchronisation.
+// full output, so the stage boundary is the only synchronisation. The RGB
+// chain runs on a side stream beside the depth median and hole fill; the
+// guided filter, which reads the luma, waits for both.
 //
 // The exponentials whose arguments take a finite set of values come from
 // tables built on the host with the same libm call the CPU path makes, so
@@ -345,6 +347,10 @@ struct azu_preprocessor {
     float* d_depth_m = nullptr;
     float* d_range_w = nullptr;  // 195076
     float* d_dw = nullptr;       // 2047 x 2047
+    // The RGB chain runs on a side stream beside the depth median and hole
+    // fill (they meet at the guided filter, which reads the luma).
+    cudaStream_t s_rgb = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace azu {
@@ -378,13 +384,18 @@ static int build_tables(azu_preprocessor* p) {
 int preprocess_enqueue(azu_preprocessor* p, float lo, float hi, cudaStream_t s) {
     const dim3 b(32, 8), g(PW / 32, PH / 8);
     const bool full = p->mode == AZU_PRE_FULL;
-    // processCpu runs the RGB chain in both modes (SignalConditioner_omp.cpp:337-341).
-    rgb_bilateral_kernel<<<g, b, 0, s>>>(p->d_rgb_in, p->d_rgb_tmp, p->d_range_w);
-    rgb_median_kernel<<<g, b, 0, s>>>(p->d_rgb_tmp, p->d_rgb_out);
-    cas_luma_kernel<<<g, b, 0, s>>>(p->d_rgb_out, p->d_luma);
+    // processCpu runs the RGB chain in both modes (SignalConditioner_omp.cpp:337-341);
+    // it runs on the side stream, beside the depth median and hole fill.
+    AZU_TRY_CUDA(cudaEventRecord(p->ev_fork, s));
+    AZU_TRY_CUDA(cudaStreamWaitEvent(p->s_rgb, p->ev_fork, 0));
+    rgb_bilateral_kernel<<<g, b, 0, p->s_rgb>>>(p->d_rgb_in, p->d_rgb_tmp, p->d_range_w);
+    rgb_median_kernel<<<g, b, 0, p->s_rgb>>>(p->d_rgb_tmp, p->d_rgb_out);
+    cas_luma_kernel<<<g, b, 0, p->s_rgb>>>(p->d_rgb_out, p->d_luma);
+    AZU_TRY_CUDA(cudaEventRecord(p->ev_join, p->s_rgb));
     depth_median_kernel<<<dim3(PW / kMTx, PH / kMTy), dim3(kMTx, kMTy), 0, s>>>(p->d_in, p->d_a, lo, hi);
+    if (full) hole_fill_kernel<<<g, b, 0, s>>>(p->d_a, p->d_b, lo, hi);
+    AZU_TRY_CUDA(cudaStreamWaitEvent(s, p->ev_join, 0));
     if (full) {
-        hole_fill_kernel<<<g, b, 0, s>>>(p->d_a, p->d_b, lo, hi);
         guided_kernel<<<dim3(PW / kGTx, PH / kGTy), dim3(kGTx, kGTy), 0, s>>>(p->d_b, p->d_a, p->d_luma, p->d_dw,
                                                                            lo, hi);
     }
@@ -431,6 +442,9 @@ extern "C" int azu_preprocessor_create(int device, int mode, void* stream, azu_p
         if (!e) e = cudaMalloc(&p->d_depth_m, n * 4);
         if (!e) e = cudaMalloc(&p->d_range_w, kRangeN * sizeof(float));
         if (!e) e = cudaMalloc(&p->d_dw, sizeof(float) * kRawCodes * kRawCodes);
+        if (!e) e = cudaStreamCreateWithFlags(&p->s_rgb, cudaStreamNonBlocking);
+        if (!e) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
+        if (!e) e = cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming);
         if (e) { set_error("preprocessor allocation: %s", cudaGetErrorString(e)); rc = AZU_E_NOMEM; }
     }
     if (!rc) rc = build_tables(p);
@@ -444,6 +458,12 @@ extern "C" int azu_preprocessor_destroy(azu_preprocessor* p) {
     if (!p) return AZU_OK;
     cudaSetDevice(p->device);
     if (p->stream.s) cudaStreamSynchronize(p->stream.s);
+    if (p->s_rgb) {
+        cudaStreamSynchronize(p->s_rgb);
+        cudaStreamDestroy(p->s_rgb);
+    }
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->ev_join) cudaEventDestroy(p->ev_join);
     for (void* q : {(void*)p->d_in, (void*)p->d_a, (void*)p->d_b, (void*)p->d_out, (void*)p->d_rgb_in,
                     (void*)p->d_rgb_tmp, (void*)p->d_rgb_out, (void*)p->d_luma, (void*)p->d_ema, (void*)p->d_depth_m,
                     (void*)p->d_range_w, (void*)p->d_dw})
