@@ -98,16 +98,27 @@ struct WaitLimits {
     unsigned arrivals;  // arrivals that complete a barrier
 };
 
+// The arrival count (bar[0]) and the generation (bar[1]) are the two halves of
+// one 64-bit word (little-endian), so the last arrival resets the count and
+// advances the generation in a single atomic: adding 2^32 - arrivals takes the
+// count from `arrivals` to 0 with a carry into the generation. An arrival
+// releases the block's earlier stores and acquires the earlier arrivals' (the
+// last block reads every partial); waiters acquire the generation, which the
+// release sequence of every arrival on this word carries.
+__device__ __forceinline__ unsigned long long atom_add_acq_rel(unsigned long long* p, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.add.acq_rel.gpu.global.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
+
 __device__ void grid_sync(unsigned* bar, unsigned* err, WaitLimits wl, unsigned& gen) {
     __syncthreads();
     if (threadIdx.x == 0) {
         if (ld_acquire(err) == 0) {
-            __threadfence();
-            const unsigned arrived = atomicAdd(&bar[0], 1u);
-            if (arrived == wl.arrivals - 1) {
-                atomicExch(&bar[0], 0u);
-                __threadfence();
-                atomicAdd(&bar[1], 1u);
+            unsigned long long* word = reinterpret_cast<unsigned long long*>(bar);
+            const unsigned long long old = atom_add_acq_rel(word, 1ull);
+            if (static_cast<unsigned>(old) == wl.arrivals - 1) {
+                atom_add_acq_rel(word, (1ull << 32) - wl.arrivals);
             } else {
                 unsigned spins = 0;
                 while (ld_acquire(&bar[1]) == gen) {
@@ -115,12 +126,11 @@ __device__ void grid_sync(unsigned* bar, unsigned* err, WaitLimits wl, unsigned&
                         atomicExch(err, kDevErrBarrierTimeout);
                         break;
                     }
-                    __nanosleep(64);
+                    __nanosleep(32);
                 }
             }
         }
         gen += 1;
-        __threadfence();
     }
     __syncthreads();
 }
