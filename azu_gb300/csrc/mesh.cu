@@ -679,7 +679,9 @@ static int ensure_slots(azu_mesher* m, size_t nslots) {
     m->slot_key = nullptr; m->pos = m->nrm = nullptr;
     m->col = nullptr; m->first_slot = m->vid = nullptr; m->indices = nullptr;
     m->slots_cap = 0;
-    const size_t c = std::max<size_t>(nslots, 3 * 4096);
+    // half again the need: a growing scene's next extraction then reuses the
+    // buffers instead of freeing and allocating them (both stall the device)
+    const size_t c = std::max<size_t>(nslots + nslots / 2, 3 * 4096);
     AZU_TRY_CUDA(cudaMalloc(&m->slot_key, c * 8));
     AZU_TRY_CUDA(cudaMalloc(&m->first_slot, c * 4));
     AZU_TRY_CUDA(cudaMalloc(&m->vid, c * 4));
@@ -763,7 +765,7 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     if (int rc = grow(m->counts, m->counts_cap, static_cast<size_t>(ncubes) + 16)) return rc;
     if (int rc = grow(m->block_sums, m->blocks_cap, nblocks)) return rc;
     if (int rc = grow(m->scratch, m->scratch_cap, scan_scratch_words(std::max<size_t>(nblocks, 1 << 24)))) return rc;
-    // candidate list: a surface's share of the cubes, regrown to the exact need when it overflows
+    // candidate list: a surface's share of the cubes, regrown with headroom when it overflows
     if (int rc = ensure_active(m, std::max<size_t>(m->active_cap, std::min<size_t>(ncubes, std::max<size_t>(
                                                                         ncubes / 64, size_t(1) << 16)))))
         return rc;
@@ -792,7 +794,7 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
         if (sc4[3] <= acap) break;
         // more candidate cubes than the list holds: grow it to fit and run again
         if (attempt == 1) { set_error("candidate list overflow"); return AZU_E_CUDA; }
-        if (int rc = ensure_active(m, sc4[3])) return rc;
+        if (int rc = ensure_active(m, std::min<size_t>(ncubes, static_cast<size_t>(sc4[3]) + sc4[3] / 2))) return rc;
     }
     const unsigned total = sc4[0], n_active = sc4[3];
     const unsigned cap = static_cast<unsigned>(std::min<int64_t>(m->max_triangles, total));
