@@ -177,8 +177,9 @@ SIGNATURES = {
     "azu_batch_destroy": (C.c_int, [vp]),
     "azu_batch_process": (C.c_int, [vp, C.POINTER(vp), C.c_int, C.POINTER(FrameResult)]),
     "azu_batch_autotune": (C.c_int, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
-    "azu_batch_set_shapes": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
-    "azu_batch_get_shapes": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "azu_batch_set_shapes": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "azu_batch_get_shapes": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int)]),
     "azu_batch_volume": (vp, [vp, C.c_int]),
     "azu_batch_stream": (vp, [vp]),
     "azu_batch_uses_graph": (C.c_int, [vp]),

@@ -558,12 +558,15 @@ class Batch:
         return a.value, b.value
 
     def shapes(self):
-        w, rw, rh = C.c_int(), C.c_int(), C.c_int()
-        check(self.lib.azu_batch_get_shapes(self.h, C.byref(w), C.byref(rw), C.byref(rh)), "get_shapes")
-        return w.value, rw.value, rh.value
+        """(integrate warps per block, integrate x-parts per row, raycast tile w, h)."""
+        w, parts, rw, rh = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(self.lib.azu_batch_get_shapes(self.h, C.byref(w), C.byref(parts), C.byref(rw), C.byref(rh)),
+              "get_shapes")
+        return w.value, parts.value, rw.value, rh.value
 
-    def set_shapes(self, int_warps, ray_w, ray_h):
-        check(self.lib.azu_batch_set_shapes(self.h, int(int_warps), int(ray_w), int(ray_h)), "set_shapes")
+    def set_shapes(self, int_warps, int_parts, ray_w, ray_h):
+        check(self.lib.azu_batch_set_shapes(self.h, int(int_warps), int(int_parts), int(ray_w), int(ray_h)),
+              "set_shapes")
 
     def volume(self, i) -> TSDFVolume:
         return TSDFVolume.borrowed(self.lib.azu_batch_volume(self.h, i), self.params[i], self.device)

@@ -198,8 +198,8 @@ namespace azu {
 // Several volumes integrated / raycast with one launch per stage (FP32, no colour).
 int volume_batch_create(const PipelineFrameView* views, int n, azu_volume_batch** out);
 void volume_batch_destroy(azu_volume_batch* b);
-int volume_batch_set_shapes(azu_volume_batch* b, int int_warps, int ray_w, int ray_h);
-void volume_batch_shapes(const azu_volume_batch* b, int* int_warps, int* ray_w, int* ray_h);
+int volume_batch_set_shapes(azu_volume_batch* b, int int_warps, int int_parts, int ray_w, int ray_h);
+void volume_batch_shapes(const azu_volume_batch* b, int* int_warps, int* int_parts, int* ray_w, int* ray_h);
 int volume_batch_integrate(azu_volume_batch* b, cudaStream_t s);
 int volume_batch_raycast(azu_volume_batch* b, cudaStream_t s);
 }  // namespace azu

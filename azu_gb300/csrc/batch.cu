@@ -32,7 +32,7 @@ struct azu_batch {
     std::map<unsigned long long, azu_volume_batch*> vbatch;  // by active mask (first 64 scenes)
     std::map<unsigned long long, azu_icp_batch*> ibatch;
     std::map<unsigned long long, cudaGraphExec_t> graphs;
-    int int_warps = 4, ray_w = 32, ray_h = 8;
+    int int_warps = 4, int_parts = 2, ray_w = 32, ray_h = 8;
     bool tuned = false;
     bool use_graph = true;
     std::vector<azu_frame_result> host_results;
@@ -77,7 +77,7 @@ static int volume_batch_for(azu_batch* b, const std::vector<int>& active, azu_vo
     for (int i : active) views.push_back(pipeline_frame_view(b->scenes[i]));
     azu_volume_batch* vb = nullptr;
     if (int rc = volume_batch_create(views.data(), static_cast<int>(views.size()), &vb)) return rc;
-    if (int rc = volume_batch_set_shapes(vb, b->int_warps, b->ray_w, b->ray_h)) {
+    if (int rc = volume_batch_set_shapes(vb, b->int_warps, b->int_parts, b->ray_w, b->ray_h)) {
         volume_batch_destroy(vb);
         return rc;
     }
@@ -116,7 +116,7 @@ static void drop_graphs(azu_batch* b) {
 
 static int apply_shapes(azu_batch* b) {
     for (auto& v : b->vbatch)
-        if (int rc = volume_batch_set_shapes(v.second, b->int_warps, b->ray_w, b->ray_h)) return rc;
+        if (int rc = volume_batch_set_shapes(v.second, b->int_warps, b->int_parts, b->ray_w, b->ray_h)) return rc;
     drop_graphs(b);  // captured launches carry the old shapes
     return AZU_OK;
 }
@@ -213,23 +213,26 @@ extern "C" int azu_batch_create(int device, int n, const azu_batch_scene* scenes
     return AZU_OK;
 }
 
-extern "C" int azu_batch_set_shapes(azu_batch* b, int int_warps, int ray_w, int ray_h) {
+extern "C" int azu_batch_set_shapes(azu_batch* b, int int_warps, int int_parts, int ray_w, int ray_h) {
     AZU_CHECK_ARG(b != nullptr, "null handle");
     AZU_CHECK_ARG(int_warps == 1 || int_warps == 2 || int_warps == 4, "integrate warps per block: 1, 2 or 4");
+    AZU_CHECK_ARG(int_parts == 1 || int_parts == 2 || int_parts == 4, "integrate x-parts per row: 1, 2 or 4");
     AZU_CHECK_ARG(ray_w >= 8 && ray_h >= 1 && ray_w * ray_h <= 256 && (ray_w * ray_h) % 32 == 0,
                   "raycast tile: at most 256 threads, whole warps");
     AZU_TRY_CUDA(cudaSetDevice(b->device));
     AZU_TRY_CUDA(cudaStreamSynchronize(b->s));
     b->int_warps = int_warps;
+    b->int_parts = int_parts;
     b->ray_w = ray_w;
     b->ray_h = ray_h;
     b->tuned = true;
     return apply_shapes(b);
 }
 
-extern "C" int azu_batch_get_shapes(azu_batch* b, int* int_warps, int* ray_w, int* ray_h) {
+extern "C" int azu_batch_get_shapes(azu_batch* b, int* int_warps, int* int_parts, int* ray_w, int* ray_h) {
     AZU_CHECK_ARG(b != nullptr, "null handle");
     if (int_warps) *int_warps = b->int_warps;
+    if (int_parts) *int_parts = b->int_parts;
     if (ray_w) *ray_w = b->ray_w;
     if (ray_h) *ray_h = b->ray_h;
     return AZU_OK;
@@ -250,7 +253,7 @@ extern "C" int azu_batch_autotune(azu_batch* b, float* best_integrate_ms, float*
     float best_r = 1e30f;
     int bw = b->ray_w, bh = b->ray_h;
     for (const auto& t : tiles) {
-        if (int rc = volume_batch_set_shapes(vb, b->int_warps, t[0], t[1])) return rc;
+        if (int rc = volume_batch_set_shapes(vb, b->int_warps, b->int_parts, t[0], t[1])) return rc;
         float ms = 0.0f;
         if (int rc = time_ms(b->s, &ms, [&] { return volume_batch_raycast(vb, b->s); }, 5)) return rc;
         if (ms < best_r) { best_r = ms; bw = t[0]; bh = t[1]; }
@@ -280,15 +283,18 @@ extern "C" int azu_batch_autotune(azu_batch* b, float* best_integrate_ms, float*
         }
         return AZU_OK;
     };
+    // integrate item shapes: warps per block x x-parts per 32-row item
     float best_i = 1e30f;
-    int bwarps = b->int_warps;
+    int bwarps = b->int_warps, bparts = b->int_parts;
     for (int warps : {1, 2, 4}) {
-        if (rc) break;
-        rc = volume_batch_set_shapes(vb, warps, bw, bh);
-        float ms = 0.0f;
-        if (!rc) rc = time_ms(b->s, &ms, [&] { return volume_batch_integrate(vb, b->s); }, 3);
-        if (!rc) rc = restore();
-        if (!rc && ms < best_i) { best_i = ms; bwarps = warps; }
+        for (int parts : {1, 2, 4}) {
+            if (rc) break;
+            rc = volume_batch_set_shapes(vb, warps, parts, bw, bh);
+            float ms = 0.0f;
+            if (!rc) rc = time_ms(b->s, &ms, [&] { return volume_batch_integrate(vb, b->s); }, 3);
+            if (!rc) rc = restore();
+            if (!rc && ms < best_i) { best_i = ms; bwarps = warps; bparts = parts; }
+        }
     }
     // integrations changed counters and free-brick flags: recompute flags from
     // the restored voxels (conservative flags stay exact for the raycast)
@@ -305,6 +311,7 @@ extern "C" int azu_batch_autotune(azu_batch* b, float* best_integrate_ms, float*
     }
     if (rc) return rc;
     b->int_warps = bwarps;
+    b->int_parts = bparts;
     b->ray_w = bw;
     b->ray_h = bh;
     b->tuned = true;

@@ -1184,12 +1184,13 @@ __global__ void integrate_setup_batch_kernel(const IntegrateArgs* __restrict__ A
     if (blockIdx.x == 0 && threadIdx.x == 0) *work = 0;  // next item of the batch integrate
 }
 
-// Persistent over the items of all scenes (32 rows x half a row each, scene by
-// prefix offsets): every warp takes the next item from the batch's counter.
+// Persistent over the items of all scenes (32 rows x one of nparts x-parts of a
+// row each, scene by prefix offsets): every warp takes the next item from the
+// batch's counter.
 template <int kWarps>
 __global__ void __launch_bounds__(kWarps * 32) integrate_batch_kernel(const IntegrateArgs* __restrict__ A,
                                                                       const int* __restrict__ off, int n,
-                                                                      unsigned* __restrict__ work) {
+                                                                      unsigned* __restrict__ work, int nparts) {
     __shared__ float s_c[kWarps][3][32][33];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int total = __ldg(off + n);
@@ -1203,7 +1204,7 @@ __global__ void __launch_bounds__(kWarps * 32) integrate_batch_kernel(const Inte
         integrate_item<false, false, false>(a.vox, nullptr, a.icp, a.depth, nullptr, a.res, a.vs, a.ox, a.oy, a.oz,
                                             a.trunc, a.max_w, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.min_d, a.max_d,
                                             a.gate, a.counters, a.bricks, a.nb, a.tiles, a.mip, item - __ldg(off + s),
-                                            warp, lane, s_c, kIntParts);
+                                            warp, lane, s_c, nparts);
     }
 }
 
@@ -1239,7 +1240,7 @@ struct azu_volume_batch {
     unsigned* d_work = nullptr;  // next integrate item
     int tiles_blocks = 0, items = 0, brick_blocks = 0, ray_blocks = 0;
     int int_grid[3] = {0, 0, 0};  // resident blocks of the persistent integrate, by 1, 2, 4 warps
-    int int_warps = 4, ray_w = 32, ray_h = 8;
+    int int_warps = 4, int_parts = azu::kIntParts, ray_w = 32, ray_h = 8;
 };
 
 namespace azu {
@@ -1255,7 +1256,7 @@ static int batch_upload_offsets(azu_volume_batch* b) {
         tb += (mip.w[0] * mip.h[0] + 31) / 32;
         off[n + 1 + i] = it;
         const int res = f.vol->p.resolution;
-        it += res * ((res + 31) / 32) * kIntParts;
+        it += res * ((res + 31) / 32) * b->int_parts;
         off[2 * (n + 1) + i] = bb;
         const size_t nbr = static_cast<size_t>(f.vol->nb) * f.vol->nb * f.vol->nb;
         bb += static_cast<int>((nbr + 255) / 256);
@@ -1336,18 +1337,21 @@ void volume_batch_destroy(azu_volume_batch* b) {
     delete b;
 }
 
-int volume_batch_set_shapes(azu_volume_batch* b, int int_warps, int ray_w, int ray_h) {
+int volume_batch_set_shapes(azu_volume_batch* b, int int_warps, int int_parts, int ray_w, int ray_h) {
     AZU_CHECK_ARG(int_warps == 1 || int_warps == 2 || int_warps == 4, "integrate warps per block: 1, 2 or 4");
+    AZU_CHECK_ARG(int_parts == 1 || int_parts == 2 || int_parts == 4, "integrate x-parts per row: 1, 2 or 4");
     AZU_CHECK_ARG(ray_w >= 8 && ray_h >= 1 && ray_w * ray_h <= 256 && (ray_w * ray_h) % 32 == 0,
                   "raycast tile: at most 256 threads, whole warps");
     b->int_warps = int_warps;
+    b->int_parts = int_parts;
     b->ray_w = ray_w;
     b->ray_h = ray_h;
     return batch_upload_offsets(b);
 }
 
-void volume_batch_shapes(const azu_volume_batch* b, int* int_warps, int* ray_w, int* ray_h) {
+void volume_batch_shapes(const azu_volume_batch* b, int* int_warps, int* int_parts, int* ray_w, int* ray_h) {
     if (int_warps) *int_warps = b->int_warps;
+    if (int_parts) *int_parts = b->int_parts;
     if (ray_w) *ray_w = b->ray_w;
     if (ray_h) *ray_h = b->ray_h;
 }
@@ -1361,9 +1365,10 @@ int volume_batch_integrate(azu_volume_batch* b, cudaStream_t s) {
     const int* ioff = b->d_off + (n + 1);
     const int k = b->int_warps == 1 ? 0 : (b->int_warps == 2 ? 1 : 2);
     const int blocks = std::min(b->int_grid[k], (b->items + b->int_warps - 1) / b->int_warps);
-    if (b->int_warps == 1) integrate_batch_kernel<1><<<blocks, 32, 0, s>>>(b->d_int, ioff, n, b->d_work);
-    else if (b->int_warps == 2) integrate_batch_kernel<2><<<blocks, 64, 0, s>>>(b->d_int, ioff, n, b->d_work);
-    else integrate_batch_kernel<4><<<blocks, 128, 0, s>>>(b->d_int, ioff, n, b->d_work);
+    const int P = b->int_parts;
+    if (b->int_warps == 1) integrate_batch_kernel<1><<<blocks, 32, 0, s>>>(b->d_int, ioff, n, b->d_work, P);
+    else if (b->int_warps == 2) integrate_batch_kernel<2><<<blocks, 64, 0, s>>>(b->d_int, ioff, n, b->d_work, P);
+    else integrate_batch_kernel<4><<<blocks, 128, 0, s>>>(b->d_int, ioff, n, b->d_work, P);
     AZU_LAUNCH_CHECK();
     for (const PipelineFrameView& f : b->views) f.vol->integrated_frames++;
     return AZU_OK;

@@ -486,7 +486,8 @@ def run_batch_form(dev, n_scenes: int, frames_scale: float):
             "batch_frames_per_s": frames_timed / t_batch,
             "single_pipelines_frames_per_s": total / t_single,
             "speedup": (frames_timed / t_batch) / (total / t_single),
-            "autotuned": {"integrate_warps": shapes[0], "raycast_tile": [shapes[1], shapes[2]],
+            "autotuned": {"integrate_warps": shapes[0], "integrate_x_parts": shapes[1],
+                          "raycast_tile": [shapes[2], shapes[3]],
                           "integrate_ms": t_int, "raycast_ms": t_ray},
             "per_scene_bit_exact_vs_single": exact,
             "timing": "host wall clock around device-resident steps (steps 2.. after autotune) and around each "

@@ -483,11 +483,12 @@ int azu_batch_destroy(azu_batch* b);
  * one launch per stage, and steps replay one CUDA graph per active set.
  * results (n entries, optional) receive the active scenes' results (sync). */
 int azu_batch_process(azu_batch* b, const uint16_t* const* depth_mm, int on_device, azu_frame_result* results);
-/* Times the integrate block sizes and raycast tile shapes on the batch's own
- * data (after at least one step) and keeps the fastest; results unchanged. */
+/* Times the integrate item shapes (warps per block 1, 2, 4 x x-parts per
+ * 32-row item 1, 2, 4) and raycast tile shapes on the batch's own data (after
+ * at least one step) and keeps the fastest; results unchanged. */
 int azu_batch_autotune(azu_batch* b, float* best_integrate_ms, float* best_raycast_ms);
-int azu_batch_set_shapes(azu_batch* b, int int_warps, int ray_w, int ray_h);
-int azu_batch_get_shapes(azu_batch* b, int* int_warps, int* ray_w, int* ray_h);
+int azu_batch_set_shapes(azu_batch* b, int int_warps, int int_parts, int ray_w, int ray_h);
+int azu_batch_get_shapes(azu_batch* b, int* int_warps, int* int_parts, int* ray_w, int* ray_h);
 azu_volume* azu_batch_volume(azu_batch* b, int i);
 void* azu_batch_stream(azu_batch* b);
 int azu_batch_uses_graph(azu_batch* b);

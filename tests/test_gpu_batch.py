@@ -60,8 +60,8 @@ def test_batch_equals_single_pipelines(cuda_lib, scenes):
         t, w = b.volume(i).download()
         assert np.array_equal(w, ref[i][2]), i
         assert np.array_equal(t.view(np.uint32), ref[i][1].view(np.uint32)), i
-    iw, rw, rh = b.shapes()
-    assert iw in (1, 2, 4) and rw * rh <= 256
+    iw, parts, rw, rh = b.shapes()
+    assert iw in (1, 2, 4) and parts in (1, 2, 4) and rw * rh <= 256
     b.close()
 
 

@@ -2,7 +2,8 @@
 parsed and paired by the rules of the reference's sensor (depth-led, nearest
 RGB within 17 ms of the 60 MHz counter, counter wrap), payloads read exactly;
 on a GPU, frames through the pinned read-ahead ring and the single-copy input
-give the pipeline the results of the plain host input."""
+give the pipeline the results of the plain host input and of the lockstep
+oracle."""
 import os
 
 import numpy as np
@@ -100,7 +101,12 @@ def test_missing_index_is_an_error(tmp_path):
 
 
 @pytest.mark.gpu
-def test_ring_and_single_copy_input_match_host_input(cuda_lib, tmp_path):
+def test_ring_and_single_copy_input_match_host_input(cuda_lib, orc, tmp_path):
+    """Frames through the recording ingest (pinned read-ahead ring, one
+    host-to-device copy of depth | RGB per frame) give the pipeline the poses of
+    the plain host input bit for bit, and the grades, fusion decisions and poses
+    (within 5e-4) of the lockstep oracle fed the same raw codes and RGB."""
+    import fixtures as F
     from azu_gb300 import api, synth
     s = synth.sequence("c1", frames=8)
     raw = [synth.encode_raw(d, s.min_depth, s.max_depth) for d in s.depth_mm]
@@ -121,6 +127,7 @@ def test_ring_and_single_copy_input_match_host_input(cuda_lib, tmp_path):
     rec = api.Recording(tmp_path)
     assert len(rec) == len(raw)
     ing = api.Ingest(rec, slots=3)
+    L = orc.Lockstep(s.volume, input_is_mm=False, min_depth=s.min_depth, max_depth=s.max_depth, fold_threads=0)
     for k in range(len(raw)):
         got = ing.next()
         assert got is not None and got[1] == k and got[2]
@@ -128,6 +135,10 @@ def test_ring_and_single_copy_input_match_host_input(cuda_lib, tmp_path):
         ing.release()
         rb = b.process_frame(raw[k], rgb)
         assert np.array_equal(ra["pose"].view(np.uint32), rb["pose"].view(np.uint32)), k
+        o = L.process(raw[k], rgb)
+        assert (ra["quality"], ra["integrated"]) == (o["quality"], o["integrated"]), k
+        rot, trans = F.rel_pose_error(ra["pose"], o["pose"])
+        assert rot <= 5e-4 and trans <= 5e-4, (k, rot, trans)
     assert ing.next() is None
     ing.close()
     rec.close()
