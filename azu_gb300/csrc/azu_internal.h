@@ -126,6 +126,12 @@ struct azu_volume {
     uint8_t* brick_tmp = nullptr;
     int nb = 0;
     bool skip_free = true;
+    // Ray start map of the raycast: per 8x8 pixel tile a lower bound of the
+    // distance from the camera to every brick that is not free and projects
+    // into the tile (float bits, atomicMin), then one word that bounds every
+    // tile (bricks across the camera plane).
+    uint32_t* ray_start = nullptr;
+    size_t ray_start_cap = 0;
     // Deepest in-band depth per 8x8 pixel tile of the frame being integrated.
     float* d_tiles = nullptr;
     size_t tile_cap = 0;

@@ -379,6 +379,9 @@ __global__ void __launch_bounds__(256) integrate_list_kernel(const IntegrateCons
 // fs_walk kept out of line (it runs once per item, not per voxel).
 __device__ __noinline__ float fs_walk_far(float v, float s, int n) { return fs_walk(v, s, n); }
 
+// A hint to load the 128-byte line holding p into L2 (p must be a valid address).
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // Voxel-projective integration (TSDFVolume.cpp:282-329).
 //
 // The CPU steps the camera coordinate of a voxel row incrementally along x
@@ -587,6 +590,17 @@ __device__ __forceinline__ void integrate_item(
         }
         const unsigned live_rows = __ballot_sync(0xffffffffu, live);
         if (!live_rows) continue;  // c stays at xat; the next chunk's jump covers this one
+        if (live) {
+            // pull the row's voxel records of this chunk into L2 now: the
+            // update reads them after the chain, so their DRAM latency overlaps
+            // it (4% of the stage on c2)
+            const size_t rbase = (static_cast<size_t>(z) * rr + static_cast<size_t>(y)) * rr;
+            const size_t es = (kHalf || kResid) ? 4 : 8;
+            const char* pa = static_cast<const char*>(vox) + (rbase + max(xc, x0)) * es;
+            const char* pb = static_cast<const char*>(vox) + (rbase + min(xc + 31, x1)) * es;
+            prefetch_l2(pa);
+            if ((reinterpret_cast<uintptr_t>(pa) >> 7) != (reinterpret_cast<uintptr_t>(pb) >> 7)) prefetch_l2(pb);
+        }
         // chain (lane = row): the sequential c-steps of the chunk
         if (row_on) {
             if (xc >= x0 && xc + 31 <= x1) {
@@ -833,6 +847,130 @@ __global__ void __launch_bounds__(64) brick_dist_kernel(const uint8_t* __restric
     brick_dist_at(x, blockIdx.y, blockIdx.z, in, out, nb, axis, from_flags);
 }
 
+// Ray start map. A march sample whose base voxel lies in a free brick, or
+// outside the grid, is skipped, so a ray's far steps are skipped up to the
+// first sample in a brick that is not free. Every such brick B (base voxels
+// [8B, 8B + 8) a side, its box widened by 0.01 voxel, far above the rounding
+// of sample positions) bounds that sample from below: a ray through a pixel
+// meets B's box only if the pixel lies in the box's projection, and then not
+// before the camera-to-box distance. One thread per brick (the grid of
+// brick_dist_kernel) takes the projection of B's 8 corners, widened by a pixel,
+// and lowers the distance bound of every 8x8 pixel tile the projection covers;
+// a box that reaches within 1 mm of the camera plane (its projection is
+// unbounded) lowers the bound of every tile instead. Bounds are distances less
+// 1e-5 relative and 0.1 mm; the raycast keeps two more far steps of margin.
+constexpr int kStartShift = 3;  // 8x8 pixel tiles
+struct StartMapArgs {
+    float vs;
+    F3 origin;
+    const float* pose;  // camera to world, row-major 4x4
+    float fx, fy, cx, cy;
+    int W, H;
+    uint32_t* smap;
+};
+__device__ __forceinline__ void ray_start_brick(const StartMapArgs& a, int bx, int by, int bz) {
+    float R[9];
+    R[0] = __ldg(a.pose + 0); R[1] = __ldg(a.pose + 1); R[2] = __ldg(a.pose + 2);
+    R[3] = __ldg(a.pose + 4); R[4] = __ldg(a.pose + 5); R[5] = __ldg(a.pose + 6);
+    R[6] = __ldg(a.pose + 8); R[7] = __ldg(a.pose + 9); R[8] = __ldg(a.pose + 10);
+    const float co[3] = {__ldg(a.pose + 3), __ldg(a.pose + 7), __ldg(a.pose + 11)};
+    const float mg = 0.01f * a.vs, side = 8.0f * a.vs;
+    const int b[3] = {bx, by, bz};
+    const float o[3] = {a.origin.x, a.origin.y, a.origin.z};
+    float lo[3], hi[3], d2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = o[k] + side * static_cast<float>(b[k]) - mg - co[k];  // relative to the camera centre
+        hi[k] = o[k] + side * static_cast<float>(b[k] + 1) + mg - co[k];
+        const float g = fmaxf(fmaxf(lo[k], -hi[k]), 0.0f);
+        d2 += g * g;
+    }
+    const float bound = fmaxf(sqrtf(d2) * (1.0f - 1e-5f) - 1e-4f, 0.0f);
+    const uint32_t key = isfinite(bound) ? __float_as_uint(bound) : 0u;
+    float umin = __int_as_float(0x7f800000), umax = -umin, vmin = umin, vmax = -umin;
+    int front = 0, near_plane = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float px = (k & 1) ? hi[0] : lo[0], py = (k & 2) ? hi[1] : lo[1], pz = (k & 4) ? hi[2] : lo[2];
+        // camera coordinates R^T (P - c)
+        const float xc = R[0] * px + R[3] * py + R[6] * pz;
+        const float yc = R[1] * px + R[4] * py + R[7] * pz;
+        const float zc = R[2] * px + R[5] * py + R[8] * pz;
+        front += zc > -1e-3f;
+        if (!(zc >= 1e-3f)) {
+            near_plane = 1;
+            continue;
+        }
+        const float u = a.fx * (xc / zc) + a.cx, w = a.fy * (yc / zc) + a.cy;
+        umin = fminf(umin, u); umax = fmaxf(umax, u);
+        vmin = fminf(vmin, w); vmax = fmaxf(vmax, w);
+    }
+    if (!front) return;  // wholly behind the camera: no ray reaches it
+    const int tw = (a.W + (1 << kStartShift) - 1) >> kStartShift, th = (a.H + (1 << kStartShift) - 1) >> kStartShift;
+    if (near_plane) {
+        atomicMin(a.smap + tw * th, key);
+        return;
+    }
+    if (!(umax >= -1.0f && umin <= static_cast<float>(a.W) && vmax >= -1.0f && vmin <= static_cast<float>(a.H))) return;
+    // tile ranges as floats first: NaNs and huge values clamp to the image
+    const float sc = 1.0f / static_cast<float>(1 << kStartShift);
+    const int tx0 = static_cast<int>(fmaxf(floorf((umin - 1.0f) * sc), 0.0f));
+    const int tx1 = static_cast<int>(fminf(floorf((umax + 1.0f) * sc), static_cast<float>(tw - 1)));
+    const int ty0 = static_cast<int>(fmaxf(floorf((vmin - 1.0f) * sc), 0.0f));
+    const int ty1 = static_cast<int>(fminf(floorf((vmax + 1.0f) * sc), static_cast<float>(th - 1)));
+    for (int ty = ty0; ty <= ty1; ++ty)
+        for (int tx = tx0; tx <= tx1; ++tx) atomicMin(a.smap + ty * tw + tx, key);
+}
+
+// The raycast's brick field in one launch: the three passes of the capped
+// distance transform (brick_dist_at, the same values) run in shared memory over
+// an 8^3 block of bricks and its halo of kDistCap - 1 bricks, and the block's
+// bricks that are not free lower the ray start map.
+constexpr int kFieldSide = 8, kFieldHalo = kDistCap - 1, kFieldExt = kFieldSide + 2 * kFieldHalo;
+__global__ void __launch_bounds__(512) brick_field_kernel(const uint8_t* __restrict__ flags, uint8_t* __restrict__ dist,
+                                                          int nb, StartMapArgs sm, const int* __restrict__ gate) {
+    __shared__ uint8_t s_in[kFieldExt][kFieldExt][kFieldExt];    // [z][y][x]: 0 not free, kDistCap free or outside
+    __shared__ uint8_t s_x[kFieldExt][kFieldExt][kFieldSide];    // after the x pass
+    __shared__ uint8_t s_y[kFieldExt][kFieldSide][kFieldSide];   // after the y pass
+    if (gate && __ldg(gate) == 0) return;
+    const int x0 = blockIdx.x * kFieldSide - kFieldHalo, y0 = blockIdx.y * kFieldSide - kFieldHalo,
+              z0 = blockIdx.z * kFieldSide - kFieldHalo;
+    for (int i = threadIdx.x; i < kFieldExt * kFieldExt * kFieldExt; i += blockDim.x) {
+        const int lx = i % kFieldExt, ly = (i / kFieldExt) % kFieldExt, lz = i / (kFieldExt * kFieldExt);
+        const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
+        uint8_t val = kDistCap;
+        if (gx >= 0 && gx < nb && gy >= 0 && gy < nb && gz >= 0 && gz < nb)
+            val = __ldg(flags + (static_cast<size_t>(gz) * nb + gy) * nb + gx) ? kDistCap : 0;
+        s_in[lz][ly][lx] = val;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kFieldExt * kFieldExt * kFieldSide; i += blockDim.x) {
+        const int lx = i % kFieldSide, ly = (i / kFieldSide) % kFieldExt, lz = i / (kFieldSide * kFieldExt);
+        int d = kDistCap;
+#pragma unroll
+        for (int k = -kFieldHalo; k <= kFieldHalo; ++k) d = min(d, max(abs(k), int(s_in[lz][ly][lx + kFieldHalo + k])));
+        s_x[lz][ly][lx] = static_cast<uint8_t>(d);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kFieldExt * kFieldSide * kFieldSide; i += blockDim.x) {
+        const int lx = i % kFieldSide, ly = (i / kFieldSide) % kFieldSide, lz = i / (kFieldSide * kFieldSide);
+        int d = kDistCap;
+#pragma unroll
+        for (int k = -kFieldHalo; k <= kFieldHalo; ++k) d = min(d, max(abs(k), int(s_x[lz][ly + kFieldHalo + k][lx])));
+        s_y[lz][ly][lx] = static_cast<uint8_t>(d);
+    }
+    __syncthreads();
+    const int lx = threadIdx.x % kFieldSide, ly = (threadIdx.x / kFieldSide) % kFieldSide,
+              lz = threadIdx.x / (kFieldSide * kFieldSide);
+    const int gx = x0 + kFieldHalo + lx, gy = y0 + kFieldHalo + ly, gz = z0 + kFieldHalo + lz;
+    if (lz >= kFieldSide || gx >= nb || gy >= nb || gz >= nb) return;
+    int d = kDistCap;
+#pragma unroll
+    for (int k = -kFieldHalo; k <= kFieldHalo; ++k) d = min(d, max(abs(k), int(s_y[lz + kFieldHalo + k][ly][lx])));
+    dist[(static_cast<size_t>(gz) * nb + gy) * nb + gx] = static_cast<uint8_t>(d);
+    if (sm.smap && s_in[lz + kFieldHalo][ly + kFieldHalo][lx + kFieldHalo] == 0) ray_start_brick(sm, gx, gy, gz);
+}
+
 // Fast-forward through free space. From a sample t whose brick b has free
 // distance r + 1, every brick of the cube b +- r is free, and the march takes
 // far steps t_k = t + k step (each sum rounded) whose samples in the cube are
@@ -891,7 +1029,8 @@ __device__ __forceinline__ void raycast_pixel(const VolView& v, const float* __r
                                               float cx, float cy, int W, int H, float trunc, float min_depth,
                                               float max_depth, float* __restrict__ vout, float* __restrict__ nout,
                                               uint8_t* __restrict__ cout, const int* __restrict__ gate,
-                                              const uint8_t* __restrict__ bdist, int nb, int x, int y) {
+                                              const uint8_t* __restrict__ bdist, int nb, int x, int y,
+                                              const uint32_t* __restrict__ smap = nullptr) {
     if (gate && __ldg(gate) == 0) return;
     if (x >= W || y >= H) return;
     const int o = y * W + x;
@@ -946,6 +1085,20 @@ __device__ __forceinline__ void raycast_pixel(const VolView& v, const float* __r
         // Such samples are not evaluated; the march keeps the same t sequence, and
         // the last skipped sample is evaluated when the state is needed again.
         bool skipped = false;
+        if (smap && (!prev_valid || f_prev >= 0.999f)) {
+            // every sample below the tile's start bound is skipped: take the far
+            // steps that stay two steps short of it (and of t_far) at once, by
+            // the closed form of the running sum
+            const int tw = (W + (1 << kStartShift) - 1) >> kStartShift;
+            const int th = (H + (1 << kStartShift) - 1) >> kStartShift;
+            const float ts = fminf(__uint_as_float(__ldg(smap + (y >> kStartShift) * tw + (x >> kStartShift))),
+                                   __uint_as_float(__ldg(smap + tw * th)));
+            const float n = floorf((fminf(ts, t_far) - t_near) / far_step) - 2.0f;
+            if (n >= 1.0f) {
+                t_prev = fs_walk_far(t_near, far_step, static_cast<int>(fminf(n, 1e8f)));
+                skipped = true;
+            }
+        }
         while (t_prev < t_far) {
             float step;
             if (skipped || !prev_valid || f_prev >= 0.999f) {
@@ -1028,9 +1181,9 @@ __global__ void __launch_bounds__(128, 10) raycast_kernel(VolView v, const float
                                                      float min_depth, float max_depth, float* __restrict__ vout,
                                                      float* __restrict__ nout, uint8_t* __restrict__ cout,
                                                      const int* __restrict__ gate, const uint8_t* __restrict__ bdist,
-                                                     int nb) {
+                                                     int nb, const uint32_t* __restrict__ smap) {
     raycast_pixel<kHalf>(v, d_pose, fx, fy, cx, cy, W, H, trunc, min_depth, max_depth, vout, nout, cout, gate, bdist,
-                         nb, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+                         nb, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, smap);
 }
 
 // ---- global point cloud (TSDFVolume.cpp:571-632) --------------------------------
@@ -1427,6 +1580,23 @@ int set_pose_async(float* d_pose, const float* pose, cudaStream_t s) {
 
 // Depth-tile buffer with room for n tiles. Grows outside stream capture only;
 // volumes are created with room for a 640x480 image.
+static int ensure_ray_start(azu_volume* v, size_t n, cudaStream_t s) {
+    if (n <= v->ray_start_cap) return AZU_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    AZU_TRY_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) {
+        set_error("raycast: image larger than the ray start map during stream capture");
+        return AZU_E_STATE;
+    }
+    AZU_TRY_CUDA(cudaStreamSynchronize(s));
+    if (v->ray_start) cudaFree(v->ray_start);
+    v->ray_start = nullptr;
+    v->ray_start_cap = 0;
+    AZU_TRY_CUDA(cudaMalloc(&v->ray_start, n * sizeof(uint32_t)));
+    v->ray_start_cap = n;
+    return AZU_OK;
+}
+
 static int ensure_tiles(azu_volume* v, size_t n, cudaStream_t s) {
     if (n <= v->tile_cap) return AZU_OK;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1535,22 +1705,27 @@ int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, f
     // 32 x 1 row: 6% faster than 16 x 8 blocks, 9% than 32 x 8)
     const dim3 blk(8, 16), grd((W + 7) / 8, (H + 15) / 16);
     const uint8_t* bricks = nullptr;
+    const uint32_t* smap = nullptr;
     if (v->skip_free) {
-        const dim3 g((v->nb + 63) / 64, v->nb, v->nb);
-        brick_dist_kernel<<<g, 64, 0, s>>>(v->bricks, v->brick_dist, v->nb, 0, 1, d_gate);
-        brick_dist_kernel<<<g, 64, 0, s>>>(v->brick_dist, v->brick_tmp, v->nb, 1, 0, d_gate);
-        brick_dist_kernel<<<g, 64, 0, s>>>(v->brick_tmp, v->brick_dist, v->nb, 2, 0, d_gate);
+        const size_t nst = static_cast<size_t>((W + (1 << kStartShift) - 1) >> kStartShift) *
+                               ((H + (1 << kStartShift) - 1) >> kStartShift) + 1;
+        if (int rc = ensure_ray_start(v, nst, s)) return rc;
+        AZU_TRY_CUDA(cudaMemsetAsync(v->ray_start, 0x7f, nst * sizeof(uint32_t), s));  // 3.4e38: no bound
+        const int gb = (v->nb + kFieldSide - 1) / kFieldSide;
+        const StartMapArgs sm{p.voxel_size, view.origin, d_pose, fx, fy, cx, cy, W, H, v->ray_start};
+        brick_field_kernel<<<dim3(gb, gb, gb), 512, 0, s>>>(v->bricks, v->brick_dist, v->nb, sm, d_gate);
         AZU_LAUNCH_CHECK();
         bricks = v->brick_dist;
+        smap = v->ray_start;
     }
     if (p.format != AZU_TSDF_FP32)
         raycast_kernel<true><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
                                                   p.max_depth, d_vertices, d_normals, d_colors, d_gate, bricks,
-                                                  v->nb);
+                                                  v->nb, smap);
     else
         raycast_kernel<false><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
                                                    p.max_depth, d_vertices, d_normals, d_colors, d_gate, bricks,
-                                                   v->nb);
+                                                   v->nb, smap);
     AZU_LAUNCH_CHECK();
     return AZU_OK;
 }
@@ -1568,6 +1743,11 @@ static int volume_alloc(azu_volume* v) {
     {
         const size_t n_items = static_cast<size_t>(v->p.resolution) * ((v->p.resolution + 31) / 32) * kIntParts;
         AZU_TRY_CUDA(cudaMalloc(&v->int_list, n_items * kIntBuckets * sizeof(int)));
+    }
+    if (!v->ray_start) {  // a 640 x 480 image; larger ones grow it outside stream capture
+        const size_t n = static_cast<size_t>(80 * 60 + 1);
+        AZU_TRY_CUDA(cudaMalloc(&v->ray_start, n * sizeof(uint32_t)));
+        v->ray_start_cap = n;
     }
     if (!v->d_tiles) {
         const size_t n = static_cast<size_t>(make_tile_mip(640, 480).total);
@@ -1662,6 +1842,7 @@ extern "C" int azu_volume_destroy(azu_volume* v) {
     if (v->d_depth_stage) cudaFree(v->d_depth_stage);
     if (v->d_rgb_stage) cudaFree(v->d_rgb_stage);
     if (v->d_tiles) cudaFree(v->d_tiles);
+    if (v->ray_start) cudaFree(v->ray_start);
     if (v->d_diff) cudaFree(v->d_diff);
     v->stream.release();
     delete v;

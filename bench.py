@@ -46,7 +46,7 @@ def mesh_due(step: int, steps: int) -> bool:
     more than its share)."""
     return (step + 1) % MESH_EVERY == 0 or (steps < MESH_EVERY and step == steps - 1)
 W, H = 640, 480
-KERNELS_PER_FRAME_RAW = 20  # 7 preprocess + 2 frame maps + 2 depth tiles + ICP + 3 integrate (setup, brick pre-cull, update) + 3 brick distance + raycast + commit
+KERNELS_PER_FRAME_RAW = 19  # 7 preprocess + 2 frame maps + 2 depth tiles + ICP + 4 integrate (setup, brick pre-cull, work list, update) + brick field + raycast + commit
 D2H_RESULT_BYTES = 336 + 264  # device pose state + azu_icp_result read back per frame
 
 
@@ -820,8 +820,8 @@ def run_gpu(args):
                     if stage_ms["raycast"] > 0 else None,
                     "output_bytes_per_frame": 24 * W * H,
                     "l1_hit": committed_hit_rates()[0], "l2_hit": committed_hit_rates()[1],
-                    "note": "stage time includes the three brick-distance passes; hit rates from the committed "
-                            "ncu summary"},
+                    "note": "stage time includes the brick field launch (free-distance field and ray start map); hit "
+                            "rates from the committed ncu summary"},
         "preprocess": {"ms": stage_ms["input"] / max(prof_frames, 1),
                        "gbs": 9.7e6 / (stage_ms["input"] / max(prof_frames, 1) * 1e-3) / 1e9
                        if stage_ms["input"] > 0 else None,
