@@ -110,6 +110,7 @@ struct azu_pipeline {
     cudaStream_t s2 = nullptr;                    // inputs, preprocessing, frame maps
     cudaStream_t s3 = nullptr;                    // result read-back beside the fusion
     cudaEvent_t ev_front = nullptr, ev_track = nullptr, ev_result = nullptr;
+    cudaEvent_t ev_fused = nullptr;               // the frame's integrate is done
     float* d_depth2[2] = {nullptr, nullptr};      // the frame's depth (metres), alternating
     float* d_tiles2[2] = {nullptr, nullptr};      // its depth tile pyramid
     int buf = 0;
@@ -231,6 +232,16 @@ static int enqueue_tail(azu_pipeline* pl, cudaStream_t s) {
                                       P.min_depth, P.max_depth, &st->gate, s,
                                       two_streams(pl) ? pl->d_tiles2[pl->buf] : nullptr))
         return rc;
+    if (two_streams(pl)) {
+        // an external record node when captured, so the next frame's input
+        // stage can wait for it from outside the graph
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        AZU_TRY_CUDA(cudaStreamIsCapturing(s, &cs));
+        if (cs == cudaStreamCaptureStatusActive)
+            AZU_TRY_CUDA(cudaEventRecordWithFlags(pl->ev_fused, s, cudaEventRecordExternal));
+        else
+            AZU_TRY_CUDA(cudaEventRecord(pl->ev_fused, s));
+    }
     if (int rc = mark(pl, 4, s)) return rc;
     if (int rc = volume_raycast_dev(pl->vol, st->cur, T.fx, T.fy, T.cx, T.cy, W, H, pl->d_model_v, pl->d_model_n,
                                     nullptr, &st->gate, s))
@@ -270,10 +281,14 @@ static int run_frame(azu_pipeline* pl, bool stage_result = false) {
     const bool first = pl->frames == 0;
     if (two_streams(pl)) {
         // input stage on s2 once frame k-1's tracking no longer needs the live
-        // maps (and frame k-2's fusion no longer needs this depth buffer)
+        // maps (and frame k-2's fusion no longer needs this depth buffer), and
+        // not before frame k-1's integrate is done: beside the persistent
+        // integrate its kernels only slow it, while the raycast's tail leaves
+        // SMs idle (frame period 0.542 -> 0.535 ms on c2 raw codes)
         const int b = pl->buf;
         cudaStream_t s = pl->s, s2 = pl->s2;
         AZU_TRY_CUDA(cudaStreamWaitEvent(s2, pl->ev_track, 0));
+        AZU_TRY_CUDA(cudaStreamWaitEvent(s2, pl->ev_fused, 0));
         int rc = first ? enqueue_input(pl, s2)
                        : run_part(pl, pl->g_part[b], pl->x_part[b], s2, [&] { return enqueue_input(pl, s2); });
         if (rc) return rc;
@@ -421,7 +436,7 @@ extern "C" int azu_pipeline_destroy(azu_pipeline* pl) {
     if (pl->h_st) cudaFreeHost(pl->h_st);
     if (pl->h_icp) cudaFreeHost(pl->h_icp);
     for (cudaEvent_t e : pl->ev) if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {pl->ev_front, pl->ev_track, pl->ev_result}) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {pl->ev_front, pl->ev_track, pl->ev_result, pl->ev_fused}) if (e) cudaEventDestroy(e);
     if (pl->s2) cudaStreamDestroy(pl->s2);
     if (pl->s3) cudaStreamDestroy(pl->s3);
     if (pl->s && pl->own_stream) cudaStreamDestroy(pl->s);
@@ -476,7 +491,7 @@ int pipeline_create_on(int device, const azu_pipeline_params* p, cudaStream_t st
             e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
             if (!e) e = cudaStreamCreateWithPriority(&pl->s2, cudaStreamNonBlocking, least);
             if (!e) e = cudaStreamCreateWithFlags(&pl->s3, cudaStreamNonBlocking);
-            for (cudaEvent_t* ev : {&pl->ev_front, &pl->ev_track, &pl->ev_result})
+            for (cudaEvent_t* ev : {&pl->ev_front, &pl->ev_track, &pl->ev_result, &pl->ev_fused})
                 if (!e) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
             for (int k = 0; !e && k < 2; ++k) e = cudaMalloc(&pl->d_depth2[k], n * 4);
             const size_t nt = static_cast<size_t>(make_tile_mip(W, H).total);
