@@ -322,8 +322,9 @@ __device__ void reduce_block_comp(const IcpArgs& a, const Acc& acc, int slot, in
     __syncthreads();
 }
 
+template <bool kP>
 __device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, int vb, double* s_red, int buf) {
-    if (a.precision) reduce_block_comp(a, acc, slot, vb, s_red);
+    if (kP) reduce_block_comp(a, acc, slot, vb, s_red);
     else reduce_block_t<float>(a, acc, slot, vb, s_red, buf);
 }
 
@@ -331,6 +332,7 @@ __device__ void reduce_block(const IcpArgs& a, Acc& acc, int slot, int vb, doubl
 // (slot vb: pixels vb * blockDim + t + k * vblocks * blockDim). The split and
 // each slot's sum are those of a launch with vblocks blocks whatever the grid,
 // so a smaller grid (several scenes tracked side by side) gives the same sums.
+template <bool kP>
 __device__ __forceinline__ void associate_all(const IcpArgs& a, const Rel& rel, const IcpLevel& L, int n, int slot,
                                               double* s_red, int gb, int gn) {
     int buf = 0;
@@ -341,7 +343,7 @@ __device__ __forceinline__ void associate_all(const IcpArgs& a, const Rel& rel, 
 #pragma unroll
         for (int k = 0; k < kNI; ++k) acc.i[k] = 0;
         associate_range(a, rel, L, vb * blockDim.x + threadIdx.x, a.vblocks * blockDim.x, n, acc);
-        reduce_block(a, acc, slot, vb, s_red, buf);
+        reduce_block<kP>(a, acc, slot, vb, s_red, buf);
     }
 }
 
@@ -510,8 +512,9 @@ __device__ __forceinline__ void reduce_grid_ff(const IcpArgs& a, int slot, doubl
     __syncthreads();
 }
 
+template <bool kP>
 __device__ void reduce_grid(const IcpArgs& a, int slot, double* s_sum, int* s_isum) {
-    if (a.precision) {
+    if (kP) {
         if (a.vblocks <= 5 * 32 && 3 * static_cast<int>(blockDim.x >> 5) >= kNF + kNI)
             reduce_grid_ff<5, 3>(a, slot, s_sum, s_isum);
         else
@@ -522,8 +525,9 @@ __device__ void reduce_grid(const IcpArgs& a, int slot, double* s_sum, int* s_is
 }
 
 // Reduced sum k as float (the storage holds floats unless in precision form).
+template <bool kP>
 __device__ __forceinline__ float sum_f(const IcpArgs& a, const double* sum, int k) {
-    return a.precision ? static_cast<float>(sum[k]) : reinterpret_cast<const float*>(sum)[k];
+    return kP ? static_cast<float>(sum[k]) : reinterpret_cast<const float*>(sum)[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -594,25 +598,27 @@ __device__ void warp_eig6(float* m /* smem 36, destroyed */, float* cs /* smem 1
     mx = hi;
 }
 
-// A x = b by Cholesky in double (precision form): unrolled on a packed lower
-// triangle, one reciprocal per pivot (GB300's FP64 divide and square root are
-// long sequences; this keeps six of each).
-__device__ __noinline__ bool chol_solve_d(const double* Ain, const double* b, double* x) {
-    double L[21], inv[6];  // L(i, j), j <= i, at i (i + 1) / 2 + j
+// A x = b by the LDL^T factorisation in double (precision form), unrolled on
+// packed triangles. On GB300 a dependent FP64 fma takes ~64 cycles, a division
+// ~430 and a square root ~700, so the factorisation's critical path is its
+// pivots: LDL^T needs one division per pivot and no square root (13.2 k cycles
+// for Cholesky with a square root and a reciprocal per pivot, measured on one
+// thread). False when a pivot is not positive.
+__device__ __noinline__ bool ldlt_solve_d(const double* Ain, const double* b, double* x) {
+    double L[21], LD[21], inv[6];  // L(i, j) and L(i, j) D(j), j < i, at i (i + 1) / 2 + j
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
         double s = Ain[j * 6 + j];
 #pragma unroll
-        for (int k = 0; k < j; ++k) s -= L[j * (j + 1) / 2 + k] * L[j * (j + 1) / 2 + k];
+        for (int k = 0; k < j; ++k) s -= L[j * (j + 1) / 2 + k] * LD[j * (j + 1) / 2 + k];
         if (!(s > 0.0)) return false;
-        const double d = sqrt(s);
-        inv[j] = 1.0 / d;
-        L[j * (j + 1) / 2 + j] = d;
+        inv[j] = 1.0 / s;
 #pragma unroll
         for (int i = j + 1; i < 6; ++i) {
             double t = Ain[i * 6 + j];
 #pragma unroll
-            for (int k = 0; k < j; ++k) t -= L[i * (i + 1) / 2 + k] * L[j * (j + 1) / 2 + k];
+            for (int k = 0; k < j; ++k) t -= L[i * (i + 1) / 2 + k] * LD[j * (j + 1) / 2 + k];
+            LD[i * (i + 1) / 2 + j] = t;
             L[i * (i + 1) / 2 + j] = t * inv[j];
         }
     }
@@ -622,14 +628,14 @@ __device__ __noinline__ bool chol_solve_d(const double* Ain, const double* b, do
         double s = b[i];
 #pragma unroll
         for (int k = 0; k < i; ++k) s -= L[i * (i + 1) / 2 + k] * y[k];
-        y[i] = s * inv[i];
+        y[i] = s;
     }
 #pragma unroll
     for (int i = 5; i >= 0; --i) {
-        double s = y[i];
+        double s = y[i] * inv[i];
 #pragma unroll
         for (int k = i + 1; k < 6; ++k) s -= L[k * (k + 1) / 2 + i] * x[k];
-        x[i] = s * inv[i];
+        x[i] = s;
     }
     return true;
 }
@@ -715,11 +721,11 @@ __device__ __forceinline__ bool is_rotation(const T* X, T tol) {
     return det > T(0);
 }
 
-// sin and cos of an angle of at most 0.5 rad (the rotation cap bounds every
-// accepted step) by their Taylor series in FP64: after the x^19 / x^18 terms
-// the remainder is below 1e-25, far under half an ulp of the results.
+// sin and cos of an angle of at most 0.5 rad by their Taylor series in FP64:
+// after the x^19 / x^18 terms the remainder is below 1e-25, far under half an
+// ulp of the results. Larger angles (not reached by capped steps) take sincos.
 __device__ __forceinline__ void sincos_small(double x, double& sn, double& cs) {
-    if (!(fabs(x) <= 0.5)) {  // outside the series' range (not reached by capped steps)
+    if (!(fabs(x) <= 0.5)) {
         sincos(x, &sn, &cs);
         return;
     }
@@ -742,20 +748,45 @@ __device__ __forceinline__ void sincos_small(double x, double& sn, double& cs) {
 
 // Precision form: SE(3) exponential of the step and pose composition in FP64,
 // then the nearest rotation (orthogonal polar factor, = U V^T of the SVD for
-// det > 0) by two Newton-Schulz steps X <- X (3 I - X^T X) / 2 in FP64.
+// det > 0) by a Newton-Schulz step X <- X (3 I - X^T X) / 2 in FP64.
+// The rotation is Rodrigues' formula R = I + A K + B K^2 of K = [r]x with
+// A = sin t / t and B = (1 - cos t) / t^2 (t = |r|), the same matrix as
+// cos t I + (1 - cos t) a a^T + sin t [a]x of the unit axis a; A and B are
+// their Taylor series in t^2 (remainder below 1e-25 for t <= 0.5), so neither
+// a square root nor a division is on the path. The composed rotation part is
+// orthogonal to the float pose's ~1e-7, and one step takes that to ~1e-14,
+// below what the float result can hold.
 __device__ void compose_precise(float* pose, const double* x) {
     const double rx = x[3], ry = x[4], rz = x[5];
-    const double angle = sqrt(rx * rx + ry * ry + rz * rz);
+    const double t2 = rx * rx + ry * ry + rz * rz;
     double R[9];
-    if (angle > 1e-4) {
-        const double ia = 1.0 / angle;
-        const double ax = rx * ia, ay = ry * ia, az = rz * ia;
-        double sn, cs;
-        sincos_small(angle, sn, cs);
-        const double cc = 1.0 - cs;
-        R[0] = cs + cc * ax * ax;      R[1] = cc * ax * ay - sn * az; R[2] = cc * ax * az + sn * ay;
-        R[3] = cc * ax * ay + sn * az; R[4] = cs + cc * ay * ay;      R[5] = cc * ay * az - sn * ax;
-        R[6] = cc * ax * az - sn * ay; R[7] = cc * ay * az + sn * ax; R[8] = cs + cc * az * az;
+    if (t2 > 1e-8) {  // angle > 1e-4
+        double A, B;
+        if (t2 <= 0.25) {
+            // 1 / (2k + 1)! and 1 / (2k + 2)!, k = 0 .. 9
+            constexpr double kA[10] = {1.0, 1.0 / 6.0, 1.0 / 120.0, 1.0 / 5040.0, 1.0 / 362880.0,
+                                       1.0 / 39916800.0, 1.0 / 6227020800.0, 1.0 / 1307674368000.0,
+                                       1.0 / 355687428096000.0, 1.0 / 121645100408832000.0};
+            constexpr double kB[10] = {1.0 / 2.0, 1.0 / 24.0, 1.0 / 720.0, 1.0 / 40320.0, 1.0 / 3628800.0,
+                                       1.0 / 479001600.0, 1.0 / 87178291200.0, 1.0 / 20922789888000.0,
+                                       1.0 / 6402373705728000.0, 1.0 / 2432902008176640000.0};
+            A = kA[9];
+            B = kB[9];
+#pragma unroll
+            for (int k = 8; k >= 0; --k) {
+                A = kA[k] - t2 * A;
+                B = kB[k] - t2 * B;
+            }
+        } else {  // outside the series' range (not reached by capped steps)
+            const double t = sqrt(t2);
+            double sn, cs;
+            sincos_small(t, sn, cs);
+            A = sn / t;
+            B = (1.0 - cs) / t2;
+        }
+        R[0] = 1.0 - B * (ry * ry + rz * rz); R[1] = B * rx * ry - A * rz;        R[2] = B * rx * rz + A * ry;
+        R[3] = B * rx * ry + A * rz;        R[4] = 1.0 - B * (rx * rx + rz * rz); R[5] = B * ry * rz - A * rx;
+        R[6] = B * rx * rz - A * ry;        R[7] = B * ry * rz + A * rx;        R[8] = 1.0 - B * (rx * rx + ry * ry);
     } else {
         R[0] = 1.0; R[1] = -rz; R[2] = ry; R[3] = rz; R[4] = 1.0; R[5] = -rx; R[6] = -ry; R[7] = rx; R[8] = 1.0;
     }
@@ -771,8 +802,7 @@ __device__ void compose_precise(float* pose, const double* x) {
             P[4 * i + j] = sum;
         }
     double X[9] = {P[0], P[1], P[2], P[4], P[5], P[6], P[8], P[9], P[10]};
-#pragma unroll
-    for (int it = 0; it < 2; ++it) {
+    {
         double G[9];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
@@ -868,6 +898,9 @@ struct SolveSmem {
     float spec_pose[16];  // the pose the step with the level's default damping leads to
     float spec_step;      // that step's norm
     int spec_ok;          // 0: that step stops the level (no solution, not finite or over a cap)
+    float spec2_pose[16];  // the same with the escalated damping
+    float spec2_step;
+    int spec2_ok;
 };
 
 // Cholesky factor of A + shift I (6x6, float), fully unrolled so that the
@@ -927,17 +960,18 @@ __device__ void chol6_solve_f(const float* A, float damp, const float* b, float*
 }
 
 // Damped solve of (A + damp I) x = b from the reduced sums: Cholesky in float,
-// or in double for the precision form (the reference's LDL^T of the same
+// or LDL^T in double for the precision form (the reference's LDL^T of the same
 // positive definite matrix agrees to rounding). False when the
 // double factorisation breaks down.
+template <bool kP>
 __device__ bool damped_solve(const IcpArgs& a, const SolveSmem& sm, float damp, float* x, double* xd) {
-    if (a.precision) {
+    if (kP) {
         double A[36], b[6];
         int k = 0;
         for (int i = 0; i < 6; ++i)
             for (int j = i; j < 6; ++j) { A[i * 6 + j] = A[j * 6 + i] = sm.sum[k++]; }
         for (int i = 0; i < 6; ++i) { A[i * 6 + i] += damp; b[i] = sm.sum[21 + i]; }
-        if (!chol_solve_d(A, b, xd)) return false;
+        if (!ldlt_solve_d(A, b, xd)) return false;
         for (int i = 0; i < 6; ++i) x[i] = static_cast<float>(xd[i]);
     } else {
         float A[36], b[6];
@@ -945,9 +979,9 @@ __device__ bool damped_solve(const IcpArgs& a, const SolveSmem& sm, float damp, 
 #pragma unroll
         for (int i = 0; i < 6; ++i)
 #pragma unroll
-            for (int j = i; j < 6; ++j) { A[i * 6 + j] = A[j * 6 + i] = sum_f(a, sm.sum, k++); }
+            for (int j = i; j < 6; ++j) { A[i * 6 + j] = A[j * 6 + i] = sum_f<kP>(a, sm.sum, k++); }
 #pragma unroll
-        for (int i = 0; i < 6; ++i) b[i] = sum_f(a, sm.sum, 21 + i);
+        for (int i = 0; i < 6; ++i) b[i] = sum_f<kP>(a, sm.sum, 21 + i);
         chol6_solve_f(A, damp, b, x);
     }
     return true;
@@ -956,11 +990,12 @@ __device__ bool damped_solve(const IcpArgs& a, const SolveSmem& sm, float damp, 
 // The step of damping `damp` from the reduced sums and the pose it leads to
 // (ICPTracker.cpp:86-119): false when the damped system has no solution or
 // the step is not finite or exceeds a cap, which stops the level.
+template <bool kP>
 __device__ __noinline__ bool step_pose(const IcpArgs& a, const SolveSmem& sm, const float* pose, float damp,
                                        float* out, float& step_norm) {
     float x[6];
     double xd[6];
-    if (!damped_solve(a, sm, damp, x, xd)) return false;
+    if (!damped_solve<kP>(a, sm, damp, x, xd)) return false;
     bool fin = true;
     for (int i = 0; i < 6; ++i) fin = fin && isfinite(x[i]);
     const float tn = norm3(mk3(x[0], x[1], x[2])), rn = norm3(mk3(x[3], x[4], x[5]));
@@ -969,7 +1004,7 @@ __device__ __noinline__ bool step_pose(const IcpArgs& a, const SolveSmem& sm, co
     for (int i = 0; i < 6; ++i) ss = fa(ss, fm(x[i], x[i]));
     step_norm = fsq(ss);
     for (int i = 0; i < 16; ++i) out[i] = pose[i];
-    if (a.precision) {
+    if (kP) {
         compose_precise(out, xd);
     } else {
         const float rx = x[3], ry = x[4], rz = x[5];
@@ -993,23 +1028,32 @@ __device__ __noinline__ bool step_pose(const IcpArgs& a, const SolveSmem& sm, co
     return true;
 }
 
-// Barrier of warps 0 and 1 only (named barrier 1, 64 threads).
-__device__ __forceinline__ void sync_solve_warps() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+// Barrier of warps 0, 1 and 2 only (named barrier 1, 96 threads).
+__device__ __forceinline__ void sync_solve_warps() { asm volatile("bar.sync 1, 96;" ::: "memory"); }
 
 // One solve from the reduced sums (ICPTracker.cpp:78-131), executed by warps
-// 0 and 1. Lanes 2..22 of warp 0 store the information matrix; lane 0 of warp
-// 1 solves with the level's default damping and composes the pose it leads
-// to while lane 0 of warp 0 runs the damping test (two warps, so the two run
+// 0, 1 and 2. Lanes 2..22 of warp 0 store the information matrix; lane 0 of
+// warp 1 solves with the level's default damping and composes the pose it
+// leads to, lane 0 of warp 2 does the same with the escalated damping, while
+// lane 0 of warp 0 runs the damping test (separate warps, so the three run
 // side by side rather than one after the other as divergent lanes of one
-// warp would), so in the usual case (no escalation) the test is off the
-// critical path; an escalated damping solves again on warp 0.
+// warp would). The test then only picks one of the two steps: no solve runs
+// after it (track stage on c2 0.0837 -> 0.0817 ms).
+template <bool kP>
 __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelState& st) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int inl = sm.isum[0];
     const float base_damp = (level == 0) ? kDampingLevel0 : kDampingDefault;
     const bool stop = (inl <= 0 || inl < kMinInliersForIteration);
     if (warp == 1) {
-        if (lane == 0 && !stop) sm.spec_ok = step_pose(a, sm, st.pose, base_damp, sm.spec_pose, sm.spec_step) ? 1 : 0;
+        if (lane == 0 && !stop)
+            sm.spec_ok = step_pose<kP>(a, sm, st.pose, base_damp, sm.spec_pose, sm.spec_step) ? 1 : 0;
+        sync_solve_warps();
+        return;
+    }
+    if (warp == 2) {
+        if (lane == 0 && !stop)
+            sm.spec2_ok = step_pose<kP>(a, sm, st.pose, kDampingEscalated, sm.spec2_pose, sm.spec2_step) ? 1 : 0;
         sync_solve_warps();
         return;
     }
@@ -1018,7 +1062,7 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
         int i = 0, r = k;
         while (r >= 6 - i) { r -= 6 - i; ++i; }
         const int j = i + r;
-        const float v = sum_f(a, sm.sum, k);
+        const float v = sum_f<kP>(a, sm.sum, k);
         st.information[i * 6 + j] = v;
         st.information[j * 6 + i] = v;
     }
@@ -1060,12 +1104,12 @@ __device__ void solve_step(const IcpArgs& a, int level, SolveSmem& sm, LevelStat
         for (int i = 0; i < 16; ++i) st.pose[i] = sm.spec_pose[i];
         step_norm = sm.spec_step;
     } else {
-        float P[16];
-        if (!step_pose(a, sm, st.pose, damp, P, step_norm)) { sm.action = 1; return; }
-        for (int i = 0; i < 16; ++i) st.pose[i] = P[i];
+        if (!sm.spec2_ok) { sm.action = 1; return; }
+        for (int i = 0; i < 16; ++i) st.pose[i] = sm.spec2_pose[i];
+        step_norm = sm.spec2_step;
     }
     st.final_step = step_norm;
-    st.error = fd(sum_f(a, sm.sum, 27), static_cast<float>(inl > 1 ? inl : 1));
+    st.error = fd(sum_f<kP>(a, sm.sum, 27), static_cast<float>(inl > 1 ? inl : 1));
     st.inliers = inl;
     st.iters++;
     if (step_norm < kConvergenceStep) {
@@ -1106,6 +1150,7 @@ __device__ int classify(const azu_icp_result& r, const float* prev) {
 // The whole track of one scene by a group of gn co-resident blocks (this one
 // is block gb of the group): a whole grid for a single tracker, a share of one
 // for scenes tracked side by side.
+template <bool kP>
 __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
     __shared__ double s_red[(kIcpThreads / 32) * (kNF + kNI)];
     __shared__ SolveSmem sm;
@@ -1139,19 +1184,19 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
         const Rel rel = s_rel;
         const int iw = L.W - 2, ih = L.H - 2;
         const int n = iw > 0 && ih > 0 ? iw * ih : 0;
-        associate_all(a, rel, L, n, 0, s_red, gb, gn);
+        associate_all<kP>(a, rel, L, n, 0, s_red, gb, gn);
         grid_sync(a.bar, a.err, wl, gen);
-        reduce_grid(a, 0, sm.sum, sm.isum);
+        reduce_grid<kP>(a, 0, sm.sum, sm.isum);
         if (gb == 0 && threadIdx.x == 0) {
             int k = 0;
             for (int i = 0; i < 6; ++i)
                 for (int j = i; j < 6; ++j) {
-                    const float v = sum_f(a, sm.sum, k++);
+                    const float v = sum_f<kP>(a, sm.sum, k++);
                     a.build_out[i * 6 + j] = v;
                     a.build_out[j * 6 + i] = v;
                 }
-            for (int i = 0; i < 6; ++i) a.build_out[36 + i] = sum_f(a, sm.sum, 21 + i);
-            a.build_out[42] = sum_f(a, sm.sum, 27);
+            for (int i = 0; i < 6; ++i) a.build_out[36 + i] = sum_f<kP>(a, sm.sum, 21 + i);
+            a.build_out[42] = sum_f<kP>(a, sm.sum, 27);
             for (int i = 0; i < 6; ++i) reinterpret_cast<int*>(a.build_out)[43 + i] = sm.isum[i];
         }
         return;
@@ -1190,15 +1235,15 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
                 if (threadIdx.x == 0) compute_rel(st.pose, s_refinv, s_rel);
                 __syncthreads();
                 const Rel rel = s_rel;
-                associate_all(a, rel, L, n, slot, s_red, gb, gn);
+                associate_all<kP>(a, rel, L, n, slot, s_red, gb, gn);
                 // Every block reduces the partials and solves on its own: the
                 // same loads in the same order and the same code give every
                 // block the same bits, so no block waits for another's result
                 // after the barrier (the partial slots alternate, so the next
                 // iteration's partials never overwrite ones still being read).
                 grid_sync(a.bar, a.err, wl, gen);
-                reduce_grid(a, slot, sm.sum, sm.isum);
-                if (threadIdx.x < 64) solve_step(a, level, sm, st);
+                reduce_grid<kP>(a, slot, sm.sum, sm.isum);
+                if (threadIdx.x < 96) solve_step<kP>(a, level, sm, st);
                 __syncthreads();
                 slot ^= 1;
                 if (sm.action != 0) break;
@@ -1255,7 +1300,10 @@ __device__ __forceinline__ void icp_body(const IcpArgs& a, int gb, int gn) {
     }
 }
 
-__global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) { icp_body(a, blockIdx.x, gridDim.x); }
+// One kernel per form, so the FP32 form carries none of the precision form's
+// FP64 code.
+template <bool kP>
+__global__ void __launch_bounds__(kIcpThreads) icp_kernel(IcpArgs a) { icp_body<kP>(a, blockIdx.x, gridDim.x); }
 
 // Scenes tracked side by side in one cooperative launch: scene s owns blocks
 // [first[s], first[s + 1]) and its own barrier words and partial slots.
@@ -1267,7 +1315,8 @@ __global__ void __launch_bounds__(kIcpThreads) icp_batch_kernel(const IcpArgs* _
     const int f0 = __ldg(first + s), f1 = __ldg(first + s + 1);
     if (threadIdx.x == 0) sa = args[s];
     __syncthreads();
-    icp_body(sa, static_cast<int>(blockIdx.x) - f0, f1 - f0);
+    if (sa.precision) icp_body<true>(sa, static_cast<int>(blockIdx.x) - f0, f1 - f0);
+    else icp_body<false>(sa, static_cast<int>(blockIdx.x) - f0, f1 - f0);
 }
 
 }  // namespace azu
@@ -1354,6 +1403,16 @@ static void fill_args_p(azu_tracker* t, const azu_tracker_params& p, IcpArgs& a,
     a.err = t->bar + 2;
 }
 
+// Blocks per SM that both forms' kernels can keep resident (a tracker's grid
+// is sized once; its form can change with its parameters).
+static cudaError_t icp_occupancy(int* occ) {
+    int o0 = 0, o1 = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o0, icp_kernel<false>, kIcpThreads, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, icp_kernel<true>, kIcpThreads, 0);
+    *occ = std::min(o0, o1);
+    return e;
+}
+
 int icp_launch(azu_tracker* t, const IcpArgs& a, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(t->nblocks);
@@ -1364,7 +1423,7 @@ int icp_launch(azu_tracker* t, const IcpArgs& a, cudaStream_t s) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    AZU_TRY_CUDA(cudaLaunchKernelEx(&cfg, icp_kernel, a));
+    AZU_TRY_CUDA(cudaLaunchKernelEx(&cfg, a.precision ? icp_kernel<true> : icp_kernel<false>, a));
     return AZU_OK;
 }
 
@@ -1485,7 +1544,7 @@ extern "C" int azu_tracker_create(int device, const azu_tracker_params* p, void*
     int sms = 0, occ = 0;
     if (!rc) {
         cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, icp_kernel, kIcpThreads, 0);
+        if (e == cudaSuccess) e = icp_occupancy(&occ);
         if (e != cudaSuccess || occ < 1) { set_error("ICP occupancy query failed"); rc = AZU_E_CUDA; }
     }
     if (!rc) {
@@ -1812,7 +1871,7 @@ static int static_slot_for_current_device(StaticSlot& out) {
         void* p = nullptr;
         AZU_TRY_CUDA(cudaGetSymbolAddress(&p, g_icp_static_scratch));
         int occ = 0;
-        AZU_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, icp_kernel, kIcpThreads, 0));
+        AZU_TRY_CUDA(icp_occupancy(&occ));
         s.nblocks = std::min(prop.multiProcessorCount * std::min(occ, 2), azu::kMaxGridBlocks);
         s.base = static_cast<unsigned char*>(p);
     }
@@ -1883,7 +1942,7 @@ extern "C" int azu_icp_build_system_noalloc(const float* d_live_vertices, const 
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    AZU_TRY_CUDA(cudaLaunchKernelEx(&cfg, icp_kernel, a));
+    AZU_TRY_CUDA(cudaLaunchKernelEx(&cfg, a.precision ? icp_kernel<true> : icp_kernel<false>, a));
     float out[49];
     unsigned err = 0;
     AZU_TRY_CUDA(cudaMemcpyAsync(out, d_out, sizeof(out), cudaMemcpyDeviceToHost, s));
