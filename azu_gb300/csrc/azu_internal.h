@@ -123,7 +123,6 @@ struct azu_volume {
     // Capped Chebyshev distance of every brick to the nearest brick that is
     // not free, recomputed from the flags before each raycast.
     uint8_t* brick_dist = nullptr;
-    uint8_t* brick_tmp = nullptr;
     int nb = 0;
     bool skip_free = true;
     // Ray start map of the raycast: per 8x8 pixel tile a lower bound of the

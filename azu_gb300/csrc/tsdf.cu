@@ -805,47 +805,13 @@ __device__ __forceinline__ int brick_state(const VolView& v, const uint8_t* __re
     return __ldg(dist + (static_cast<size_t>(bz) * nb + by) * nb + bx);
 }
 
-// One pass of the capped Chebyshev distance transform of the free flags:
-// out(b) = min over |k| <= kDistCap of max(|k|, in(b + k e_axis)), with
-// in = 0 for a brick that is not free and kDistCap for a free one (the first
-// pass reads the flags) and kDistCap outside the grid. Three passes (x, y, z)
-// give the distance to the nearest non-free brick, capped.
+// Capped Chebyshev distance of the free flags: d(b) = the smallest Chebyshev
+// distance from brick b to a brick that is not free, capped at kDistCap
+// (bricks outside the grid count as free). It is separable: three 1-D passes
+// out(b) = min over |k| < kDistCap of max(|k|, in(b + k e_axis)), the first
+// reading in = 0 for a brick that is not free and kDistCap for a free one
+// (brick_field_body runs them in shared memory).
 constexpr int kDistCap = 6;
-__device__ __forceinline__ void brick_dist_at(int x, int y, int z, const uint8_t* __restrict__ in,
-                                              uint8_t* __restrict__ out, int nb, int axis, int from_flags) {
-    const int b = (z * nb + y) * nb + x;  // nb <= 256: 32-bit
-    const int stride = axis == 0 ? 1 : (axis == 1 ? nb : nb * nb);
-    const int pos = axis == 0 ? x : (axis == 1 ? y : z);
-    int d = kDistCap;
-#pragma unroll
-    for (int k = -kDistCap + 1; k < kDistCap; ++k) {
-        const int q = pos + k;
-        if (q < 0 || q >= nb) continue;
-        const uint8_t raw = __ldg(in + b + k * stride);
-        const int val = from_flags ? (raw ? kDistCap : 0) : raw;
-        d = min(d, max(abs(k), val));
-    }
-    out[b] = static_cast<uint8_t>(d);
-}
-__device__ __forceinline__ void brick_dist_body(size_t blk, const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
-                                                int nb, int axis, int from_flags, const int* __restrict__ gate) {
-    if (gate && __ldg(gate) == 0) return;
-    const unsigned n = static_cast<unsigned>(nb) * nb * nb;
-    const unsigned b = static_cast<unsigned>(blk) * blockDim.x + threadIdx.x;
-    if (b >= n) return;
-    const unsigned row = b / static_cast<unsigned>(nb);
-    brick_dist_at(static_cast<int>(b - row * nb), static_cast<int>(row % nb), static_cast<int>(row / nb), in, out, nb,
-                  axis, from_flags);
-}
-// Grid (ceil(nb / 64), nb, nb) of 64 threads: brick (x, y, z) without divisions.
-__global__ void __launch_bounds__(64) brick_dist_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out,
-                                                        int nb, int axis, int from_flags,
-                                                        const int* __restrict__ gate) {
-    if (gate && __ldg(gate) == 0) return;
-    const int x = blockIdx.x * 64 + threadIdx.x;
-    if (x >= nb) return;
-    brick_dist_at(x, blockIdx.y, blockIdx.z, in, out, nb, axis, from_flags);
-}
 
 // Ray start map. A march sample whose base voxel lies in a free brick, or
 // outside the grid, is skipped, so a ray's far steps are skipped up to the
@@ -853,8 +819,8 @@ __global__ void __launch_bounds__(64) brick_dist_kernel(const uint8_t* __restric
 // [8B, 8B + 8) a side, its box widened by 0.01 voxel, far above the rounding
 // of sample positions) bounds that sample from below: a ray through a pixel
 // meets B's box only if the pixel lies in the box's projection, and then not
-// before the camera-to-box distance. One thread per brick (the grid of
-// brick_dist_kernel) takes the projection of B's 8 corners, widened by a pixel,
+// before the camera-to-box distance. One thread per brick (in the brick field
+// launch below) takes the projection of B's 8 corners, widened by a pixel,
 // and lowers the distance bound of every 8x8 pixel tile the projection covers;
 // a box that reaches within 1 mm of the camera plane (its projection is
 // unbounded) lowers the bound of every tile instead. Bounds are distances less
@@ -923,18 +889,17 @@ __device__ __forceinline__ void ray_start_brick(const StartMapArgs& a, int bx, i
 }
 
 // The raycast's brick field in one launch: the three passes of the capped
-// distance transform (brick_dist_at, the same values) run in shared memory over
-// an 8^3 block of bricks and its halo of kDistCap - 1 bricks, and the block's
-// bricks that are not free lower the ray start map.
+// distance transform run in shared memory over an 8^3 block of bricks and its
+// halo of kDistCap - 1 bricks, and the block's bricks that are not free lower
+// the ray start map.
 constexpr int kFieldSide = 8, kFieldHalo = kDistCap - 1, kFieldExt = kFieldSide + 2 * kFieldHalo;
-__global__ void __launch_bounds__(512) brick_field_kernel(const uint8_t* __restrict__ flags, uint8_t* __restrict__ dist,
-                                                          int nb, StartMapArgs sm, const int* __restrict__ gate) {
+// The tile (tx, ty, tz) of 8^3 bricks, by a block of 512 threads.
+__device__ __forceinline__ void brick_field_body(const uint8_t* __restrict__ flags, uint8_t* __restrict__ dist, int nb,
+                                                 const StartMapArgs& sm, int tx, int ty, int tz) {
     __shared__ uint8_t s_in[kFieldExt][kFieldExt][kFieldExt];    // [z][y][x]: 0 not free, kDistCap free or outside
     __shared__ uint8_t s_x[kFieldExt][kFieldExt][kFieldSide];    // after the x pass
     __shared__ uint8_t s_y[kFieldExt][kFieldSide][kFieldSide];   // after the y pass
-    if (gate && __ldg(gate) == 0) return;
-    const int x0 = blockIdx.x * kFieldSide - kFieldHalo, y0 = blockIdx.y * kFieldSide - kFieldHalo,
-              z0 = blockIdx.z * kFieldSide - kFieldHalo;
+    const int x0 = tx * kFieldSide - kFieldHalo, y0 = ty * kFieldSide - kFieldHalo, z0 = tz * kFieldSide - kFieldHalo;
     for (int i = threadIdx.x; i < kFieldExt * kFieldExt * kFieldExt; i += blockDim.x) {
         const int lx = i % kFieldExt, ly = (i / kFieldExt) % kFieldExt, lz = i / (kFieldExt * kFieldExt);
         const int gx = x0 + lx, gy = y0 + ly, gz = z0 + lz;
@@ -969,6 +934,11 @@ __global__ void __launch_bounds__(512) brick_field_kernel(const uint8_t* __restr
     for (int k = -kFieldHalo; k <= kFieldHalo; ++k) d = min(d, max(abs(k), int(s_y[lz + kFieldHalo + k][ly][lx])));
     dist[(static_cast<size_t>(gz) * nb + gy) * nb + gx] = static_cast<uint8_t>(d);
     if (sm.smap && s_in[lz + kFieldHalo][ly + kFieldHalo][lx + kFieldHalo] == 0) ray_start_brick(sm, gx, gy, gz);
+}
+__global__ void __launch_bounds__(512) brick_field_kernel(const uint8_t* __restrict__ flags, uint8_t* __restrict__ dist,
+                                                          int nb, StartMapArgs sm, const int* __restrict__ gate) {
+    if (gate && __ldg(gate) == 0) return;
+    brick_field_body(flags, dist, nb, sm, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // Fast-forward through free space. From a sample t whose brick b has free
@@ -1024,7 +994,7 @@ __global__ void rebuild_bricks_kernel(const void* vox, int res, uint8_t* bricks,
 // Front-face raycast (TSDFVolume.cpp:372-475): one thread per pixel; a warp is
 // 32 adjacent pixels of one row, so its rays march side by side and their
 // trilinear gathers share cache lines.
-template <bool kHalf>
+template <bool kHalf, bool kCol = true>
 __device__ __forceinline__ void raycast_pixel(const VolView& v, const float* __restrict__ d_pose, float fx, float fy,
                                               float cx, float cy, int W, int H, float trunc, float min_depth,
                                               float max_depth, float* __restrict__ vout, float* __restrict__ nout,
@@ -1150,7 +1120,7 @@ __device__ __forceinline__ void raycast_pixel(const VolView& v, const float* __r
         F3 nrm;
         if (!compute_normal<kHalf>(v, hit, nrm)) break;
         if (!finite3(hit)) break;
-        if (cout) {
+        if (kCol && cout) {
             const F3 q = to_voxel(v, hit);
             int vx, vy, vz;
             if (floor_to_int(q.x, &vx) && floor_to_int(q.y, &vy) && floor_to_int(q.z, &vz) && vx >= 0 &&
@@ -1172,18 +1142,19 @@ __device__ __forceinline__ void raycast_pixel(const VolView& v, const float* __r
     } while (false);
     vout[3 * o] = vres.x; vout[3 * o + 1] = vres.y; vout[3 * o + 2] = vres.z;
     nout[3 * o] = nres.x; nout[3 * o + 1] = nres.y; nout[3 * o + 2] = nres.z;
-    if (cout) { cout[3 * o] = col[0]; cout[3 * o + 1] = col[1]; cout[3 * o + 2] = col[2]; }
+    if (kCol && cout) { cout[3 * o] = col[0]; cout[3 * o + 1] = col[1]; cout[3 * o + 2] = col[2]; }
 }
 
-template <bool kHalf>
+template <bool kHalf, bool kCol>
 __global__ void __launch_bounds__(128, 10) raycast_kernel(VolView v, const float* __restrict__ d_pose, float fx,
                                                      float fy, float cx, float cy, int W, int H, float trunc,
                                                      float min_depth, float max_depth, float* __restrict__ vout,
                                                      float* __restrict__ nout, uint8_t* __restrict__ cout,
                                                      const int* __restrict__ gate, const uint8_t* __restrict__ bdist,
                                                      int nb, const uint32_t* __restrict__ smap) {
-    raycast_pixel<kHalf>(v, d_pose, fx, fy, cx, cy, W, H, trunc, min_depth, max_depth, vout, nout, cout, gate, bdist,
-                         nb, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, smap);
+    raycast_pixel<kHalf, kCol>(v, d_pose, fx, fy, cx, cy, W, H, trunc, min_depth, max_depth, vout, nout, cout, gate,
+                               bdist, nb, blockIdx.x * blockDim.x + threadIdx.x,
+                               blockIdx.y * blockDim.y + threadIdx.y, smap);
 }
 
 // ---- global point cloud (TSDFVolume.cpp:571-632) --------------------------------
@@ -1275,6 +1246,7 @@ __global__ void __launch_bounds__(kPcThreads) pc_emit_kernel(const void* vox, co
 }
 
 static int ensure_tiles(azu_volume* v, size_t n, cudaStream_t s);
+static int ensure_ray_start(azu_volume* v, size_t n, cudaStream_t s);
 
 // ---- batches: several volumes, one launch per stage --------------------------
 // A batch integrates and raycasts the current frame of several independent
@@ -1313,8 +1285,8 @@ struct RaycastArgs {
     const int* gate;
     const uint8_t* bricks;
     uint8_t* bdist;
-    uint8_t* btmp;
     int nb;
+    uint32_t* smap;  // the volume's ray start map
 };
 
 __device__ __forceinline__ int batch_find(const int* __restrict__ off, int n, int i) {
@@ -1361,13 +1333,25 @@ __global__ void __launch_bounds__(kWarps * 32) integrate_batch_kernel(const Inte
     }
 }
 
-__global__ void brick_dist_batch_kernel(const RaycastArgs* __restrict__ A, const int* __restrict__ off, int n,
-                                        int pass) {
+// Every scene's start map back to "no bound" (block s: scene s).
+__global__ void ray_start_reset_batch_kernel(const RaycastArgs* __restrict__ A) {
+    const RaycastArgs& a = A[blockIdx.x];
+    if (a.gate && __ldg(a.gate) == 0) return;
+    const int n = ((a.W + (1 << kStartShift) - 1) >> kStartShift) * ((a.H + (1 << kStartShift) - 1) >> kStartShift) + 1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) a.smap[i] = 0x7f7f7f7fu;
+}
+
+// The brick field of every scene: scene s owns blocks [off[s], off[s + 1]), one
+// per tile of 8^3 bricks.
+__global__ void __launch_bounds__(512) brick_field_batch_kernel(const RaycastArgs* __restrict__ A,
+                                                                const int* __restrict__ off, int n) {
     const int s = batch_find(off, n, blockIdx.x);
     const RaycastArgs& a = A[s];
-    const uint8_t* in = pass == 0 ? a.bricks : (pass == 1 ? a.bdist : a.btmp);
-    uint8_t* out = pass == 1 ? a.btmp : a.bdist;
-    brick_dist_body(blockIdx.x - __ldg(off + s), in, out, a.nb, pass, pass == 0 ? 1 : 0, a.gate);
+    if (a.gate && __ldg(a.gate) == 0) return;
+    const int gb = (a.nb + kFieldSide - 1) / kFieldSide;
+    const int t = blockIdx.x - __ldg(off + s);
+    const StartMapArgs sm{a.v.vs, a.v.origin, a.pose, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.smap};
+    brick_field_body(a.bricks, a.bdist, a.nb, sm, t % gb, (t / gb) % gb, t / (gb * gb));
 }
 
 __global__ void __launch_bounds__(256, 5) raycast_batch_kernel(const RaycastArgs* __restrict__ A,
@@ -1377,9 +1361,9 @@ __global__ void __launch_bounds__(256, 5) raycast_batch_kernel(const RaycastArgs
     const int tile = blockIdx.x - __ldg(off + s);
     const int tiles_x = (a.W + blockDim.x - 1) / blockDim.x;
     const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
-    raycast_pixel<false>(a.v, a.pose, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.trunc, a.min_depth, a.max_depth, a.vout,
-                         a.nout, nullptr, a.gate, a.bdist, a.nb, tx * blockDim.x + threadIdx.x,
-                         ty * blockDim.y + threadIdx.y);
+    raycast_pixel<false, false>(a.v, a.pose, a.fx, a.fy, a.cx, a.cy, a.W, a.H, a.trunc, a.min_depth, a.max_depth,
+                                a.vout, a.nout, nullptr, a.gate, a.bdist, a.nb, tx * blockDim.x + threadIdx.x,
+                                ty * blockDim.y + threadIdx.y, a.smap);
 }
 
 }  // namespace azu
@@ -1389,7 +1373,7 @@ struct azu_volume_batch {
     std::vector<azu::PipelineFrameView> views;
     azu::IntegrateArgs* d_int = nullptr;
     azu::RaycastArgs* d_ray = nullptr;
-    int* d_off = nullptr;  // [0..n] tile blocks, [n+1..2n+1] integrate items, [2n+2..3n+2] bricks, [3n+3..4n+3] ray tiles
+    int* d_off = nullptr;  // [0..n] tile blocks, [n+1..2n+1] integrate items, [2n+2..3n+2] brick field tiles, [3n+3..4n+3] ray tiles
     unsigned* d_work = nullptr;  // next integrate item
     int tiles_blocks = 0, items = 0, brick_blocks = 0, ray_blocks = 0;
     int int_grid[3] = {0, 0, 0};  // resident blocks of the persistent integrate, by 1, 2, 4 warps
@@ -1411,8 +1395,8 @@ static int batch_upload_offsets(azu_volume_batch* b) {
         const int res = f.vol->p.resolution;
         it += res * ((res + 31) / 32) * b->int_parts;
         off[2 * (n + 1) + i] = bb;
-        const size_t nbr = static_cast<size_t>(f.vol->nb) * f.vol->nb * f.vol->nb;
-        bb += static_cast<int>((nbr + 255) / 256);
+        const int gb = (f.vol->nb + kFieldSide - 1) / kFieldSide;
+        bb += gb * gb * gb;
         off[3 * (n + 1) + i] = rb;
         rb += ((f.W + b->ray_w - 1) / b->ray_w) * ((f.H + b->ray_h - 1) / b->ray_h);
     }
@@ -1452,9 +1436,13 @@ int volume_batch_create(const PipelineFrameView* views, int n, azu_volume_batch*
                               p.origin[1], p.origin[2], p.truncation, p.max_weight, f.fx, f.fy, f.cx, f.cy, f.W,
                               f.H, f.min_d, f.max_d, f.d_gate, v->d_counters, v->bricks, v->nb, v->d_tiles, mip,
                               v->d_iconsts, f.d_pose};
+        if (!rc)
+            rc = ensure_ray_start(v, static_cast<size_t>((f.W + (1 << kStartShift) - 1) >> kStartShift) *
+                                             ((f.H + (1 << kStartShift) - 1) >> kStartShift) + 1,
+                                  v->stream.s);
         ra[i] = RaycastArgs{make_view(v), f.d_pose, f.fx, f.fy, f.cx, f.cy, f.W, f.H, p.truncation, p.min_depth,
-                            p.max_depth, f.d_vertices, f.d_normals, f.d_gate, v->bricks, v->brick_dist,
-                            v->brick_tmp, v->nb};
+                            p.max_depth, f.d_vertices, f.d_normals, f.d_gate, v->bricks, v->brick_dist, v->nb,
+                            v->ray_start};
         AZU_CHECK_ARG(v->skip_free, "batched raycasts use free-space skipping");
     }
     if (!rc) {
@@ -1530,10 +1518,10 @@ int volume_batch_integrate(azu_volume_batch* b, cudaStream_t s) {
 int volume_batch_raycast(azu_volume_batch* b, cudaStream_t s) {
     const int n = b->n;
     const int* boff = b->d_off + 2 * (n + 1);
-    for (int pass = 0; pass < 3; ++pass) {
-        brick_dist_batch_kernel<<<b->brick_blocks, 256, 0, s>>>(b->d_ray, boff, n, pass);
-        AZU_LAUNCH_CHECK();
-    }
+    ray_start_reset_batch_kernel<<<n, 256, 0, s>>>(b->d_ray);
+    AZU_LAUNCH_CHECK();
+    brick_field_batch_kernel<<<b->brick_blocks, 512, 0, s>>>(b->d_ray, boff, n);
+    AZU_LAUNCH_CHECK();
     raycast_batch_kernel<<<b->ray_blocks, dim3(b->ray_w, b->ray_h), 0, s>>>(b->d_ray, b->d_off + 3 * (n + 1), n);
     AZU_LAUNCH_CHECK();
     return AZU_OK;
@@ -1718,14 +1706,17 @@ int volume_raycast_dev(azu_volume* v, const float* d_pose, float fx, float fy, f
         bricks = v->brick_dist;
         smap = v->ray_start;
     }
-    if (p.format != AZU_TSDF_FP32)
-        raycast_kernel<true><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
-                                                  p.max_depth, d_vertices, d_normals, d_colors, d_gate, bricks,
-                                                  v->nb, smap);
-    else
-        raycast_kernel<false><<<grd, blk, 0, s>>>(view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth,
-                                                   p.max_depth, d_vertices, d_normals, d_colors, d_gate, bricks,
-                                                   v->nb, smap);
+    // one instantiation per (format, colour output): without colour output the
+    // march carries none of the colour lookup's code
+#define AZU_RC_ARGS                                                                                            \
+    view, d_pose, fx, fy, cx, cy, W, H, p.truncation, p.min_depth, p.max_depth, d_vertices, d_normals, d_colors, \
+        d_gate, bricks, v->nb, smap
+    const bool half = p.format != AZU_TSDF_FP32;
+    if (half && d_colors) raycast_kernel<true, true><<<grd, blk, 0, s>>>(AZU_RC_ARGS);
+    else if (half) raycast_kernel<true, false><<<grd, blk, 0, s>>>(AZU_RC_ARGS);
+    else if (d_colors) raycast_kernel<false, true><<<grd, blk, 0, s>>>(AZU_RC_ARGS);
+    else raycast_kernel<false, false><<<grd, blk, 0, s>>>(AZU_RC_ARGS);
+#undef AZU_RC_ARGS
     AZU_LAUNCH_CHECK();
     return AZU_OK;
 }
@@ -1737,7 +1728,6 @@ static int volume_alloc(azu_volume* v) {
     v->nb = (v->p.resolution + 7) >> kBrickShift;
     AZU_TRY_CUDA(cudaMalloc(&v->bricks, static_cast<size_t>(v->nb) * v->nb * v->nb));
     AZU_TRY_CUDA(cudaMalloc(&v->brick_dist, static_cast<size_t>(v->nb) * v->nb * v->nb));
-    AZU_TRY_CUDA(cudaMalloc(&v->brick_tmp, static_cast<size_t>(v->nb) * v->nb * v->nb));
     v->int_live_words = (v->nb + 31) / 32;
     AZU_TRY_CUDA(cudaMalloc(&v->int_live, static_cast<size_t>(v->nb) * v->nb * v->int_live_words * 4));
     {
@@ -1761,13 +1751,11 @@ static void volume_free_storage(azu_volume* v) {
     if (v->color) cudaFree(v->color);
     if (v->bricks) cudaFree(v->bricks);
     if (v->brick_dist) cudaFree(v->brick_dist);
-    if (v->brick_tmp) cudaFree(v->brick_tmp);
     if (v->int_live) cudaFree(v->int_live);
     v->int_live = nullptr;
     if (v->int_list) cudaFree(v->int_list);
     v->int_list = nullptr;
     v->brick_dist = nullptr;
-    v->brick_tmp = nullptr;
     v->vox = nullptr;
     v->color = nullptr;
     v->bricks = nullptr;
@@ -2081,10 +2069,10 @@ extern "C" int azu_volume_raycast_many(azu_volume* v, const float* poses, int co
     const VolView view = make_view(v);
     const uint8_t* bricks = nullptr;
     if (!e && v->skip_free) {
-        const dim3 g((v->nb + 63) / 64, v->nb, v->nb);
-        brick_dist_kernel<<<g, 64, 0, s>>>(v->bricks, v->brick_dist, v->nb, 0, 1, nullptr);
-        brick_dist_kernel<<<g, 64, 0, s>>>(v->brick_dist, v->brick_tmp, v->nb, 1, 0, nullptr);
-        brick_dist_kernel<<<g, 64, 0, s>>>(v->brick_tmp, v->brick_dist, v->nb, 2, 0, nullptr);
+        // the distance field only: each image has its own pose, so no start map
+        const int gb = (v->nb + kFieldSide - 1) / kFieldSide;
+        const StartMapArgs sm{p.voxel_size, view.origin, nullptr, fx, fy, cx, cy, width, height, nullptr};
+        brick_field_kernel<<<dim3(gb, gb, gb), 512, 0, s>>>(v->bricks, v->brick_dist, v->nb, sm, nullptr);
         e = cudaGetLastError();
         bricks = v->brick_dist;
     }
