@@ -289,7 +289,7 @@ def run_forms(seq, raw, rgb, dev, frames: int, err_frames: int):
     ang = float(np.arccos(np.clip((np.trace(dp[:3, :3]) - 1) / 2, -1, 1)))
     out["precision_fp16r"] = {
         "workload": f"c3: 1024^3 over a 4 m cube, FP16R tsdf (half + 9-bit residual, 4 B/voxel) vs FP32 (8 B/voxel), "
-                    f"ICP with compensated FP32 block sums, float-float cross-block sum, FP64 Cholesky, SE(3) exponential and composition; "
+                    f"ICP with compensated FP32 block sums, float-float cross-block sum, FP64 LDL^T solve, SE(3) exponential and composition; "
                     f"frames 3..{2 + frames} of the c2 orbit (stage times: the next {frames}, one at a time)",
         "frames_per_s": res["fp16r"]["frames_per_s"], "stage_ms_per_frame": res["fp16r"]["stage_ms_per_frame"],
         "fp32_same_workload": {"frames_per_s": res["fp32"]["frames_per_s"],

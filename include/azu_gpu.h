@@ -190,8 +190,8 @@ typedef struct {
     float min_depth, max_depth;
     float fx, fy, cx, cy;    /* camera intrinsics at 640x480 (setIntrinsics) */
     int   precision;         /* 0: FP32 reduction + FP32 solve (reference semantics);
-                                1: compensated FP32 per-block sums, FP64 cross-block
-                                sum, FP64 Cholesky and SE(3) update */
+                                1: compensated FP32 per-block sums, float-float
+                                cross-block sum, FP64 LDL^T solve and SE(3) update */
 } azu_tracker_params;
 
 /* Mirrors ICPResult (ICPTracker.h:27-47); pose row-major. */
