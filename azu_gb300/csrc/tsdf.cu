@@ -1146,7 +1146,7 @@ __device__ __forceinline__ void raycast_pixel(const VolView& v, const float* __r
 }
 
 template <bool kHalf, bool kCol>
-__global__ void __launch_bounds__(128, 10) raycast_kernel(VolView v, const float* __restrict__ d_pose, float fx,
+__global__ void __launch_bounds__(128, 9) raycast_kernel(VolView v, const float* __restrict__ d_pose, float fx,
                                                      float fy, float cx, float cy, int W, int H, float trunc,
                                                      float min_depth, float max_depth, float* __restrict__ vout,
                                                      float* __restrict__ nout, uint8_t* __restrict__ cout,
