@@ -5,8 +5,9 @@
 //   vn_kernel      — one thread per level-0 pixel: vertex from depth, normal
 //                    from the 4 neighbours' vertices (recomputed from depth,
 //                    bit-identical to the stored ones).
-//   pyramid_kernel — one thread per level-2 pixel: its four level-1 pixels
-//                    (each the 2x2 reduction of level 0) and then itself.
+//   pyramid_kernel — one thread per level-1 pixel (the 2x2 reduction of
+//                    level 0), then a quarter of them each level-2 pixel
+//                    from four level-1 pixels in shared memory.
 // Maps are packed float3 (12 B per pixel), depth float.
 #include "azu_internal.h"
 #include "kf_math.cuh"
@@ -106,28 +107,45 @@ __device__ __forceinline__ void down_px(const float* __restrict__ sd, const floa
     }
 }
 
-__global__ void __launch_bounds__(256) pyramid_kernel(const float* __restrict__ d0, const float* __restrict__ v0,
-                                                      const float* __restrict__ n0, int W0, float* __restrict__ d1,
-                                                      float* __restrict__ v1, float* __restrict__ n1,
-                                                      float* __restrict__ d2, float* __restrict__ v2,
-                                                      float* __restrict__ n2, int W2, int H2) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+// 16 x 16 level-1 pixels per block (the 2x2 reductions of level 0), staged in
+// shared memory, then the block's 8 x 8 level-2 pixels from them.
+constexpr int kPyrSide = 16;
+__global__ void __launch_bounds__(kPyrSide * kPyrSide) pyramid_kernel(
+    const float* __restrict__ d0, const float* __restrict__ v0, const float* __restrict__ n0, int W0, int W1, int H1,
+    float* __restrict__ d1, float* __restrict__ v1, float* __restrict__ n1, float* __restrict__ d2,
+    float* __restrict__ v2, float* __restrict__ n2, int W2, int H2) {
+    __shared__ float s_d[kPyrSide][kPyrSide];
+    __shared__ float s_v[kPyrSide][kPyrSide][3];
+    __shared__ float s_n[kPyrSide][kPyrSide][3];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x1 = blockIdx.x * kPyrSide + tx, y1 = blockIdx.y * kPyrSide + ty;
+    if (x1 < W1 && y1 < H1) {
+        float d;
+        F3 v, n;
+        down_px(d0, v0, n0, W0, x1, y1, d, v, n);
+        const int i1 = y1 * W1 + x1;
+        d1[i1] = d;
+        st3(v1, i1, v);
+        st3(n1, i1, n);
+        s_d[ty][tx] = d;
+        s_v[ty][tx][0] = v.x; s_v[ty][tx][1] = v.y; s_v[ty][tx][2] = v.z;
+        s_n[ty][tx][0] = n.x; s_n[ty][tx][1] = n.y; s_n[ty][tx][2] = n.z;
+    }
+    __syncthreads();
+    if (tx >= kPyrSide / 2 || ty >= kPyrSide / 2) return;
+    const int x = blockIdx.x * (kPyrSide / 2) + tx, y = blockIdx.y * (kPyrSide / 2) + ty;
     if (x >= W2 || y >= H2) return;
-    const int W1 = W0 / 2;
+    // Level 2 from the four level-1 pixels, in the order a read-back takes them:
+    // (0,0), (1,0), (0,1), (1,1).
     float ld1[4];
     F3 lv1[4], ln1[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const int x1 = 2 * x + (k & 1), y1 = 2 * y + (k >> 1);
-        down_px(d0, v0, n0, W0, x1, y1, ld1[k], lv1[k], ln1[k]);
-        const int i1 = y1 * W1 + x1;
-        d1[i1] = ld1[k];
-        st3(v1, i1, lv1[k]);
-        st3(n1, i1, ln1[k]);
+        const int sx = 2 * tx + (k & 1), sy = 2 * ty + (k >> 1);
+        ld1[k] = s_d[sy][sx];
+        lv1[k] = mk3(s_v[sy][sx][0], s_v[sy][sx][1], s_v[sy][sx][2]);
+        ln1[k] = mk3(s_n[sy][sx][0], s_n[sy][sx][1], s_n[sy][sx][2]);
     }
-    // Level 2 from the four level-1 pixels held in registers (same order as a
-    // read-back: (0,0), (1,0), (0,1), (1,1)).
     F3 sumv = mk3(0.0f, 0.0f, 0.0f), sumn = mk3(0.0f, 0.0f, 0.0f);
     float sumd = 0.0f, dmin = 0.0f, dmax = 0.0f;
     int count = 0, mk = 0;
@@ -174,9 +192,9 @@ int launch_prepare_live(const float* d_depth, int W, int H, float fx, float fy, 
     }
     if (D[0] != d_depth) AZU_TRY_CUDA(cudaMemcpyAsync(D[0], d_depth, sizeof(float) * W * H, cudaMemcpyDeviceToDevice, s));
     {
-        const int W2 = W / 4, H2 = H / 4;
-        const dim3 b(32, 8), g((W2 + 31) / 32, (H2 + 7) / 8);
-        pyramid_kernel<<<g, b, 0, s>>>(d_depth, V[0], N[0], W, D[1], V[1], N[1], D[2], V[2], N[2], W2, H2);
+        const int W1 = W / 2, H1 = H / 2, W2 = W / 4, H2 = H / 4;
+        const dim3 b(kPyrSide, kPyrSide), g((W1 + kPyrSide - 1) / kPyrSide, (H1 + kPyrSide - 1) / kPyrSide);
+        pyramid_kernel<<<g, b, 0, s>>>(d_depth, V[0], N[0], W, W1, H1, D[1], V[1], N[1], D[2], V[2], N[2], W2, H2);
         AZU_LAUNCH_CHECK();
     }
     return AZU_OK;

@@ -867,7 +867,8 @@ __device__ __forceinline__ void ray_start_brick(const StartMapArgs& a, int bx, i
             near_plane = 1;
             continue;
         }
-        const float u = a.fx * (xc / zc) + a.cx, w = a.fy * (yc / zc) + a.cy;
+        // a fast quotient: its few ulps are far inside the pixel of margin
+        const float u = a.fx * __fdividef(xc, zc) + a.cx, w = a.fy * __fdividef(yc, zc) + a.cy;
         umin = fminf(umin, u); umax = fmaxf(umax, u);
         vmin = fminf(vmin, w); vmax = fmaxf(vmax, w);
     }
