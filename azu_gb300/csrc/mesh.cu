@@ -44,6 +44,10 @@ struct MeshVol {
     int res;
     float vs;
     F3 origin;
+    // the volume's free-brick flags (1: every voxel of the brick and its
+    // 1-voxel apron unobserved or >= 0.9995), nb bricks a side
+    const uint8_t* bricks;
+    int nb;
     __device__ __forceinline__ size_t idx(int x, int y, int z) const {
         const size_t r = static_cast<size_t>(res);
         return (static_cast<size_t>(z) * r + static_cast<size_t>(y)) * r + static_cast<size_t>(x);
@@ -317,6 +321,16 @@ __global__ void __launch_bounds__(kClassifyThreads) mc_classify_kernel(MeshVol v
     const VT* src_main = base + (in_main ? static_cast<size_t>(y0 + ty) * res + (x0 + tx) : 0);
     const VT* src_apron = base + (in_apron ? static_cast<size_t>(y0 + ay) * res + (x0 + ax) : 0);
     const int own = ty * kCodeW + tx, apron = ay * kCodeW + ax;
+    {
+        // The tile's cubes have their base voxels in 4 x 1 x 4 bricks (x0, y0,
+        // z0 are multiples of 8) and their corners in those bricks' aprons. In
+        // a free brick every usable corner is >= 0.9995, so no cube there has a
+        // sign change: a tile of free bricks lists nothing and reads nothing.
+        const int bx = (x0 >> 3) + (tid & 3), by = y0 >> 3, bz = (z0 >> 3) + ((tid >> 2) & 3);
+        const bool open = tid < 16 && bx < v.nb && by < v.nb && bz < v.nb &&
+                          __ldg(v.bricks + (static_cast<size_t>(bz) * v.nb + by) * v.nb + bx) == 0;
+        if (!__syncthreads_or(open)) return;
+    }
     if (tid == 0) list_n = 0;
     auto issue = [&](int s) {  // slice s = voxel layer z0 + s
         if (s <= nz) {
@@ -416,6 +430,13 @@ __global__ void __launch_bounds__(256) mc_validate_kernel(MeshVol v, const unsig
 }
 
 __device__ __forceinline__ unsigned byte_sum(unsigned w) { return __dp4a(w, 0x01010101u, 0u); }
+
+// The counts of the listed cubes (the only ones the validate step writes) back
+// to zero.
+__global__ void __launch_bounds__(256) mc_clear_counts_kernel(const unsigned long long* __restrict__ active, unsigned n,
+                                                              uint8_t* __restrict__ counts) {
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) counts[active[k]] = 0;
+}
 
 // ---- 4. emit: the vertex slots of every emitted triangle ---------------------
 // A candidate's first triangle is its block's offset plus the triangles of the
@@ -636,6 +657,7 @@ struct azu_mesher {
     // per-volume buffers
     uint8_t* counts = nullptr;  // triangles per cube (linear cube order)
     size_t counts_cap = 0;
+    bool counts_zero = false;   // every count is zero (cleared after each extraction)
     unsigned* block_sums = nullptr;  // per 256 cubes; scanned in place into offsets
     size_t blocks_cap = 0;
     unsigned* scratch = nullptr;
@@ -760,9 +782,13 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     const unsigned long long ncubes = cr * cr * cr;
     if (ncubes == 0) { m->last = *info; return AZU_OK; }
     MeshVol mv{v->vox, v->p.format != AZU_TSDF_FP32 ? 1 : 0, v->color, res, v->p.voxel_size,
-               mk3(v->p.origin[0], v->p.origin[1], v->p.origin[2])};
+               mk3(v->p.origin[0], v->p.origin[1], v->p.origin[2]), v->bricks, v->nb};
     const size_t nblocks = static_cast<size_t>((ncubes + 255) / 256);
-    if (int rc = grow(m->counts, m->counts_cap, static_cast<size_t>(ncubes) + 16)) return rc;
+    {
+        const size_t cap_before = m->counts_cap;
+        if (int rc = grow(m->counts, m->counts_cap, static_cast<size_t>(ncubes) + 16)) return rc;
+        if (m->counts_cap != cap_before) m->counts_zero = false;  // a new buffer
+    }
     if (int rc = grow(m->block_sums, m->blocks_cap, nblocks)) return rc;
     if (int rc = grow(m->scratch, m->scratch_cap, scan_scratch_words(std::max<size_t>(nblocks, 1 << 24)))) return rc;
     // candidate list: a surface's share of the cubes, regrown with headroom when it overflows
@@ -774,8 +800,12 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     const unsigned pgrid = static_cast<unsigned>(std::max(m->sms, 1) * 8);
     unsigned sc4[4] = {0, 0, 0, 0};
     for (int attempt = 0; attempt < 2; ++attempt) {
-        // counts carries one uint4 of slack: the emit's byte sums read whole words
-        AZU_TRY_CUDA(cudaMemsetAsync(m->counts, 0, static_cast<size_t>(ncubes) + 16, s));
+        // counts carries one uint4 of slack: the emit's byte sums read whole
+        // words. It is zeroed once; after each extraction the listed cubes'
+        // counts are set back to zero (a few MB of writes instead of a memset
+        // of one byte per cube).
+        if (!m->counts_zero) AZU_TRY_CUDA(cudaMemsetAsync(m->counts, 0, m->counts_cap, s));  // the whole buffer
+        m->counts_zero = false;
         AZU_TRY_CUDA(cudaMemsetAsync(m->block_sums, 0, nblocks * 4, s));
         AZU_TRY_CUDA(cudaMemsetAsync(m->d_scalars, 0, 16, s));
         const unsigned acap = static_cast<unsigned>(std::min<size_t>(m->active_cap, 0xFFFFFFFFu));
@@ -797,15 +827,32 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
         if (int rc = ensure_active(m, std::min<size_t>(ncubes, static_cast<size_t>(sc4[3]) + sc4[3] / 2))) return rc;
     }
     const unsigned total = sc4[0], n_active = sc4[3];
+    // the listed cubes' counts back to zero once the emit has read them
+    auto clear_counts = [&]() -> int {
+        if (n_active) {
+            mc_clear_counts_kernel<<<std::min(pgrid, (n_active + 255) / 256), 256, 0, s>>>(m->active, n_active,
+                                                                                         m->counts);
+            AZU_LAUNCH_CHECK();
+            ++t_launches;
+        }
+        m->counts_zero = true;
+        return AZU_OK;
+    };
     const unsigned cap = static_cast<unsigned>(std::min<int64_t>(m->max_triangles, total));
     const size_t nslots = 3 * static_cast<size_t>(cap);
     info->truncated = total > cap ? 1 : 0;
-    if (cap == 0) { info->launches = t_launches; m->last = *info; return AZU_OK; }
+    if (cap == 0) {
+        if (int rc = clear_counts()) return rc;
+        info->launches = t_launches;
+        m->last = *info;
+        return AZU_OK;
+    }
     if (int rc = ensure_slots(m, nslots)) return rc;
     mc_emit_kernel<<<std::min(pgrid, (n_active + 255) / 256), 256, 0, s>>>(mv, m->active, m->meta, n_active, m->counts,
                                                                           m->block_sums, cap, m->slot_key);
     AZU_LAUNCH_CHECK();
     ++t_launches;
+    if (int rc = clear_counts()) return rc;
     size_t tsize = 1024;
     while (tsize < 2 * nslots) tsize <<= 1;
     if (tsize > m->table_cap || !m->tkeys) {
