@@ -814,7 +814,9 @@ def run_gpu(args):
                      "final_pose_err_m": float(np.linalg.norm(pl.last_result()["pose"][:3, 3] - gt[:3, 3]))},
         "meshes": [{"vertices": m["n_vertices"], "triangles": m["n_indices"] // 3} for m in meshes[:3]],
         "marching_cubes": {"extract_ms": mesh_ms, "mvoxels_per_s": 512 ** 3 / (mesh_ms * 1e-3) / 1e6,
-                           "classify_bytes": 8 * 512 ** 3, "triangles": mesh_last["n_indices"] // 3,
+                           "classify_bytes_upper_bound": 8 * 512 ** 3,
+                           "note": "classify reads only the 32x8x32-cube tiles that hold a brick that is not free",
+                           "triangles": mesh_last["n_indices"] // 3,
                            "vertices": mesh_last["n_vertices"], "truncated": bool(mesh_last["truncated"])},
         "raycast": {"rays_per_s": W * H / (stage_ms["raycast"] / max(prof_frames, 1) * 1e-3)
                     if stage_ms["raycast"] > 0 else None,
