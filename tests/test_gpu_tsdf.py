@@ -176,3 +176,46 @@ def test_free_space_skipping_is_exact(cuda_lib, orc, c1_seq):
         for key in ("vertices", "normals"):
             assert np.array_equal(on[key].view(np.uint32), off[key].view(np.uint32))
             assert np.array_equal(on[key].view(np.uint32), ro[key].view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_ray_start_map_near_and_inside_surfaces(cuda_lib, orc, c1_seq):
+    """The ray start map skips far steps only below every brick that is not
+    free: cameras moved towards and into the fused surfaces (bricks across the
+    camera plane bound every tile), turned away from them, and looking along
+    them give the same images with skipping on and off, and the oracle's."""
+    from azu_gb300 import synth
+    s = c1_seq
+    prm = dict(s.volume, min_depth=s.min_depth, max_depth=s.max_depth)
+    prm.pop("format")
+    g = _gpu_volume(prm)
+    o = _orc_volume(orc, prm)
+    K = (s.fx, s.fy, s.cx, s.cy)
+    for k in range(8):
+        dm = synth.mm_to_meters(s.depth_mm[k])
+        g.integrate(dm, s.poses[k], K, s.width, s.height, s.min_depth, s.max_depth)
+        o.integrate(dm, s.poses[k], orc.intr(*K), s.width, s.height, s.min_depth, s.max_depth)
+    base = np.asarray(s.poses[7], np.float32)
+    fwd = base[:3, 2]
+    poses = []
+    for d in (0.6, 1.0, 1.15, 1.25):  # towards the scene centre, 1.5 m ahead: up to inside the sphere's band
+        p = base.copy()
+        p[:3, 3] += np.float32(d) * fwd
+        poses.append(p)
+    turn = base.copy()  # looking away from the scene
+    turn[:3, 0] *= -1
+    turn[:3, 2] *= -1
+    poses.append(turn)
+    c, sn = np.float32(np.cos(1.3)), np.float32(np.sin(1.3))
+    side = base.copy()  # yawed 75 degrees: along the fused surfaces
+    side[:3, :3] = base[:3, :3] @ np.array([[c, 0, sn], [0, 1, 0], [-sn, 0, c]], np.float32)
+    poses.append(side)
+    for i, p in enumerate(poses):
+        on = g.raycast(p, K, s.width, s.height)
+        g.lib.azu_volume_set_free_space_skipping(g.h, 0)
+        off = g.raycast(p, K, s.width, s.height)
+        g.lib.azu_volume_set_free_space_skipping(g.h, 1)
+        ro = o.raycast(p, orc.intr(*K), s.width, s.height)
+        for key in ("vertices", "normals"):
+            assert np.array_equal(on[key].view(np.uint32), off[key].view(np.uint32)), (i, key)
+            assert np.array_equal(on[key].view(np.uint32), ro[key].view(np.uint32)), (i, key)
