@@ -96,6 +96,7 @@ SIGNATURES = {
     "azu_volume_upload": (C.c_int, [vp, vp, vp, vp]),
     "azu_volume_device_voxels": (vp, [vp]),
     "azu_volume_set_free_space_skipping": (C.c_int, [vp, C.c_int]),
+    "azu_volume_voxels_changed": (C.c_int, [vp]),
     "azu_volume_raycast_many": (C.c_int, [vp, fp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                                           C.c_int, vp, vp]),
     "azu_volume_point_cloud": (C.c_int, [vp, vp, vp, C.c_int64, C.POINTER(C.c_int64)]),

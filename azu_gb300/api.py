@@ -137,6 +137,13 @@ class TSDFVolume:
         check(self.lib.azu_volume_set_params(self.h, C.byref(p)), "set_params")
         self.params = p
 
+    def voxels_changed(self):
+        """After writing voxels through the device pointer: recompute the free-space flags."""
+        check(self.lib.azu_volume_voxels_changed(self.h), "voxels_changed")
+
+    def set_free_space_skipping(self, on: bool):
+        check(self.lib.azu_volume_set_free_space_skipping(self.h, int(bool(on))), "set_free_space_skipping")
+
     def integrate_gpu(self, d_depth, pose, K, W, H, min_depth, max_depth, d_rgb=None):
         _ready()
         check(self.lib.azu_volume_integrate(self.h, _ptr(d_depth), _ptr(d_rgb), _pose(pose), *map(float, K), W, H,

@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(kClassifyThreads) mc_classify_kernel(MeshVol v
     const VT* src_main = base + (in_main ? static_cast<size_t>(y0 + ty) * res + (x0 + tx) : 0);
     const VT* src_apron = base + (in_apron ? static_cast<size_t>(y0 + ay) * res + (x0 + ax) : 0);
     const int own = ty * kCodeW + tx, apron = ay * kCodeW + ax;
-    {
+    if (v.bricks) {
         // The tile's cubes have their base voxels in 4 x 1 x 4 bricks (x0, y0,
         // z0 are multiples of 8) and their corners in those bricks' aprons. In
         // a free brick every usable corner is >= 0.9995, so no cube there has a
@@ -782,7 +782,7 @@ extern "C" int azu_mesher_extract(azu_mesher* m, azu_volume* v, azu_mesh_info* i
     const unsigned long long ncubes = cr * cr * cr;
     if (ncubes == 0) { m->last = *info; return AZU_OK; }
     MeshVol mv{v->vox, v->p.format != AZU_TSDF_FP32 ? 1 : 0, v->color, res, v->p.voxel_size,
-               mk3(v->p.origin[0], v->p.origin[1], v->p.origin[2]), v->bricks, v->nb};
+               mk3(v->p.origin[0], v->p.origin[1], v->p.origin[2]), v->skip_free ? v->bricks : nullptr, v->nb};
     const size_t nblocks = static_cast<size_t>((ncubes + 255) / 256);
     {
         const size_t cap_before = m->counts_cap;

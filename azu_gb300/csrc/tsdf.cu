@@ -1992,6 +1992,12 @@ extern "C" int azu_volume_set_free_space_skipping(azu_volume* v, int on) {
 
 extern "C" void* azu_volume_device_voxels(azu_volume* v) { return v ? v->vox : nullptr; }
 
+extern "C" int azu_volume_voxels_changed(azu_volume* v) {
+    AZU_CHECK_ARG(v != nullptr, "volume is null");
+    AZU_TRY_CUDA(cudaSetDevice(v->device));
+    return rebuild_bricks(v, v->stream.s);
+}
+
 extern "C" int azu_volume_point_cloud(azu_volume* v, float* h_points, uint8_t* h_colors, int64_t capacity,
                                       int64_t* n_points) {
     AZU_CHECK_ARG(v != nullptr && n_points != nullptr, "null argument");

@@ -124,13 +124,20 @@ int azu_volume_get_stats(azu_volume* v, azu_volume_stats* s);
  * FP16 volumes convert on the device. Synchronous. */
 int azu_volume_download(azu_volume* v, float* h_tsdf, float* h_weight, float* h_color);
 int azu_volume_upload(azu_volume* v, const float* h_tsdf, const float* h_weight, const float* h_color);
-/* Free-space skipping in the raycast (on by default): samples whose 8 corners
- * are all unobserved or at tsdf >= 0.9995 are not loaded, only stepped over;
- * results are identical either way. For A/B timing. */
+/* Free-space skipping (on by default): the raycast does not load samples whose
+ * 8 corners are all unobserved or at tsdf >= 0.9995, and the marching cubes do
+ * not read tiles of such bricks; results are identical either way. For A/B
+ * timing. */
 int azu_volume_set_free_space_skipping(azu_volume* v, int on);
 /* TSDFVolume::getGPUVoxels (TSDFVolume.h:163): device voxel array (float2
- * {tsdf, weight} for FP32, uint32 {half, u16} for FP16). */
+ * {tsdf, weight} for FP32, uint32 {half, u16} for FP16). The free-space flags
+ * follow integrate, upload and reset; a caller that writes voxels through this
+ * pointer calls azu_volume_voxels_changed afterwards (on the volume's stream
+ * order), or turns free-space skipping off. */
 void* azu_volume_device_voxels(azu_volume* v);
+/* Recomputes the free-space flags from the voxels (stream-ordered). No
+ * reference counterpart: the reference's CPU and GPU paths keep no such flags. */
+int azu_volume_voxels_changed(azu_volume* v);
 
 /* The relocaliser's candidate renders (PipelineController::renderModel,
  * src/app/PipelineController.cpp:619-657, called per candidate by

@@ -219,3 +219,48 @@ def test_ray_start_map_near_and_inside_surfaces(cuda_lib, orc, c1_seq):
         for key in ("vertices", "normals"):
             assert np.array_equal(on[key].view(np.uint32), off[key].view(np.uint32)), (i, key)
             assert np.array_equal(on[key].view(np.uint32), ro[key].view(np.uint32)), (i, key)
+
+
+def test_voxels_written_through_the_device_pointer(cuda_lib, orc, c1_seq):
+    """Voxels written through azu_volume_device_voxels (here: a fused volume's
+    array copied into a fresh volume by the driver API) take effect in the
+    raycast and the marching cubes once azu_volume_voxels_changed has
+    recomputed the free-space flags, and with skipping off before that: the
+    same images and mesh as the source volume."""
+    import ctypes as C
+    import torch
+    from azu_gb300 import api, synth
+    s = c1_seq
+    prm = dict(s.volume, min_depth=s.min_depth, max_depth=s.max_depth)
+    prm.pop("format")
+    src = _gpu_volume(prm)
+    K = (s.fx, s.fy, s.cx, s.cy)
+    for k in range(6):
+        src.integrate(synth.mm_to_meters(s.depth_mm[k]), s.poses[k], K, s.width, s.height, s.min_depth,
+                      s.max_depth)
+    dst = _gpu_volume(prm)  # fresh: every brick flagged free
+    torch.cuda.synchronize()
+    drv = C.CDLL("libcuda.so.1")
+    drv.cuMemcpyDtoD_v2.argtypes = [C.c_uint64, C.c_uint64, C.c_size_t]
+    ps = src.lib.azu_volume_device_voxels(src.h)
+    pd = dst.lib.azu_volume_device_voxels(dst.h)
+    assert drv.cuMemcpyDtoD_v2(pd, ps, src.n * 8) == 0
+    torch.cuda.synchronize()
+    pose = s.poses[5]
+    want = src.raycast(pose, K, s.width, s.height)
+    dst.set_free_space_skipping(False)
+    off = dst.raycast(pose, K, s.width, s.height)
+    mc = api.MarchingCubes()
+    m_off = mc.extract(dst)
+    dst.set_free_space_skipping(True)
+    dst.voxels_changed()
+    on = dst.raycast(pose, K, s.width, s.height)
+    m_src = mc.extract(src)
+    m_on = mc.extract(dst)
+    for key in ("vertices", "normals"):
+        assert np.array_equal(off[key].view(np.uint32), want[key].view(np.uint32))
+        assert np.array_equal(on[key].view(np.uint32), want[key].view(np.uint32))
+    assert len(m_src["positions"]) > 0
+    for key, val in m_src.items():
+        if isinstance(val, np.ndarray):
+            assert np.array_equal(val, m_off[key]) and np.array_equal(val, m_on[key]), key
